@@ -1,0 +1,245 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 dense Goldbach verify path.
+
+Workload: production segments of 467.5M integers at 4e18 + k * 467.5e6, k
+drawn from seed 1 in [0, 1e5) (the reference's production segment shape);
+a step is one batch of --batch consecutive segments (default 8: one sieve
+pass over one HBM-resident class map, then per-segment exact p(n) of every
+even, prime / twin / gap statistics and the class-map hash). Successive
+steps take successive batches, so no step repeats work; the class map of a
+batch (125 MB for 8 segments) and the sieving primes exceed what one step
+reuses from L2 (inputs larger than L2, see config.l2).
+
+value  = evens verified per second over the timed steps, device time from
+         CUDA events on the launching stream (inputs resident in HBM).
+e2e    = the same metric through the C ABI as a caller uses it: two slots in
+         flight, gbc_enqueue_batch + gbc_collect, per-segment results copied
+         to host memory inside the timed region, wall clock.
+--impl reference times the reference's CPU algorithm (the oracle's
+restatement of tests/stats_ref.cpp, run on all host cores) on a bounded
+sample of the same workload.
+"""
+import argparse
+import json
+import os
+import random
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "goldbach-l0_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+SEG = 467_500_000
+METRIC = "G evens/s at 4e18, bit-exact stats"
+
+
+def workload_start():
+    k = random.Random(1).randrange(100000)
+    return 4 * 10**18 + k * SEG
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.rows, self.proc = [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.rows.append([x.strip() for x in ln.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def batches(start, nbatch, batch):
+    out = []
+    s = start
+    for _ in range(nbatch):
+        segs = []
+        for _ in range(batch):
+            segs.append((s, s + SEG - 2))
+            s += SEG
+        out.append(segs)
+    return out
+
+
+def cpu_baseline(evens, start):
+    import oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.stats_line(start, start + 2 * (evens - 1), oracle.MR, threads)
+    dt = time.perf_counter() - t0
+    return {"value": evens / dt / 1e9, "unit": "G evens/s", "cores": threads, "kind": "port",
+            "sample": f"{evens} evens from {start}: the oracle's restatement of tests/stats_ref.cpp "
+                      f"(Miller-Rabin p(n), primes, twins, gaps) on {threads} threads, {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    start = workload_start()
+    per_step = args.ref_evens
+    for i in range(args.warmup):
+        cpu_baseline(per_step // 10, start + 2 * per_step * i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        cpu_baseline(per_step, start + 2 * per_step * (args.warmup + i))
+    dt = time.perf_counter() - t0
+    v = per_step * args.steps / dt / 1e9
+    cores = os.cpu_count() or 1
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "G evens/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"{per_step} evens per step of the production segments at {start}",
+                       "segment": SEG},
+            "cpu_baseline": {"value": v, "unit": "G evens/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} evens per step, Miller-Rabin per even (tests/stats_ref.cpp's "
+                                       f"algorithm, restated in oracle/gb_oracle.c), {cores} threads"},
+            "e2e": {"value": v, "unit": "G evens/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=12)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--tile-log2", type=int, default=0)
+    ap.add_argument("--p-mid", type=int, default=0)
+    ap.add_argument("--ref-evens", type=int, default=1_000_000)
+    ap.add_argument("--cpu-evens", type=int, default=4_000_000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
+        print(json.dumps({"error": "one GPU per process: run N independent replicas for N > 1"}))
+        return 2
+    import gbc
+
+    start = workload_start()
+    nb = args.warmup + args.steps
+    allb = batches(start, 2 * nb, args.batch)
+    limit = allb[-1][-1][1]
+    evens_per_step = sum((e - s) // 2 + 1 for s, e in allb[0])
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=args.batch, tile_log2=args.tile_log2,
+                     p_mid=args.p_mid) as ctx:
+        # ---- device-time value: one slot, steps back to back, CUDA events of the launching stream
+        for i in range(args.warmup):
+            ctx.enqueue_batch(0, allb[i], limit)
+            ctx.collect(0, len(allb[i]))
+        launches0 = ctx.launches()
+        stage = {"tile": 0.0, "large": 0.0, "check": 0.0, "count": 0.0}
+        dev_ms = 0.0
+        with Clocks() as clk:
+            t0 = time.perf_counter()
+            for i in range(args.steps):
+                b = allb[args.warmup + i]
+                ctx.enqueue_batch(0, b, limit)
+                _, t = ctx.collect(0, len(b))
+                dev_ms += t.ms_total
+                stage["tile"] += t.ms_tile
+                stage["large"] += t.ms_large
+                stage["check"] += t.ms_check
+                stage["count"] += t.ms_count
+            wall = time.perf_counter() - t0
+        launches = ctx.launches() - launches0
+        value = evens_per_step * args.steps / (dev_ms / 1e3) / 1e9
+        # ---- e2e: the caller's loop, two slots in flight, results to host memory
+        off = nb
+        for i in range(2):
+            ctx.enqueue_batch(i, allb[off + i], limit)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            slot = i & 1
+            res, _ = ctx.collect(slot, len(allb[off + i]))
+            if i + 2 < args.steps:
+                ctx.enqueue_batch(slot, allb[off + i + 2], limit)
+        e2e_wall = time.perf_counter() - t0
+        e2e = evens_per_step * args.steps / e2e_wall / 1e9
+        import ctypes
+        d2h = args.batch * ctypes.sizeof(gbc.SegmentResult)
+    hbm, kind = peaks()
+    # dominant stage and its algorithmic HBM bytes per launch
+    dom = max(stage, key=stage.get)
+    seg_map_bytes = 8 * (SEG / 30) / 8                  # class-map bits of a segment, as bytes
+    nprime = 98_222_287                                  # odd primes <= 2.0e9 (sqrt of the workload)
+    alg = {"tile": seg_map_bytes * args.batch,           # one write of the batch's map
+           "large": 4 * nprime + 2 * 4 * 30_800_000 * args.batch / 8 * 0,  # prime stream (marks hit L2)
+           "check": seg_map_bytes * args.batch,          # one read of the map
+           "count": seg_map_bytes * args.batch}[dom]
+    per_launch_ms = stage[dom] / args.steps
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"production segments of {SEG} integers from {start} (4e18 + k*467.5e6, k seed 1), "
+                               f"{args.batch} segments per step", "segments_per_step": args.batch,
+                   "evens_per_step": evens_per_step, "l2": "inputs larger than L2 (class map 125 MB + primes "
+                                                           "393 MB per step)",
+                   "tile_log2": ctx.cfg.tile_log2, "p_mid": ctx.cfg.p_mid},
+        "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+        "wall_ms_per_step": wall * 1e3 / args.steps,
+        "e2e": {"value": e2e, "unit": "G evens/s", "h2d_bytes_per_step": 16 * args.batch,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_evens, start)
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

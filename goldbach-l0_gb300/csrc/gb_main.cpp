@@ -1,0 +1,140 @@
+// gb_main.cpp -- goldbach_gb300: command-line front end of the GB300 dense
+// verify path. Flags and exit codes follow the reference's CLI
+// (src/main.cpp:28-86, 265-411): --start, --limit (decimal or e-notation,
+// strict), --segment, --csv; exit 0 = PASS, 1 = verification or GPU
+// failure, 2 = usage error. --batch sets the segments per sieve batch;
+// --stats prints the run's stats_ref line (tests/stats_ref.cpp:97-189).
+#include <cinttypes>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "gb_run.hpp"
+
+namespace {
+
+// Strict count parser: digits, or <digits>[.<digits>]e<digits> that is an
+// exact integer (the reference's parse_count, src/main.cpp:28-57).
+bool parse_count(const char *s, uint64_t &out)
+{
+    if (!s || !*s) return false;
+    const char *e = std::strchr(s, 'e');
+    if (!e) e = std::strchr(s, 'E');
+    if (!e) {
+        uint64_t v = 0;
+        for (const char *p = s; *p; ++p) {
+            if (*p < '0' || *p > '9') return false;
+            const uint64_t d = uint64_t(*p - '0');
+            if (v > (UINT64_MAX - d) / 10) return false;
+            v = v * 10 + d;
+        }
+        out = v;
+        return true;
+    }
+    // mantissa digits with an optional point, exponent digits
+    std::string mant(s, e), digits;
+    int frac = 0;
+    bool point = false;
+    for (char c : mant) {
+        if (c == '.') {
+            if (point) return false;
+            point = true;
+        } else if (c >= '0' && c <= '9') {
+            digits += c;
+            if (point) ++frac;
+        } else return false;
+    }
+    if (digits.empty()) return false;
+    int ex = 0;
+    const char *x = e + 1;
+    if (!*x) return false;
+    for (; *x; ++x) {
+        if (*x < '0' || *x > '9' || ex > 40) return false;
+        ex = ex * 10 + (*x - '0');
+    }
+    ex -= frac;
+    if (ex < 0) return false;
+    uint64_t v = 0;
+    for (char c : digits) {
+        const uint64_t d = uint64_t(c - '0');
+        if (v > (UINT64_MAX - d) / 10) return false;
+        v = v * 10 + d;
+    }
+    for (int i = 0; i < ex; ++i) {
+        if (v > UINT64_MAX / 10) return false;
+        v *= 10;
+    }
+    out = v;
+    return true;
+}
+
+int usage()
+{
+    std::fprintf(stderr,
+                 "usage: goldbach_gb300 [--start N] --limit N [--segment N] [--batch N] [--csv] [--stats] "
+                 "[--verbose]\n");
+    return 2;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8;
+    bool csv = false, stats = false, verbose = false;
+    for (int i = 1; i < argc; ++i) {
+        const std::string a = argv[i];
+        auto val = [&](uint64_t &dst) {
+            if (i + 1 >= argc || !parse_count(argv[i + 1], dst)) return false;
+            ++i;
+            return true;
+        };
+        if (a == "--start") {
+            if (!val(start)) return usage();
+        } else if (a == "--limit") {
+            if (!val(limit)) return usage();
+        } else if (a == "--segment") {
+            if (!val(segment)) return usage();
+        } else if (a == "--batch") {
+            if (!val(batch) || !batch || batch > 256) return usage();
+        } else if (a == "--csv") csv = true;
+        else if (a == "--stats") stats = true;
+        else if (a == "--verbose") verbose = true;
+        else return usage();
+    }
+    if (!limit) return usage();
+    if (start > limit) {
+        std::fprintf(stderr, "empty range: start %" PRIu64 " > limit %" PRIu64 "\n", start, limit);
+        return 2;
+    }
+    if (limit > GBC_MAX_LIMIT) {
+        std::fprintf(stderr, "limit %" PRIu64 " is above the supported maximum 2^64 - 2^40\n", limit);
+        return 1;
+    }
+    try {
+        const gb::RunStats st = gb::run_gpu(limit, segment, verbose, start, uint32_t(batch));
+        const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
+        if (csv)
+            std::printf("result=PASS,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64 ",segments=%" PRIu64
+                        ",leftovers=%" PRIu64 ",pmax=%" PRIu64 ",primes=%" PRIu64 ",twins=%" PRIu64
+                        ",gpu_s=%.6f,total_s=%.6f,evens_per_sec=%.6e,sieve_s=%.6f,large_s=%.6f,verify_s=%.6f,"
+                        "count_s=%.6f\n",
+                        st.start, st.limit, st.evens, st.segments, st.leftovers, st.pmax, st.primes, st.twins,
+                        st.gpu_seconds, st.wall_seconds, eps, st.tile_ms / 1e3, st.large_ms / 1e3,
+                        st.check_ms / 1e3, st.count_ms / 1e3);
+        else
+            std::printf("PASS: every even n in [%" PRIu64 ", %" PRIu64 "] is a sum of two primes "
+                        "(%" PRIu64 " evens, largest p(n) %" PRIu64 ", %.3f G evens/s)\n",
+                        st.start, st.limit, st.evens, st.pmax, eps / 1e9);
+        if (stats) std::printf("%s\n", st.stats_line.c_str());
+        return 0;
+    } catch (const gb::GbcError &e) {
+        std::fprintf(stderr, "FAIL: %s\n", e.what());
+        return e.code == GBC_E_ARG ? 2 : 1;
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "FAIL: %s\n", e.what());
+        return 1;
+    }
+}

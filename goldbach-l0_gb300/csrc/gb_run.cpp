@@ -1,0 +1,400 @@
+// gb_run.cpp -- the run driver above the C ABI: gbc_verify_range and the
+// C++ gb::run_gpu of include/gb_run.hpp.
+//
+// Follows the reference's DenseRun (src/verifier.cpp:2487-2569): segments
+// of segment_even integers, two slots in flight (batch k + 1 is enqueued
+// before batch k is collected), per-segment results merged into run
+// statistics with the rules of GoldbachStats (include/gstats.hpp:507-772:
+// sums, the smallest first occurrence, the largest gap with the smallest
+// lower prime on ties, gaps >= 700 with count and first lower prime), fail
+// closed on any error. The statistics are printed in the format of the
+// reference's CPU oracle tests/stats_ref.cpp:97-189, so a run can be diffed
+// against it line for line.
+#include "gb_run.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cinttypes>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace gb {
+
+namespace {
+
+using u128 = unsigned __int128;
+
+std::string u128_str(u128 v)
+{
+    std::string s;
+    do {
+        s.insert(s.begin(), char('0' + int(v % 10)));
+        v /= 10;
+    } while (v);
+    return s;
+}
+
+std::vector<uint16_t> candidates()
+{
+    std::vector<uint16_t> c(GBC_NCAND);
+    gbc_candidates(c.data(), GBC_NCAND);
+    return c;
+}
+
+}  // namespace
+
+RunAccumulator::RunAccumulator(uint64_t start, uint64_t limit) : start_(start), limit_(limit)
+{
+    cand_ = candidates();
+    hist_.assign(size_t(GBC_NCLASS) * GBC_NCAND, 0);
+    first_.assign(GBC_NCAND, 0);
+    ghist_.assign(GBC_GBINS, 0);
+    evens_ = (limit - start) / 2 + 1;
+    // q = 3 and q = 5 are not in the class map (multiples of 3 and 5): their
+    // counts, twins and gaps come from here, exactly, for a run that starts
+    // low enough to count them.
+    const uint64_t lo = start + 1, hi = limit - 1;
+    auto in = [&](uint64_t q) { return q >= lo && q <= hi; };
+    if (in(3)) {
+        primes30_[3] += 1;
+        add_gap(1, 3);
+        if (3 + 2 <= limit - 1) twins30_[3] += 1;
+    }
+    if (in(5)) {
+        primes30_[5] += 1;
+        add_gap(2, 5);
+        if (5 + 2 <= limit - 1) twins30_[5] += 1;
+    }
+    if (in(7)) add_gap(2, 7);  // 7's predecessor 5 is not in the map
+}
+
+void RunAccumulator::add_gap(uint64_t g, uint64_t upper)
+{
+    if (g / 2 >= GBC_GBINS) throw std::runtime_error("gap above the histogram range");
+    if (g & 1) odd_gaps_ += 1;  // 3 - 2: not an entry of the even-gap histogram
+    else ghist_[g / 2] += 1;
+    note_gap_max(g, upper - g);
+    if (g >= GBC_GTAIL) note_tail(uint32_t(g), 1, upper - g);
+}
+
+void RunAccumulator::note_gap_max(uint64_t g, uint64_t lower)
+{
+    if (g > gmax_ || (g == gmax_ && g && lower < gmax_lo_)) {
+        gmax_ = g;
+        gmax_lo_ = lower;
+    }
+}
+
+void RunAccumulator::note_tail(uint32_t g, uint64_t c, uint64_t lower)
+{
+    auto &t = tail_[g];
+    if (!t.first || lower < t.second) t.second = lower;
+    t.first += c;
+}
+
+void RunAccumulator::add_pn(uint64_t n, uint64_t p)
+{
+    auto &b = beyond_[p];
+    if (!b.first || n < b.second) b.second = n;
+    b.first += 1;
+}
+
+void RunAccumulator::add_segment(const gbc_segment_result &r)
+{
+    for (int cr = 0; cr < GBC_NCLASS; ++cr)
+        for (int i = 0; i < GBC_NCAND; ++i) hist_[size_t(cr) * GBC_NCAND + i] += r.hist[cr][i];
+    for (int i = 0; i < GBC_NCAND; ++i)
+        if (r.first[i] != 0xFFFFFFFFu) {
+            const uint64_t n = r.seg_start + 2ull * r.first[i];
+            if (!first_[i] || n < first_[i]) first_[i] = n;
+        }
+    for (uint32_t i = 0; i < r.nleft; ++i) {
+        if (!r.left_p[i])
+            throw std::runtime_error("no Goldbach partition found for n = " + std::to_string(r.left_n[i]) +
+                                     " (reported, never passed)");
+        add_pn(r.left_n[i], r.left_p[i]);
+        ++leftovers_;
+    }
+    static const int res[8] = {1, 7, 11, 13, 17, 19, 23, 29};
+    for (int k = 0; k < 8; ++k) primes30_[res[k]] += r.primes30[k];
+    twins30_[11] += r.twins[0];
+    twins30_[17] += r.twins[1];
+    twins30_[29] += r.twins[2];
+    for (int b = 0; b < GBC_GBINS; ++b) ghist_[b] += r.ghist[b];
+    if (r.gmax_key) {
+        const uint64_t g = r.gmax_key >> 32;
+        const uint64_t lower = r.hash_lo + (0xFFFFFFFFull - (r.gmax_key & 0xFFFFFFFFull));
+        note_gap_max(g, lower);
+    }
+    for (uint32_t i = 0; i < r.ntail; ++i) note_tail(r.tail_g[i], 1, r.tail_lo[i]);
+    uint64_t tcount = 0;
+    for (int b = GBC_GTAIL / 2; b < GBC_GBINS; ++b) tcount += r.ghist[b];
+    if (tcount != r.ntail) throw std::runtime_error("gap tail list does not match the gap histogram");
+    segments_ += 1;
+}
+
+uint64_t RunAccumulator::primes() const
+{
+    uint64_t s = 0;
+    for (uint64_t v : primes30_) s += v;
+    return s;
+}
+
+uint64_t RunAccumulator::twins() const
+{
+    uint64_t s = 0;
+    for (uint64_t v : twins30_) s += v;
+    return s;
+}
+
+uint64_t RunAccumulator::pmax() const
+{
+    uint64_t m = 0;
+    for (int i = 0; i < GBC_NCAND; ++i) {
+        uint64_t c = 0;
+        for (int cr = 0; cr < GBC_NCLASS; ++cr) c += hist_[size_t(cr) * GBC_NCAND + i];
+        if (c) m = cand_[i];
+    }
+    for (auto &b : beyond_) m = std::max(m, b.first);
+    return m;
+}
+
+uint64_t RunAccumulator::gap_count() const
+{
+    uint64_t n = odd_gaps_;
+    for (uint64_t v : ghist_) n += v;
+    return n;
+}
+
+std::string RunAccumulator::stats_ref_line() const
+{
+    std::string o;
+    char b[128];
+    std::snprintf(b, sizeof b, "evens=%" PRIu64 " pmax=%" PRIu64 " primes=%" PRIu64 " twins=%" PRIu64 " primes30=",
+                  evens_, pmax(), primes(), twins());
+    o += b;
+    static const int u[8] = {1, 7, 11, 13, 17, 19, 23, 29};
+    for (int i = 0; i < 8; ++i) {
+        std::snprintf(b, sizeof b, "%s%" PRIu64, i ? "," : "", primes30_[u[i]]);
+        o += b;
+    }
+    std::snprintf(b, sizeof b, " twins30=%" PRIu64 ",%" PRIu64 ",%" PRIu64, twins30_[11], twins30_[17], twins30_[29]);
+    o += b;
+    // first occurrences of every p(n) value, ascending p
+    std::map<uint64_t, uint64_t> firsts;
+    std::vector<uint64_t> tot(GBC_NCAND, 0);
+    for (int i = 0; i < GBC_NCAND; ++i) {
+        for (int cr = 0; cr < GBC_NCLASS; ++cr) tot[i] += hist_[size_t(cr) * GBC_NCAND + i];
+        if (tot[i]) firsts[cand_[i]] = first_[i];
+    }
+    for (auto &bp : beyond_) {
+        auto it = firsts.find(bp.first);
+        if (it == firsts.end() || bp.second.second < it->second) firsts[bp.first] = bp.second.second;
+    }
+    o += " first=";
+    bool f1 = true;
+    for (auto &f : firsts) {
+        std::snprintf(b, sizeof b, "%s%" PRIu64 ":%" PRIu64, f1 ? "" : ";", f.first, f.second);
+        o += b;
+        f1 = false;
+    }
+    o += " hist=";
+    size_t last = 0;
+    for (size_t i = 0; i < tot.size(); ++i) {
+        uint64_t c = tot[i];
+        auto it = beyond_.find(cand_[i]);
+        if (it != beyond_.end()) c += it->second.first;
+        if (c) last = i + 1;
+    }
+    for (size_t i = 0; i < last; ++i) {
+        if (i) o += ",";
+        uint64_t c = tot[i];
+        auto it = beyond_.find(cand_[i]);
+        if (it != beyond_.end()) c += it->second.first;
+        if (c) o += std::to_string(c);
+    }
+    // gaps: count, moments, largest, tail, histogram
+    u128 m[4] = {odd_gaps_, odd_gaps_, odd_gaps_, odd_gaps_};  // g = 1
+    uint64_t n = odd_gaps_;
+    for (size_t i = 0; i < ghist_.size(); ++i) {
+        const u128 c = ghist_[i], g = 2 * i, g2 = g * g;
+        n += ghist_[i];
+        m[0] += c * g;
+        m[1] += c * g2;
+        m[2] += c * g2 * g;
+        m[3] += c * g2 * g2;
+    }
+    o += " gaps=" + std::to_string(n) + " gmom=" + u128_str(m[0]) + "," + u128_str(m[1]) + "," + u128_str(m[2]) +
+         "," + u128_str(m[3]);
+    std::snprintf(b, sizeof b, " gmax=%" PRIu64 ":%" PRIu64 " gtail=", gmax_, gmax_lo_);
+    o += b;
+    if (tail_.empty()) o += "-";
+    bool t1 = true;
+    for (auto &t : tail_) {
+        std::snprintf(b, sizeof b, "%s%u:%" PRIu64 ":%" PRIu64, t1 ? "" : ";", t.first, t.second.first,
+                      t.second.second);
+        o += b;
+        t1 = false;
+    }
+    o += " ghist=";
+    size_t hb = 0;
+    for (size_t i = 0; i < ghist_.size(); ++i)
+        if (ghist_[i]) hb = i + 1;
+    for (size_t i = 0; i < hb; ++i) {
+        if (i) o += ",";
+        if (ghist_[i]) o += std::to_string(ghist_[i]);
+    }
+    return o;
+}
+
+std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_t limit, uint64_t segment_even)
+{
+    std::vector<std::pair<uint64_t, uint64_t>> segs;
+    uint64_t s = start;
+    while (s <= limit) {
+        uint64_t len = segment_even;
+        // the lowest evens reach q < 7 and take the generic checker: keep
+        // that segment short
+        if (s < GBC_MAX_CAND + 7) len = std::min<uint64_t>(len, 65536);
+        const uint64_t e = limit - s <= len - 2 ? limit : s + len - 2;
+        segs.push_back({s, e});
+        if (e >= limit) break;
+        s = e + 2;
+    }
+    return segs;
+}
+
+namespace {
+
+struct CtxCloser {
+    void operator()(gbc_ctx *c) const { gbc_destroy(c); }
+};
+
+void check(gbc_ctx *ctx, int rc, const char *what)
+{
+    if (rc != GBC_OK) throw GbcError(rc, std::string(what) + ": " + gbc_last_error(ctx));
+}
+
+}  // namespace
+
+RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
+                   uint16_t *pn, RunAccumulator *acc_out)
+{
+    RunStats st;
+    const auto t0 = std::chrono::steady_clock::now();
+    if (start < 4) start = 4;
+    if (start & 1) start += 1;
+    limit &= ~uint64_t(1);
+    if (limit < 6 || start > limit) throw GbcError(GBC_E_ARG, "no even n >= 4 in [start, limit] (need limit >= 6)");
+    st.start = start;
+    st.limit = limit;
+    const auto segs = plan_segments(start, limit, segment_even);
+    RunAccumulator acc(start, limit);
+    std::vector<std::vector<std::pair<uint64_t, uint64_t>>> batches;
+    for (size_t i = 0; i < segs.size(); i += max_batch)
+        batches.emplace_back(segs.begin() + i, segs.begin() + std::min(segs.size(), i + max_batch));
+    std::vector<gbc_segment_result> out[2];
+    double gpu_ms = 0;
+    auto collect = [&](size_t b) {
+        const int slot = int(b & 1);
+        const int n = int(batches[b].size());
+        out[slot].resize(n);
+        gbc_batch_times tm{};
+        check(ctx, gbc_collect(ctx, slot, out[slot].data(), n, &tm, 600000), "collect");
+        gpu_ms += tm.ms_total;
+        st.tile_ms += tm.ms_tile;
+        st.large_ms += tm.ms_large;
+        st.check_ms += tm.ms_check;
+        st.count_ms += tm.ms_count;
+        for (int i = 0; i < n; ++i) {
+            acc.add_segment(out[slot][i]);
+            if (pn) {
+                const auto &r = out[slot][i];
+                check(ctx, gbc_copy_pn(ctx, slot, i, pn + (r.seg_start - start) / 2, r.evens), "copy p(n)");
+            }
+        }
+    };
+    for (size_t b = 0; b < batches.size(); ++b) {
+        std::vector<uint64_t> bounds;
+        for (auto &s : batches[b]) {
+            bounds.push_back(s.first);
+            bounds.push_back(s.second);
+        }
+        check(ctx, gbc_enqueue_batch(ctx, int(b & 1), bounds.data(), nullptr, int(batches[b].size()), limit),
+              "enqueue");
+        if (b) collect(b - 1);
+    }
+    collect(batches.size() - 1);
+    st.evens = acc.evens();
+    st.segments = segs.size();
+    st.batches = batches.size();
+    st.leftovers = acc.leftovers();
+    st.pmax = acc.pmax();
+    st.primes = acc.primes();
+    st.twins = acc.twins();
+    st.gpu_seconds = gpu_ms / 1e3;
+    st.wall_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st.stats_line = acc.stats_ref_line();
+    if (acc_out) *acc_out = acc;
+    return st;
+}
+
+RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even, uint32_t max_batch,
+                 uint16_t *pn)
+{
+    gbc_config cfg{};
+    cfg.limit = limit & ~uint64_t(1);
+    cfg.segment_even = segment_even;
+    cfg.max_batch = max_batch;
+    cfg.want_pn = pn ? 1 : 0;
+    gbc_ctx *raw = nullptr;
+    const int rc = gbc_create(&cfg, &raw);
+    std::unique_ptr<gbc_ctx, CtxCloser> ctx(raw);
+    if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_create: ") + gbc_last_error(raw));
+    RunStats st = run_range(ctx.get(), start_even, limit, segment_even ? segment_even : GBC_DEFAULT_SEGMENT,
+                            max_batch ? max_batch : 8, pn, nullptr);
+    if (verbose)
+        std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",
+                     st.start, st.limit, st.segments, st.gpu_seconds, st.wall_seconds);
+    return st;
+}
+
+}  // namespace gb
+
+extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gbc_run_result *res, char *line,
+                                uint64_t line_cap, uint16_t *pn)
+{
+    if (!ctx) return GBC_E_ARG;
+    try {
+        gbc_config cfg{};
+        if (gbc_get_config(ctx, &cfg) != GBC_OK) return GBC_E_ARG;
+        gb::RunStats st = gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, pn, nullptr);
+        if (res) {
+            res->start = st.start;
+            res->limit = st.limit;
+            res->evens = st.evens;
+            res->segments = st.segments;
+            res->batches = st.batches;
+            res->leftovers = st.leftovers;
+            res->pmax = st.pmax;
+            res->primes = st.primes;
+            res->twins = st.twins;
+            res->gpu_seconds = st.gpu_seconds;
+            res->wall_seconds = st.wall_seconds;
+        }
+        if (line && line_cap) {
+            if (st.stats_line.size() + 1 > line_cap) return GBC_E_OVERFLOW;
+            std::memcpy(line, st.stats_line.c_str(), st.stats_line.size() + 1);
+        }
+        return GBC_OK;
+    } catch (const gb::GbcError &e) {
+        return e.code;
+    } catch (const std::exception &) {
+        return GBC_E_DEVICE;
+    }
+}

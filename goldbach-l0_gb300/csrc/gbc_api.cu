@@ -1,0 +1,503 @@
+// gbc_api.cu -- the per-segment C ABI (include/gbc.h): context, tables,
+// slots, batch enqueue and bounded-wait collect.
+//
+// Replaces the reference's Level Zero run driver plumbing
+// (src/verifier.cpp:346-354 construction, 633-692 base primes, 853-1001
+// buffer sizing, 1361-1440 table upload, 1741-2146 per-segment enqueue,
+// 2402-2444 collect) for one CUDA device: two slots, each with its own
+// stream, class map, first-bit table and result area; a batch is enqueued
+// on a slot and collected later, so the host's work on batch k overlaps the
+// GPU's work on batch k + 1.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gbc_common.cuh"
+#include "gbc_internal.h"
+
+namespace {
+
+constexpr uint32_t kGroupPrimes[gbk::kNumGroups][3] = {{7, 11, 13},  {17, 19, 23}, {29, 31, 1}, {37, 41, 1},
+                                                       {43, 47, 1}, {53, 59, 1},   {61, 67, 1}};
+
+uint64_t isqrt64(uint64_t n)
+{
+    uint64_t r = 0;
+    for (int b = 31; b >= 0; --b) {
+        const uint64_t t = r | (1ull << b);
+        if (t <= n / t) r = t;
+    }
+    return r;
+}
+
+uint32_t inv_mod_small(uint32_t a, uint32_t m)  // a^-1 mod m, 0 if none
+{
+    int64_t t = 0, nt = 1, r = m, nr = a % m;
+    while (nr) {
+        const int64_t q = r / nr;
+        int64_t x = t - q * nt;
+        t = nt;
+        nt = x;
+        x = r - q * nr;
+        r = nr;
+        nr = x;
+    }
+    if (r != 1) return 0;
+    if (t < 0) t += m;
+    return uint32_t(t);
+}
+
+}  // namespace
+
+// The odd primes <= n (n < 2^32), by a segmented sieve on all host threads.
+std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n)
+{
+    std::vector<uint32_t> out;
+    if (n < 3) return out;
+    const uint64_t r = isqrt64(n);
+    std::vector<uint8_t> comp(r + 1, 0);
+    std::vector<uint32_t> small;
+    for (uint64_t i = 2; i <= r; ++i)
+        if (!comp[i]) {
+            if (i & 1) small.push_back(uint32_t(i));
+            for (uint64_t k = i * i; k <= r; k += i) comp[k] = 1;
+        }
+    const uint64_t nodd = (n - 1) / 2;  // odd numbers 3..n: index i <-> 2 i + 3
+    const uint64_t blk = 1u << 21;
+    const uint64_t nblk = (nodd + blk - 1) / blk;
+    unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+    if (nt > nblk) nt = unsigned(nblk ? nblk : 1);
+    std::vector<std::vector<uint32_t>> parts(nt);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            std::vector<uint8_t> buf(blk);
+            for (uint64_t b = nblk * t / nt; b < nblk * (t + 1) / nt; ++b) {
+                const uint64_t i0 = b * blk, i1 = std::min(nodd, i0 + blk);
+                std::fill(buf.begin(), buf.begin() + (i1 - i0), 1);
+                const uint64_t v0 = 2 * i0 + 3, v1 = 2 * (i1 - 1) + 3;
+                for (uint32_t p : small) {
+                    const uint64_t pp = uint64_t(p) * p;
+                    if (pp > v1) break;
+                    uint64_t s = pp;
+                    if (s < v0) {
+                        s = (v0 + p - 1) / p * p;
+                        if (!(s & 1)) s += p;
+                    }
+                    for (uint64_t v = s; v <= v1; v += 2ull * p) buf[(v - 3) / 2 - i0] = 0;
+                }
+                for (uint64_t i = i0; i < i1; ++i)
+                    if (buf[i - i0]) parts[t].push_back(uint32_t(2 * i + 3));
+            }
+        });
+    for (auto &x : th) x.join();
+    size_t tot = 0;
+    for (auto &p : parts) tot += p.size();
+    out.reserve(tot);
+    for (auto &p : parts) out.insert(out.end(), p.begin(), p.end());
+    return out;
+}
+
+static int fail(gbc_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        const cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(ctx, GBC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+extern "C" int gbc_candidates(uint16_t *out, int cap)
+{
+    std::vector<uint32_t> p = gbh_odd_primes_upto(GBC_MAX_CAND);
+    const int n = int(p.size());
+    for (int i = 0; i < n && i < cap; ++i) out[i] = uint16_t(p[i]);
+    return n;
+}
+
+static int slot_alloc(gbc_ctx *ctx, Slot &s)
+{
+    CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    for (auto &e : s.ev) CK(cudaEventCreate(&e));
+    CK(cudaMalloc(&s.map, size_t(8) * ctx->wpc_cap * 4 + kMapPadBytes));
+    CK(cudaMemset(s.map, 0, size_t(8) * ctx->wpc_cap * 4 + kMapPadBytes));
+    CK(cudaMalloc(&s.xfirst, std::max<size_t>(size_t(8) * ctx->n_mid * 4, 4)));
+    CK(cudaMalloc(&s.res, size_t(ctx->cfg.max_batch) * sizeof(gbc_segment_result)));
+    CK(cudaMalloc(&s.err, 4));
+    if (ctx->cfg.want_pn) {
+        s.pn_stride = ctx->cfg.segment_even / 2 + 1;
+        CK(cudaMalloc(&s.pn, size_t(ctx->cfg.max_batch) * s.pn_stride * 2));
+    }
+    return GBC_OK;
+}
+
+extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
+{
+    if (!out) return GBC_E_ARG;
+    *out = nullptr;
+    gbc_ctx *ctx = new (std::nothrow) gbc_ctx();
+    if (!ctx) return GBC_E_ARG;
+    gbc_config cfg{};
+    if (cfg_in) cfg = *cfg_in;
+    if (!cfg.limit) cfg.limit = 100000000ull;
+    if (!cfg.segment_even) cfg.segment_even = GBC_DEFAULT_SEGMENT;
+    if (cfg.segment_even & 1) cfg.segment_even += 1;
+    if (!cfg.max_batch) cfg.max_batch = 8;
+    if (!cfg.tile_log2) cfg.tile_log2 = 20;
+    if (!cfg.p_mid) cfg.p_mid = 1u << 22;
+    int rc = GBC_OK;
+    if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
+    else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
+        rc = fail(ctx, GBC_E_ARG, "segment_even outside [1000, 2^33]");
+    else if (cfg.max_batch > 256) rc = fail(ctx, GBC_E_ARG, "max_batch above 256");
+    else if (cfg.tile_log2 < 14 || cfg.tile_log2 > 20) rc = fail(ctx, GBC_E_ARG, "tile_log2 outside [14, 20]");
+    else if (cfg.p_mid < 128) rc = fail(ctx, GBC_E_ARG, "p_mid below 128");
+    else if (uint64_t(cfg.max_batch) * cfg.segment_even / 30 > (1ull << 31))
+        rc = fail(ctx, GBC_E_ARG, "max_batch * segment_even / 30 must stay below 2^31 class bits");
+    if (rc) {
+        *out = ctx;  // let the caller read the message, then destroy
+        return rc;
+    }
+    ctx->cfg = cfg;
+    ctx->err.clear();
+    cudaError_t e = cudaSetDevice(cfg.device);
+    if (e != cudaSuccess) {
+        *out = ctx;
+        return fail(ctx, GBC_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    }
+    int dev = cfg.device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (ctx->sm_count <= 0) ctx->sm_count = 1;
+
+    // sieving primes: every odd prime <= floor(sqrt(limit + 3)) + 16, saturated below 2^32
+    // (the reference's base_prime_bound, include/primes.hpp:222-225)
+    const double rt = std::sqrt(double(cfg.limit + 3)) + 16.0;
+    const uint64_t bound = rt >= 4294967295.0 ? 0xFFFFFFFFull : uint64_t(rt);
+    ctx->primes = gbh_odd_primes_upto(std::max<uint64_t>(bound, 127));
+    const auto &pr = ctx->primes;
+    ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
+    ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());
+    const uint32_t tb = 1u << cfg.tile_log2, tw = tb / 32;
+    ctx->i_warp = uint32_t(std::lower_bound(pr.begin(), pr.end(), std::max(tb / 64, 72u)) - pr.begin());
+    if (ctx->i_warp > ctx->n_mid) ctx->i_warp = ctx->n_mid;
+    std::vector<uint32_t> magic(ctx->n_mid);
+    for (uint32_t i = 0; i < ctx->n_mid; ++i) magic[i] = uint32_t((1ull << 32) / pr[i]);
+
+    // pattern groups (primes 7..67): canonical bit y = (y mod P coprime to P)
+    std::vector<uint32_t> pat;
+    for (int g = 0; g < gbk::kNumGroups; ++g) {
+        uint32_t P = 1;
+        for (int j = 0; j < 3; ++j) P *= kGroupPrimes[g][j];
+        const uint32_t words = (P + 64 + 31) / 32 + 1;
+        ctx->gi.P[g] = P;
+        ctx->gi.off[g] = uint32_t(pat.size());
+        ctx->gi.inv30[g] = inv_mod_small(30 % P, P);
+        for (uint32_t wd = 0; wd < words; ++wd) {
+            uint32_t v = 0;
+            for (uint32_t b = 0; b < 32; ++b) {
+                const uint32_t y = (wd * 32 + b) % P;
+                bool keep = true;
+                for (int j = 0; j < 3; ++j)
+                    if (kGroupPrimes[g][j] > 1 && y % kGroupPrimes[g][j] == 0) keep = false;
+                if (keep) v |= 1u << b;
+            }
+            pat.push_back(v);
+        }
+    }
+    ctx->gi.words = uint32_t(pat.size());
+    // multiplier skip bits and inverses (mod 1001, mod 7429)
+    std::vector<uint32_t> skip((gbk::kSkip1 + 31) / 32 + (gbk::kSkip2 + 31) / 32, 0);
+    std::vector<uint16_t> inv(gbk::kSkip1 + gbk::kSkip2, 0);
+    for (uint32_t m = 0; m < gbk::kSkip1; ++m) {
+        if (m % 7 == 0 || m % 11 == 0 || m % 13 == 0) skip[m / 32] |= 1u << (m % 32);
+        inv[m] = uint16_t(inv_mod_small(m, gbk::kSkip1));
+    }
+    const uint32_t w1 = (gbk::kSkip1 + 31) / 32;
+    for (uint32_t m = 0; m < gbk::kSkip2; ++m) {
+        if (m % 17 == 0 || m % 19 == 0 || m % 23 == 0) skip[w1 + m / 32] |= 1u << (m % 32);
+        inv[gbk::kSkip1 + m] = uint16_t(inv_mod_small(m, gbk::kSkip2));
+    }
+    // candidates and their per-class lists (useful: r - p coprime to 30)
+    std::vector<uint32_t> c32 = gbh_odd_primes_upto(GBC_MAX_CAND);
+    if (c32.size() != GBC_NCAND) {
+        *out = ctx;
+        return fail(ctx, GBC_E_ARG, "candidate count mismatch");
+    }
+    std::vector<uint16_t> cand(c32.begin(), c32.end()), list;
+    for (int cr = 0; cr < GBC_NCLASS; ++cr) {
+        ctx->ct.off[cr] = uint32_t(list.size());
+        for (int i = 0; i < GBC_NCAND; ++i) {
+            const uint32_t u = (2u * cr + 30 - cand[i] % 30) % 30;
+            if (gbk::class_of(u) < 8) list.push_back(uint16_t(i));
+        }
+        ctx->ct.cnt[cr] = uint32_t(list.size()) - ctx->ct.off[cr];
+    }
+
+    // slot geometry: a batch of max_batch full segments plus the 9781 + 3 margin
+    const uint64_t span = uint64_t(cfg.max_batch) * cfg.segment_even + GBC_MAX_CAND + 3 + 64;
+    const uint64_t nblk_cap = span / 30 + 4;
+    const uint64_t tiles_cap = (nblk_cap + 64 + tb - 1) / tb;
+    ctx->wpc_cap = uint32_t(tiles_cap * tw);
+
+    *out = ctx;
+    CK(cudaMalloc(&ctx->d_primes, std::max<size_t>(pr.size(), 1) * 4));
+    CK(cudaMemcpy(ctx->d_primes, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_magic, std::max<size_t>(magic.size(), 1) * 4));
+    if (!magic.empty()) CK(cudaMemcpy(ctx->d_magic, magic.data(), magic.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_pat, pat.size() * 4));
+    CK(cudaMemcpy(ctx->d_pat, pat.data(), pat.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_skip, skip.size() * 4));
+    CK(cudaMemcpy(ctx->d_skip, skip.data(), skip.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_inv, inv.size() * 2));
+    CK(cudaMemcpy(ctx->d_inv, inv.data(), inv.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_cand, cand.size() * 2));
+    CK(cudaMemcpy(ctx->d_cand, cand.data(), cand.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_list, list.size() * 2));
+    CK(cudaMemcpy(ctx->d_list, list.data(), list.size() * 2, cudaMemcpyHostToDevice));
+    ctx->ct.cand = ctx->d_cand;
+    ctx->ct.list = ctx->d_list;
+    for (auto &s : ctx->slot)
+        if (int r = slot_alloc(ctx, s)) return r;
+    CK(cudaDeviceSynchronize());
+    return GBC_OK;
+}
+
+extern "C" void gbc_destroy(gbc_ctx *ctx)
+{
+    if (!ctx) return;
+    for (auto &s : ctx->slot) {
+        if (s.st) cudaStreamSynchronize(s.st);
+        for (auto &e : s.ev)
+            if (e) cudaEventDestroy(e);
+        cudaFree(s.map);
+        cudaFree(s.xfirst);
+        cudaFree(s.res);
+        cudaFree(s.err);
+        cudaFree(s.pn);
+        if (s.st) cudaStreamDestroy(s.st);
+    }
+    cudaFree(ctx->d_primes);
+    cudaFree(ctx->d_magic);
+    cudaFree(ctx->d_pat);
+    cudaFree(ctx->d_skip);
+    cudaFree(ctx->d_inv);
+    cudaFree(ctx->d_cand);
+    cudaFree(ctx->d_list);
+    delete ctx;
+}
+
+extern "C" const char *gbc_last_error(const gbc_ctx *ctx)
+{
+    if (!ctx) return "no context";
+    return ctx->err.c_str();
+}
+
+extern "C" int gbc_get_config(const gbc_ctx *ctx, gbc_config *out)
+{
+    if (!ctx || !out) return GBC_E_ARG;
+    *out = ctx->cfg;
+    return GBC_OK;
+}
+
+extern "C" void *gbc_stream(gbc_ctx *ctx, int slot)
+{
+    if (!ctx || slot < 0 || slot > 1) return nullptr;
+    return ctx->slot[slot].st;
+}
+
+extern "C" uint64_t gbc_launch_count(const gbc_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+// Batch geometry and the per-segment kernel parameters (the reference's
+// segment_geometry / class_geometry / seg30 / count30_limits,
+// src/host_math.cpp:13-78, include/check30.hpp:196-210,
+// include/gstats.hpp:272-296, for the batch map layout).
+int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl, int nseg, uint64_t limit,
+                   gbk::BatchParams &bp)
+{
+    const auto &cfg = ctx->cfg;
+    if (nseg < 1 || uint32_t(nseg) > cfg.max_batch) return fail(ctx, GBC_E_ARG, "nseg outside [1, max_batch]");
+    if (limit > cfg.limit || limit & 1) return fail(ctx, GBC_E_ARG, "limit odd or above the context's limit");
+    for (int i = 0; i < nseg; ++i) {
+        const uint64_t a = b[2 * i], e = b[2 * i + 1];
+        if ((a | e) & 1 || a < 4 || e < a || e > limit)
+            return fail(ctx, GBC_E_ARG, "segment bounds must be even with 4 <= start <= end <= limit");
+        if (e - a > cfg.segment_even) return fail(ctx, GBC_E_ARG, "segment longer than segment_even");
+        if (i && a != b[2 * i - 1] + 2) return fail(ctx, GBC_E_ARG, "segments must be consecutive");
+    }
+    const uint64_t s0 = b[0], sN = b[2 * nseg - 1];
+    const uint64_t qlo = s0 > GBC_MAX_CAND + 30 ? s0 - GBC_MAX_CAND : 0;
+    bp.base = qlo / 30 * 30;
+    bp.qmax = sN + 3;
+    const uint64_t nblk = (bp.qmax - bp.base) / 30 + 1;
+    const uint32_t tb = 1u << cfg.tile_log2, tw = tb / 32;
+    const uint64_t tiles = (nblk + 64 + tb - 1) / tb;
+    if (tiles * tw > ctx->wpc_cap) return fail(ctx, GBC_E_ARG, "batch wider than the slot's class map");
+    bp.nblk = uint32_t(nblk);
+    bp.tiles_pc = uint32_t(tiles);
+    bp.wpc = uint32_t(tiles * tw);
+    bp.map = s.map;
+    bp.primes = ctx->d_primes;
+    bp.magic = ctx->d_magic;
+    bp.xfirst = s.xfirst;
+    bp.tile_log2 = cfg.tile_log2;
+    bp.pat = ctx->d_pat;
+    bp.skip_tab = ctx->d_skip;
+    bp.inv_tab = ctx->d_inv;
+    bp.err = s.err;
+    const uint64_t root = isqrt64(bp.qmax);
+    const auto &pr = ctx->primes;
+    bp.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
+    if (bp.n_all < pr.size() && pr.back() < root) return fail(ctx, GBC_E_ARG, "sieving primes too short");
+    bp.i0 = std::min(ctx->i0, bp.n_all);
+    bp.n_mid = std::min(ctx->n_mid, bp.n_all);
+    if (bp.n_mid < bp.i0) bp.n_mid = bp.i0;
+    bp.i_warp = std::min(std::max(ctx->i_warp, bp.i0), bp.n_mid);
+
+    s.segs.assign(nseg, gbk::SegParams{});
+    for (int i = 0; i < nseg; ++i) {
+        gbk::SegParams &sp = s.segs[i];
+        sp.seg_start = b[2 * i];
+        sp.seg_end = b[2 * i + 1];
+        sp.flags = fl ? fl[i] : 0;
+        sp.low = sp.seg_start < GBC_MAX_CAND + 7 ? 1 : 0;
+        const bool last = sp.seg_end == limit;
+        sp.cnt_lo = sp.seg_start + 1;
+        sp.cnt_hi = last ? limit - 1 : sp.seg_end + 1;
+        sp.twin_hi = std::min(sp.cnt_hi, limit >= 3 ? limit - 3 : 0);
+        sp.hash_lo = sp.seg_start > GBC_MAX_CAND + 1 ? sp.seg_start - GBC_MAX_CAND : 1;
+        sp.hash_hi = sp.seg_end + 3;
+        sp.res = s.res + i;
+        sp.pn = s.pn ? s.pn + size_t(i) * s.pn_stride : nullptr;
+    }
+    return GBC_OK;
+}
+
+extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags,
+                                 int nseg, uint64_t limit)
+{
+    if (!ctx || slot < 0 || slot > 1 || !seg_bounds) return fail(ctx, GBC_E_ARG, "bad context, slot or bounds");
+    Slot &s = ctx->slot[slot];
+    if (s.pending) return fail(ctx, GBC_E_STATE, "slot already holds an uncollected batch");
+    gbk::BatchParams bp{};
+    if (int r = gbh_plan_batch(ctx, s, seg_bounds, seg_flags, nseg, limit, bp)) return r;
+    s.bp = bp;
+    s.nseg = nseg;
+    cudaStream_t st = s.st;
+    CK(cudaMemsetAsync(s.res, 0, size_t(nseg) * sizeof(gbc_segment_result), st));
+    for (int i = 0; i < nseg; ++i) {
+        CK(cudaMemsetAsync(s.res[i].first, 0xFF, sizeof(s.res[i].first), st));
+        CK(cudaMemsetAsync(&s.res[i].first_prime, 0xFF, sizeof(uint64_t), st));
+    }
+    CK(cudaEventRecord(s.ev[0], st));
+    gbh::launch_xfirst(bp, st);
+    gbh::launch_tile(bp, ctx->gi, st);
+    ctx->launches += 2;
+    CK(cudaEventRecord(s.ev[1], st));
+    if (bp.n_all > bp.n_mid) {
+        gbh::launch_large(bp, st);
+        ctx->launches += 1;
+    }
+    CK(cudaEventRecord(s.ev[2], st));
+    for (int i = 0; i < nseg; ++i) {
+        gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);
+        gbh::launch_retry(s.segs[i], st);
+        ctx->launches += 2;
+    }
+    CK(cudaEventRecord(s.ev[3], st));
+    for (int i = 0; i < nseg; ++i) {
+        gbh::launch_count(bp, s.segs[i], st);
+        ctx->launches += 1;
+    }
+    CK(cudaEventRecord(s.ev[4], st));
+    CK(cudaGetLastError());
+    s.pending = true;
+    return GBC_OK;
+}
+
+extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int nseg, gbc_batch_times *times,
+                           int timeout_ms)
+{
+    if (!ctx || slot < 0 || slot > 1 || !out) return fail(ctx, GBC_E_ARG, "bad context, slot or output");
+    Slot &s = ctx->slot[slot];
+    if (!s.pending) return fail(ctx, GBC_E_STATE, "collect without an enqueued batch");
+    if (nseg != s.nseg) return fail(ctx, GBC_E_ARG, "nseg differs from the enqueued batch");
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t q = cudaEventQuery(s.ev[4]);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) return fail(ctx, GBC_E_CUDA, std::string("batch: ") + cudaGetErrorString(q));
+        if (timeout_ms >= 0 &&
+            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+            return fail(ctx, GBC_E_TIMEOUT, "batch not finished within the timeout");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    CK(cudaMemcpy(out, s.res, size_t(nseg) * sizeof(gbc_segment_result), cudaMemcpyDeviceToHost));
+    s.pending = false;
+    if (times) {
+        float a = 0, b = 0, c = 0, d = 0;
+        cudaEventElapsedTime(&a, s.ev[0], s.ev[1]);
+        cudaEventElapsedTime(&b, s.ev[1], s.ev[2]);
+        cudaEventElapsedTime(&c, s.ev[2], s.ev[3]);
+        cudaEventElapsedTime(&d, s.ev[3], s.ev[4]);
+        times->ms_setup = 0;
+        times->ms_tile = a;
+        times->ms_large = b;
+        times->ms_check = c;
+        times->ms_count = d;
+        times->ms_total = a + b + c + d;
+    }
+    for (int i = 0; i < nseg; ++i) {
+        gbc_segment_result &r = out[i];
+        const gbk::SegParams &sp = s.segs[i];
+        r.seg_start = sp.seg_start;
+        r.seg_end = sp.seg_end;
+        r.evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+        r.cnt_lo = sp.cnt_lo;
+        r.cnt_hi = sp.cnt_hi;
+        r.twin_hi = sp.twin_hi;
+        r.hash_lo = sp.hash_lo;
+        r.hash_hi = sp.hash_hi;
+        if (r.err) {
+            char m[160];
+            std::snprintf(m, sizeof m, "device error flags 0x%x in segment [%llu, %llu]", r.err,
+                          (unsigned long long)sp.seg_start, (unsigned long long)sp.seg_end);
+            return fail(ctx, GBC_E_DEVICE, m);
+        }
+        if (r.nleft > GBC_LEFT_CAP || r.ntail > GBC_TAIL_CAP)
+            return fail(ctx, GBC_E_OVERFLOW, "leftover or gap-tail list overflow");
+    }
+    return GBC_OK;
+}
+
+extern "C" int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint64_t evens)
+{
+    if (!ctx || slot < 0 || slot > 1 || !out) return fail(ctx, GBC_E_ARG, "bad arguments");
+    Slot &s = ctx->slot[slot];
+    if (!s.pn) return fail(ctx, GBC_E_STATE, "context made without want_pn");
+    if (seg < 0 || seg >= s.nseg) return fail(ctx, GBC_E_ARG, "segment index");
+    const gbk::SegParams &sp = s.segs[seg];
+    if (evens != (sp.seg_end - sp.seg_start) / 2 + 1) return fail(ctx, GBC_E_ARG, "evens differs from the segment");
+    CK(cudaMemcpyAsync(out, s.pn + size_t(seg) * s.pn_stride, evens * 2, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return GBC_OK;
+}
+
+extern "C" const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg)
+{
+    if (!ctx || slot < 0 || slot > 1) return nullptr;
+    Slot &s = ctx->slot[slot];
+    if (!s.pn || seg < 0 || uint32_t(seg) >= ctx->cfg.max_batch) return nullptr;
+    return s.pn + size_t(seg) * s.pn_stride;
+}

@@ -1,0 +1,208 @@
+// k_check.cu -- the exact smallest Goldbach prime p(n) of every even.
+//
+// Evens are grouped by class r = n mod 30 (the reference's check30 layout,
+// include/check30.hpp:1-19): for a candidate p, q = n - p of every even of
+// class r lies in the class array of residue r - p, and consecutive evens of
+// the class are consecutive bits there, so one funnel shift tests 32 evens
+// (goldbach.cl:1950-2001). Unlike the reference's phase A (funnels of
+// several candidates, any witness), this checker tests the candidates of
+// each class in ascending order, so the first candidate that hits an even
+// IS p(n): the exact per-even result that the reference only computes on
+// sampled segments (check30_xs* + check30_xb, goldbach.cl:2339-2418,
+// 2880-3021). Per candidate, a warp reduction adds the hits to the
+// histogram and the first occurrence; evens left without a witness <= 9781
+// go to a list that k_retry settles on the GPU (the reference's CPU
+// fallback cpu_min_goldbach_prime, src/primes.cpp:482-493, moved on device).
+#include <cuda_runtime.h>
+
+#include "gbc_common.cuh"
+
+namespace gbk {
+
+__device__ __forceinline__ void append_leftover(gbc_segment_result *res, uint64_t n)
+{
+    const uint32_t slot = atomicAdd(&res->nleft, 1u);
+    if (slot < GBC_LEFT_CAP) res->left_n[slot] = n;
+    else atomicOr(&res->err, kErrLeftOverflow);
+}
+
+constexpr int kCheckThreads = 256;
+
+__global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegParams sp, CheckTables ct)
+{
+    __shared__ uint32_t s_pos[GBC_NCAND];   // bit offset D of the candidate's window at word 0
+    __shared__ uint32_t s_koff[GBC_NCAND];  // word offset of its class array
+    __shared__ uint16_t s_p[GBC_NCAND];
+    __shared__ uint16_t s_ci[GBC_NCAND];
+    __shared__ uint32_t s_hist[GBC_NCAND];
+    __shared__ uint32_t s_first[GBC_NCAND];
+
+    const uint32_t cr = blockIdx.y, r = 2 * cr;
+    const uint64_t seg_start = sp.seg_start;
+    const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;  // first even of class r
+    if (n0 > sp.seg_end) return;
+    const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
+    const uint32_t nwords = uint32_t((ecount + 31) / 32);
+    const uint32_t ncand = ct.cnt[cr];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+
+    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+        const uint32_t ci = ct.list[ct.off[cr] + c];
+        const uint32_t p = ct.cand[ci];
+        const uint32_t u = (r + 30 - p % 30) % 30;
+        const uint32_t k = class_of(u);
+        // q = n0 + 30 t - p = base + 30 (D + t) + u
+        s_pos[c] = uint32_t((n0 - bp.base - p - u) / 30);
+        s_koff[c] = k * bp.wpc;
+        s_p[c] = uint16_t(p);
+        s_ci[c] = uint16_t(ci);
+        s_hist[c] = 0;
+        s_first[c] = kNone;
+    }
+    __syncthreads();
+
+    const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
+    const uint32_t *map = bp.map;
+    for (uint32_t ch = blockIdx.x * nw + warp; ch * 32 < nwords; ch += gridDim.x * nw) {
+        const uint32_t j = ch * 32 + lane;  // this lane's word of class r: evens n0 + 30 (32 j + b)
+        uint32_t unres = 0;
+        if (j < nwords) {
+            const uint64_t e0 = uint64_t(j) * 32;
+            unres = (ecount - e0 >= 32) ? ~0u : ((1u << uint32_t(ecount - e0)) - 1u);
+        }
+        for (uint32_t c = 0; c < ncand; ++c) {
+            if (!__any_sync(~0u, unres)) break;
+            const uint32_t pos = s_pos[c] + 32 * j;
+            const uint32_t *wk = map + s_koff[c] + (pos >> 5);
+            const uint32_t lo = __ldg(wk);
+            uint32_t hi = __shfl_down_sync(~0u, lo, 1);
+            if (lane == 31) hi = __ldg(wk + 1);
+            const uint32_t w = __funnelshift_r(lo, hi, pos & 31);
+            const uint32_t hit = unres & w;
+            const uint32_t cnt = __reduce_add_sync(~0u, __popc(hit));
+            if (cnt) {
+                const uint32_t mine = hit ? idx0 + 15u * (32u * j + __ffs(hit) - 1u) : kNone;
+                const uint32_t mn = __reduce_min_sync(~0u, mine);
+                if (lane == 0) {
+                    atomicAdd(&s_hist[c], cnt);
+                    if (mn < s_first[c]) atomicMin(&s_first[c], mn);
+                }
+                if (sp.pn) {
+                    const uint16_t pv = s_p[c];
+                    uint32_t h = hit;
+                    while (h) {
+                        const uint32_t b = __ffs(h) - 1u;
+                        sp.pn[idx0 + 15u * (32u * j + b)] = pv;
+                        h &= h - 1u;
+                    }
+                }
+                unres &= ~hit;
+            }
+        }
+        while (unres) {
+            const uint32_t b = __ffs(unres) - 1u;
+            append_leftover(sp.res, n0 + 30ull * (32ull * j + b));
+            unres &= unres - 1u;
+        }
+    }
+    __syncthreads();
+    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+        if (s_hist[c]) atomicAdd(&sp.res->hist[cr][s_ci[c]], s_hist[c]);
+        if (s_first[c] != kNone) atomicMin(&sp.res->first[s_ci[c]], s_first[c]);
+    }
+}
+
+// Generic checker for a segment that reaches q < 7 (seg_start < 9788): one
+// thread per even, every candidate ascending, q = 3 and q = 5 prime by
+// definition (they are not in the class map), q < 3 ends the search.
+__global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp, const uint16_t *cand)
+{
+    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < evens;
+         e += uint64_t(gridDim.x) * blockDim.x) {
+        const uint64_t n = sp.seg_start + 2 * e;
+        const uint32_t cr = uint32_t(n % 30) / 2;
+        int ci = -1;
+        for (int c = 0; c < GBC_NCAND; ++c) {
+            const uint64_t p = cand[c];
+            if (p + 3 > n) break;
+            const uint64_t q = n - p;
+            bool prime;
+            if (q == 3 || q == 5) prime = true;
+            else if (q % 3 == 0 || q % 5 == 0) prime = false;
+            else {
+                const uint64_t t = (q - bp.base) / 30;
+                const uint32_t k = class_of(uint32_t(q % 30));
+                prime = (bp.map[size_t(k) * bp.wpc + (t >> 5)] >> (t & 31)) & 1u;
+            }
+            if (prime) {
+                ci = c;
+                break;
+            }
+        }
+        if (ci >= 0) {
+            atomicAdd(&sp.res->hist[cr][ci], 1u);
+            atomicMin(&sp.res->first[ci], uint32_t(e));
+            if (sp.pn) sp.pn[e] = cand[ci];
+        } else {
+            append_leftover(sp.res, n);
+        }
+    }
+}
+
+// Evens without a witness <= 9781: ascending odd p > 9781 by Miller-Rabin on
+// both p and n - p (n = 4: p = 2). A bounded search: a wait that runs out
+// sets an error flag instead of looping.
+__global__ void __launch_bounds__(64) k_retry(SegParams sp)
+{
+    gbc_segment_result *res = sp.res;
+    const uint32_t nl = res->nleft < GBC_LEFT_CAP ? res->nleft : GBC_LEFT_CAP;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+        const uint64_t n = res->left_n[i];
+        uint64_t found = 0;
+        if (n == 4) found = 2;
+        else {
+            uint32_t tries = 0;
+            for (uint64_t p = GBC_MAX_CAND + 2; p <= n / 2; p += 2) {
+                if (++tries > (1u << 22)) {
+                    atomicOr(&res->err, kErrRetry);
+                    break;
+                }
+                if (is_prime_u64_dev(p) && is_prime_u64_dev(n - p)) {
+                    found = p;
+                    break;
+                }
+            }
+        }
+        res->left_p[i] = found;
+        if (sp.pn) sp.pn[(n - sp.seg_start) / 2] = found < 65536 ? uint16_t(found) : 0;
+    }
+}
+
+}  // namespace gbk
+
+namespace gbh {
+
+void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
+                  cudaStream_t st)
+{
+    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+    if (sp.low) {
+        uint64_t blocks = (evens + 255) / 256;
+        if (blocks > uint64_t(sm_count) * 16) blocks = uint64_t(sm_count) * 16;
+        gbk::k_check_low<<<uint32_t(blocks), 256, 0, st>>>(bp, sp, ct.cand);
+        return;
+    }
+    // words per class ~ evens / 15 / 32; 8 warps per CTA, a few chunks each
+    const uint64_t words = (evens / 15 + 32) / 32 + 1;
+    uint64_t bx = (words + 8 * 32 - 1) / (8 * 32);
+    const uint64_t cap = uint64_t(sm_count) * 4;  // per class: the 15 classes share the GPU
+    if (bx > cap) bx = cap;
+    if (bx < 1) bx = 1;
+    dim3 grid(uint32_t(bx), GBC_NCLASS);
+    gbk::k_check<<<grid, gbk::kCheckThreads, 0, st>>>(bp, sp, ct);
+}
+
+void launch_retry(const gbk::SegParams &sp, cudaStream_t st) { gbk::k_retry<<<1, 64, 0, st>>>(sp); }
+
+}  // namespace gbh

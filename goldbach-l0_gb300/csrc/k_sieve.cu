@@ -1,0 +1,241 @@
+// k_sieve.cu -- builds a batch's mod-30 class map on the GPU.
+//
+// Stages (the reference's make_prime_map, mid_setup/mid_window and
+// sieve_large_packed, kernels/goldbach.cl:1092-1608, 3528-3701, 1738-1849,
+// re-designed for one HBM-resident map per batch of segments):
+//   k_xfirst  per tile-sieve prime and class: the first class bit of the
+//             batch that is a multiple of p and >= p^2 (mid_setup's job,
+//             goldbach.cl:3528-3563; host_math.cpp:80-113).
+//   k_tile    one CTA per (tile, class): 2^tile_log2 bits in shared memory;
+//             the primes 7..67 by whole-word AND patterns of seven prime
+//             groups, then every prime 71..p_mid by shared-memory atomics
+//             (small primes warp-cooperatively, the rest one per thread);
+//             one coalesced store of the finished tile.
+//   k_large   primes above p_mid, one thread per prime, marking every
+//             multiple p m (m coprime to 30) of the batch with a global
+//             atomic AND after a read (read-before-mark, goldbach.cl:
+//             328-336), skipping multipliers divisible by 7..23 whose
+//             multiples the pattern stage already cleared (the 30030 wheel
+//             and the 17..29 skip of goldbach.cl:638-748).
+#include <cuda_runtime.h>
+
+#include "gbc_common.cuh"
+
+namespace gbk {
+
+// First class bit, for each class k, of a multiple of p in the batch with
+// q >= p^2; kNone when the first one is at or past nblk. p > 29.
+__device__ __forceinline__ void first_bits8(uint64_t base, uint32_t nblk, uint32_t p, uint32_t *out)
+{
+    const uint32_t r = uint32_t(base % p);
+    const uint32_t iv = inv30_mod(p);
+    const uint64_t pp = uint64_t(p) * p;
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) {
+        const uint32_t u = unit30(k);
+        uint32_t a = r + u;                 // (base + u) mod p
+        if (a >= p) a -= p;
+        a = a ? p - a : 0;                  // -(base + u) mod p
+        uint64_t t = uint64_t(a) * iv % p;  // base + 30 t + u = 0 (mod p)
+        const uint64_t q = base + 30 * t + u;
+        if (q < pp) {                       // p itself and smaller multiples stay unmarked
+            const uint64_t tmin = (pp - base - u + 29) / 30;
+            if (tmin > t) t += (tmin - t + p - 1) / p * p;
+        }
+        out[k] = t < nblk ? uint32_t(t) : kNone;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_xfirst(BatchParams bp)
+{
+    const uint32_t n = bp.n_mid;
+    for (uint32_t i = bp.i0 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t x[8];
+        first_bits8(bp.base, bp.nblk, bp.primes[i], x);
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) bp.xfirst[size_t(k) * n + i] = x[k];
+    }
+}
+
+// Tile-local first mark of a prime from its batch-level first bit x.
+__device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_t p, uint32_t magic, uint32_t tb)
+{
+    if (x == kNone) return kNone;
+    if (x >= t0) {
+        const uint32_t d = x - t0;
+        return d < tb ? d : kNone;
+    }
+    const uint32_t d = t0 - x;
+    const uint32_t q = __umulhi(d, magic);  // floor(d / p) or one less
+    uint32_t rem = d - q * p;
+    if (rem >= p) rem -= p;
+    return rem ? p - rem : 0;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
+{
+    extern __shared__ uint32_t sm[];
+    const uint32_t tb = 1u << bp.tile_log2, tw = tb >> 5;
+    uint32_t *s = sm;
+    uint32_t *pat = sm + tw;
+    const uint32_t k = blockIdx.y, tid = threadIdx.x, bs = blockDim.x;
+    const uint32_t t0 = blockIdx.x << bp.tile_log2;
+    const uint64_t q0 = bp.base + 30ull * t0 + unit30(k);
+
+    for (uint32_t i = tid; i < gi.words; i += bs) pat[i] = bp.pat[i];
+
+    // phase of this thread's first word in each group's canonical pattern:
+    // local bit x is cleared by the group iff (x + c) mod P has a factor in
+    // the group, c = (P - Y) mod P, Y = -q0 / 30 (mod P)
+    uint32_t ph[kNumGroups], stp[kNumGroups];
+#pragma unroll
+    for (int g = 0; g < kNumGroups; ++g) {
+        const uint32_t P = gi.P[g];
+        const uint32_t qm = uint32_t(q0 % P);
+        const uint32_t y = uint32_t(uint64_t((P - qm) % P) * gi.inv30[g] % P);
+        const uint32_t c = (P - y) % P;
+        ph[g] = uint32_t((32ull * tid + c) % P);
+        stp[g] = uint32_t((32ull * bs) % P);
+    }
+    __syncthreads();
+    for (uint32_t w = tid; w < tw; w += bs) {
+        uint32_t v = ~0u;
+#pragma unroll
+        for (int g = 0; g < kNumGroups; ++g) {
+            const uint32_t *pg = pat + gi.off[g];
+            const uint32_t x = ph[g];
+            v &= __funnelshift_r(pg[x >> 5], pg[(x >> 5) + 1], x & 31);
+            uint32_t nx = x + stp[g];
+            if (nx >= gi.P[g]) nx -= gi.P[g];
+            ph[g] = nx;
+        }
+        s[w] = v;
+    }
+    __syncthreads();
+    if (tid == 0 && q0 < 4096) {
+        // the pattern primes are prime themselves; 1 is not
+        const uint32_t small[16] = {7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67};
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t p = small[i];
+            if (p % 30 == unit30(k) && p >= q0) {
+                const uint32_t b = uint32_t((p - q0) / 30);
+                if (b < tb) s[b >> 5] |= 1u << (b & 31);
+            }
+        }
+        if (q0 == 1) s[0] &= ~1u;
+    }
+    __syncthreads();
+
+    const uint32_t lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    const uint32_t *xk = bp.xfirst + size_t(k) * bp.n_mid;
+    // small primes: a warp per prime, lanes take every 32nd multiple
+    for (uint32_t i = bp.i0 + warp; i < bp.i_warp; i += nw) {
+        const uint32_t p = bp.primes[i];
+        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tb);
+        if (l >= tb) continue;
+        for (uint32_t b = l + lane * p; b < tb; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+    }
+    // the rest: a thread per prime
+    for (uint32_t i = bp.i_warp + tid; i < bp.n_mid; i += bs) {
+        const uint32_t p = bp.primes[i];
+        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tb);
+        for (uint32_t b = l; b < tb; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+    }
+    __syncthreads();
+    uint4 *dst = reinterpret_cast<uint4 *>(bp.map + size_t(k) * bp.wpc + (t0 >> 5));
+    const uint4 *src = reinterpret_cast<const uint4 *>(s);
+    for (uint32_t i = tid; i < tw / 4; i += bs) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(256) k_large(BatchParams bp)
+{
+    __shared__ uint32_t s_skip[(kSkip1 + 31) / 32 + (kSkip2 + 31) / 32];
+    __shared__ uint16_t s_inv[kSkip1 + kSkip2];
+    constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
+    for (uint32_t i = threadIdx.x; i < kW1 + (kSkip2 + 31) / 32; i += blockDim.x) s_skip[i] = bp.skip_tab[i];
+    for (uint32_t i = threadIdx.x; i < kSkip1 + kSkip2; i += blockDim.x) s_inv[i] = bp.inv_tab[i];
+    __syncthreads();
+    const uint32_t bm1 = uint32_t(bp.base % kSkip1), bm2 = uint32_t(bp.base % kSkip2);
+    const uint32_t nblk = bp.nblk;
+    for (uint32_t i = bp.n_mid + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_all;
+         i += gridDim.x * blockDim.x) {
+        const uint32_t p = bp.primes[i];
+        uint32_t x[8];
+        first_bits8(bp.base, nblk, p, x);
+        const uint32_t pi1 = s_inv[p % kSkip1], pi2 = s_inv[kSkip1 + p % kSkip2];
+#pragma unroll 1
+        for (uint32_t k = 0; k < 8; ++k) {
+            uint32_t t = x[k];
+            if (t == kNone) continue;
+            uint32_t *wk = bp.map + size_t(k) * bp.wpc;
+            const uint32_t u = unit30(k);
+            // multiplier m = q / p modulo 1001 and 7429: m = q p^-1
+            uint32_t m1 = (bm1 + uint32_t((30ull * t + u) % kSkip1)) % kSkip1 * pi1 % kSkip1;
+            uint32_t m2 = (bm2 + uint32_t((30ull * t + u) % kSkip2)) % kSkip2 * pi2 % kSkip2;
+            for (;;) {
+                const uint32_t sk = ((s_skip[m1 >> 5] >> (m1 & 31)) | (s_skip[kW1 + (m2 >> 5)] >> (m2 & 31))) & 1u;
+                if (!sk) {
+                    uint32_t *a = wk + (t >> 5);
+                    const uint32_t bit = 1u << (t & 31);
+                    if (__ldcg(a) & bit) atomicAnd(a, ~bit);
+                }
+                if (nblk - t <= p) break;
+                t += p;
+                m1 += 30;
+                if (m1 >= kSkip1) m1 -= kSkip1;
+                m2 += 30;
+                if (m2 >= kSkip2) m2 -= kSkip2;
+            }
+        }
+    }
+}
+
+}  // namespace gbk
+
+namespace gbh {
+
+static int sm_count_cached()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+void launch_xfirst(const gbk::BatchParams &bp, cudaStream_t st)
+{
+    if (bp.n_mid <= bp.i0) return;
+    const uint32_t n = bp.n_mid - bp.i0;
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    gbk::k_xfirst<<<blocks, 256, 0, st>>>(bp);
+}
+
+void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st)
+{
+    const uint32_t tw = (1u << bp.tile_log2) >> 5;
+    const size_t smem = size_t(tw + gi.words) * 4;
+    static size_t set_for = 0;
+    if (set_for != smem) {
+        cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        set_for = smem;
+    }
+    dim3 grid(bp.tiles_pc, 8);
+    gbk::k_tile<<<grid, 1024, smem, st>>>(bp, gi);
+}
+
+void launch_large(const gbk::BatchParams &bp, cudaStream_t st)
+{
+    if (bp.n_all <= bp.n_mid) return;
+    const uint32_t n = bp.n_all - bp.n_mid;
+    uint32_t blocks = uint32_t(sm_count_cached()) * 8;
+    const uint32_t need = (n + 255) / 256;
+    if (blocks > need) blocks = need;
+    gbk::k_large<<<blocks, 256, 0, st>>>(bp);
+}
+
+}  // namespace gbh

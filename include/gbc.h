@@ -1,0 +1,185 @@
+/*
+ * gbc.h -- C ABI of the GB300 dense Goldbach verify path.
+ *
+ * The reference (goldbach-l0) has no FFI: its boundary for this path is the
+ * dense run driver's per-segment contract (src/verifier.cpp:1741-2444:
+ * prepare_segment_tables / enqueue_sieve / enqueue_large_primes /
+ * enqueue_check / collect_slot) under gb::run_gpu (include/verifier.hpp:
+ * 71-110). Every entry point below replaces one piece of that contract, as
+ * its comment says. Plain C types only; every call returns an int status
+ * (GBC_OK = 0, negative = error class) and gbc_last_error() gives the text.
+ * Nothing here throws, nothing here falls back to the CPU.
+ *
+ * Terms: an "even" is an even n to verify; p(n) is the smallest odd prime p
+ * with n - p prime (2 for n = 4). A "segment" is a run of consecutive evens
+ * [seg_start, seg_end] (inclusive) whose statistics are reported together;
+ * a "batch" is up to max_batch consecutive segments sieved in one pass over
+ * one HBM-resident mod-30 class map. A "slot" is one of two independent sets
+ * of device buffers, so batch k + 1 can be enqueued while batch k is being
+ * collected.
+ */
+#ifndef GBC_H
+#define GBC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBC_OK 0
+#define GBC_E_ARG (-1)      /* bad argument (range, size, slot, alignment) */
+#define GBC_E_CUDA (-2)     /* a CUDA runtime call failed */
+#define GBC_E_DEVICE (-3)   /* a device-side error flag was set */
+#define GBC_E_TIMEOUT (-4)  /* a bounded wait ran out */
+#define GBC_E_STATE (-5)    /* call out of order (collect without enqueue, ...) */
+#define GBC_E_OVERFLOW (-6) /* a fixed-capacity output overflowed */
+
+#define GBC_NCAND 1205      /* odd primes 3..9781 (include/config.hpp:81-86 MAX_GB_PRIME) */
+#define GBC_MAX_CAND 9781u
+#define GBC_NCLASS 15       /* even classes r = n mod 30 = 0, 2, ..., 28 */
+#define GBC_GBINS 1024      /* gap histogram bins g / 2 (include/gstats.hpp:78 GAPS30_HBINS) */
+#define GBC_GTAIL 700u      /* gaps >= 700 are listed with their position (gstats.hpp:77) */
+#define GBC_TAIL_CAP 256    /* listed tail gaps per segment */
+#define GBC_LEFT_CAP 1024   /* evens per segment without a candidate witness */
+#define GBC_DEFAULT_SEGMENT 467500000ull /* include/config.hpp:163 DEFAULT_SEGMENT_EVEN */
+#define GBC_MAX_LIMIT 18446742974197923840ull /* 2^64 - 2^40 (include/primes.hpp:212) */
+
+/* segment flags */
+#define GBC_SEG_LAST 1u     /* the run's last segment: counts end at limit - 1 */
+#define GBC_SEG_NOHASH 2u   /* skip the class-map hash */
+
+/* Context configuration (the knobs of include/config.hpp and the GB_*
+ * environment, as fields). Zero means "default" for every field. */
+typedef struct gbc_config {
+    uint64_t limit;          /* largest even any batch will reach: sizes the sieving primes */
+    uint64_t segment_even;   /* integer span of a full segment (default 467.5M) */
+    uint32_t max_batch;      /* segments per batch the slots are sized for (default 8) */
+    uint32_t tile_log2;      /* log2 of shared-memory tile bits per class (16..20, default 20) */
+    uint32_t p_mid;          /* primes <= p_mid: shared-memory tiles; above: large-prime kernel (default 2^22) */
+    uint32_t want_pn;        /* 1: slots also hold a per-even u16 p(n) buffer */
+    int32_t device;          /* CUDA device ordinal (default 0) */
+    uint32_t reserved[7];
+} gbc_config;
+
+typedef struct gbc_ctx gbc_ctx;
+
+/* Per-segment results (collect_slot + GoldbachStats::add_* inputs,
+ * src/verifier.cpp:2402-2444, include/gstats.hpp:507-624). Indices into the
+ * candidate list are positions in gbc_candidates(). */
+typedef struct gbc_segment_result {
+    uint64_t seg_start, seg_end, evens;
+    uint64_t cnt_lo, cnt_hi;       /* primes counted: q in [cnt_lo, cnt_hi] (odd) */
+    uint64_t twin_hi;              /* twin pairs (q, q + 2) counted for q in [cnt_lo, twin_hi] */
+    uint64_t hash_lo, hash_hi;     /* class-map hash range */
+    /* p(n) of every even (exact; the smallest witness) */
+    uint32_t hist[GBC_NCLASS][GBC_NCAND]; /* evens with p(n) = cand[i], by class r / 2 */
+    uint32_t first[GBC_NCAND];     /* (n - seg_start) / 2 of the first such even, or UINT32_MAX */
+    uint32_t nleft;                /* evens with no witness <= 9781 (retried on the GPU) */
+    uint32_t pad0;
+    uint64_t left_n[GBC_LEFT_CAP]; /* those evens ... */
+    uint64_t left_p[GBC_LEFT_CAP]; /* ... and their p(n) from the GPU retry (0: none found) */
+    /* primes, twins, gaps of q in the count range (count30 + add_gap_segment) */
+    uint64_t primes30[8];          /* by residue 1, 7, 11, 13, 17, 19, 23, 29 */
+    uint64_t twins[3];             /* lower prime = 11, 17, 29 (mod 30) */
+    uint32_t ghist[GBC_GBINS];     /* gaps q - prev(q) by g / 2 */
+    uint64_t gmax_key;             /* largest gap: g << 32 | (UINT32_MAX - (lower - hash_lo)) */
+    uint32_t ntail;                /* gaps >= 700 listed below (count may exceed the cap: error) */
+    uint32_t pad1;
+    uint32_t tail_g[GBC_TAIL_CAP];
+    uint64_t tail_lo[GBC_TAIL_CAP];/* lower prime of each listed gap */
+    uint64_t first_prime, last_prime; /* in the count range (0: none) */
+    uint64_t map_hash;             /* sum of splitmix64(q) over primes q in [hash_lo, hash_hi] coprime to 30 */
+    uint64_t map_primes;           /* number of those primes */
+    uint32_t err;                  /* device error flags (0 = none) */
+    uint32_t pad2;
+} gbc_segment_result;
+
+/* Stage times of one batch (device events on the slot's stream). */
+typedef struct gbc_batch_times {
+    float ms_setup, ms_tile, ms_large, ms_check, ms_count, ms_total;
+} gbc_batch_times;
+
+/* Creates a context on cfg->device: the sieving primes up to
+ * sqrt(cfg->limit + 3), the pattern and wheel tables, and two slots.
+ * Replaces DenseRun's construction (src/verifier.cpp:346-354) and
+ * RunSetup::load_base_primes / upload_tables (src/verifier.cpp:633-692,
+ * 1361-1440). Returns GBC_OK and *out, or an error (then *out = NULL). */
+int gbc_create(const gbc_config *cfg, gbc_ctx **out);
+
+/* Frees every device and host buffer of the context (release_device_objects,
+ * src/verifier.cpp). Safe on NULL. */
+void gbc_destroy(gbc_ctx *ctx);
+
+/* Text of the last error on this context (ZE_CHECK's message,
+ * include/l0_context.hpp:14-20); never NULL. */
+const char *gbc_last_error(const gbc_ctx *ctx);
+
+/* The configuration in force, defaults filled in (the values RunSetup
+ * resolves in resolve_range / load_base_primes, src/verifier.cpp:573-692). */
+int gbc_get_config(const gbc_ctx *ctx, gbc_config *out);
+
+/* The odd candidate primes 3..9781 ascending (gb_primes of
+ * RunSetup::load_base_primes, src/verifier.cpp:686-691). Returns the count. */
+int gbc_candidates(uint16_t *out, int cap);
+
+/* Enqueues one batch of nseg consecutive segments on a slot: tile sieve,
+ * large primes, checker, counts (prepare_segment_tables + enqueue_sieve +
+ * enqueue_large_primes + enqueue_check, src/verifier.cpp:1741-2146).
+ * seg_bounds holds 2 * nseg evens: [seg_start, seg_end] of each segment,
+ * consecutive (seg_start[i+1] = seg_end[i] + 2), all even, 4 <= seg_start,
+ * seg_end <= limit <= GBC_MAX_LIMIT. seg_flags (nseg entries or NULL) holds
+ * GBC_SEG_* flags; limit is the run's last even (counts stop at limit - 1).
+ * Returns at once; the work runs on the slot's stream. */
+int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags, int nseg,
+                      uint64_t limit);
+
+/* Waits (at most timeout_ms; < 0 waits without a limit) for the slot's
+ * batch and copies its nseg results to host memory (collect_slot,
+ * src/verifier.cpp:2402-2444). Fails closed with GBC_E_DEVICE on any device
+ * error flag and GBC_E_OVERFLOW when a leftover or tail list overflowed.
+ * times may be NULL. */
+int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int nseg, gbc_batch_times *times,
+                int timeout_ms);
+
+/* Copies segment i's per-even p(n) of the last collected batch of the slot
+ * (u16, index (n - seg_start) / 2; 2 for n = 4; 0 only for a counterexample)
+ * into host memory. Needs want_pn. evens = the segment's even count. */
+int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint64_t evens);
+
+/* Device pointer of the slot's per-even p(n) buffer of segment i (or NULL
+ * without want_pn), for callers that keep results on the device. */
+const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg);
+
+/* The CUDA stream of a slot (a cudaStream_t), for callers that time or
+ * order their own work against it. */
+void *gbc_stream(gbc_ctx *ctx, int slot);
+
+/* Number of CUDA kernels this context has launched so far. */
+uint64_t gbc_launch_count(const gbc_ctx *ctx);
+
+/* Run-level result (RunStats of include/verifier.hpp:30-69, the counts only). */
+typedef struct gbc_run_result {
+    uint64_t start, limit, evens, segments, batches;
+    uint64_t leftovers;          /* evens retried on the GPU beyond 9781 */
+    uint64_t pmax;               /* largest p(n) */
+    uint64_t primes, twins;      /* in [start + 1, limit - 1] */
+    double gpu_seconds;          /* device time of the batch loop */
+    double wall_seconds;
+} gbc_run_result;
+
+/* Verifies every even in [start, limit] through the per-segment contract
+ * above and writes the reference's stats_ref line (tests/stats_ref.cpp:
+ * 97-189) into line (NUL-terminated; line may be NULL). pn (host, or NULL)
+ * receives p(n) of every even, (limit - start) / 2 + 1 entries; it needs
+ * want_pn. The run driver of gb::run_gpu (src/verifier.cpp:2487-2569) as one
+ * call: segments of cfg->segment_even, batches of cfg->max_batch, two slots
+ * in flight, fail closed on any error. */
+int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gbc_run_result *res, char *line,
+                     uint64_t line_cap, uint16_t *pn);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBC_H */
