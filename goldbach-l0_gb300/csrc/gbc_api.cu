@@ -494,6 +494,23 @@ extern "C" int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint6
     return GBC_OK;
 }
 
+extern "C" int gbc_map_info(gbc_ctx *ctx, int slot, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
+                            uint64_t out_words)
+{
+    if (!ctx || slot < 0 || slot > 1) return fail(ctx, GBC_E_ARG, "bad context or slot");
+    Slot &s = ctx->slot[slot];
+    if (s.pending) return fail(ctx, GBC_E_STATE, "the slot's batch is not collected yet");
+    if (!s.nseg) return fail(ctx, GBC_E_STATE, "no batch on this slot yet");
+    if (base) *base = s.bp.base;
+    if (nblk) *nblk = s.bp.nblk;
+    if (wpc) *wpc = s.bp.wpc;
+    if (out) {
+        if (out_words < uint64_t(8) * s.bp.wpc) return fail(ctx, GBC_E_ARG, "output smaller than 8 * wpc words");
+        CK(cudaMemcpy(out, s.map, size_t(8) * s.bp.wpc * 4, cudaMemcpyDeviceToHost));
+    }
+    return GBC_OK;
+}
+
 extern "C" const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg)
 {
     if (!ctx || slot < 0 || slot > 1) return nullptr;

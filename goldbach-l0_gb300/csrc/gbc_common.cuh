@@ -24,7 +24,8 @@ constexpr uint32_t kSkip2 = 7429;     // 17 * 19 * 23
 // u_k, the residue of class array k
 __host__ __device__ __forceinline__ uint32_t unit30(uint32_t k)
 {
-    return uint32_t((0x1D17130D110B0701ull >> (8 * k)) & 0xFF);
+    // bytes, low to high: 1, 7, 11, 13, 17, 19, 23, 29
+    return uint32_t((0x1D1713110D0B0701ull >> (8 * k)) & 0xFF);
 }
 
 // class array index of a residue mod 30, or 8 when it is not coprime to 30

@@ -70,6 +70,8 @@ SIGNATURES = {
                               C.c_int]),
     "gbc_copy_pn": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_uint16), C.c_uint64]),
     "gbc_pn_device_ptr": (C.c_void_p, [C.c_void_p, C.c_int, C.c_int]),
+    "gbc_map_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint64]),
     "gbc_stream": (C.c_void_p, [C.c_void_p, C.c_int]),
     "gbc_launch_count": (C.c_uint64, [C.c_void_p]),
     "gbc_verify_range": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(RunResult), C.c_char_p,
@@ -159,6 +161,15 @@ class Context:
         buf = (C.c_uint16 * evens)()
         self._check(self.lib.gbc_copy_pn(self.h, slot, seg, buf, evens))
         return buf
+
+    def map(self, slot):
+        """(base, nblk, wpc, words) of the slot's last collected class map;
+        words is a u32 array of 8 * wpc entries."""
+        base, nblk, wpc = C.c_uint64(), C.c_uint32(), C.c_uint32()
+        self._check(self.lib.gbc_map_info(self.h, slot, C.byref(base), C.byref(nblk), C.byref(wpc), None, 0))
+        words = (C.c_uint32 * (8 * wpc.value))()
+        self._check(self.lib.gbc_map_info(self.h, slot, None, None, None, words, len(words)))
+        return base.value, nblk.value, wpc.value, words
 
     def stream(self, slot):
         return self.lib.gbc_stream(self.h, slot)

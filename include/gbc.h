@@ -151,6 +151,16 @@ int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint64_t evens);
  * without want_pn), for callers that keep results on the device. */
 const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg);
 
+/* The class map of the slot's last collected batch, for bit-exact
+ * validation against an independent primality test (the reference's
+ * debug_map validator, docs/PROJECT-REFERENCE.md:615-620): *base (q of
+ * class-array bit 0 minus its residue, a multiple of 30), *nblk (bits per
+ * class array in use) and *wpc (words per class array); when out is not
+ * NULL, 8 * wpc words are copied to it (class k at out + k * wpc, bit t of
+ * class k <-> q = base + 30 t + u_k, u = 1, 7, 11, 13, 17, 19, 23, 29). */
+int gbc_map_info(gbc_ctx *ctx, int slot, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
+                 uint64_t out_words);
+
 /* The CUDA stream of a slot (a cudaStream_t), for callers that time or
  * order their own work against it. */
 void *gbc_stream(gbc_ctx *ctx, int slot);

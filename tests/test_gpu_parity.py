@@ -72,6 +72,31 @@ def test_segment_hash_and_counts_match_oracle(ctx):
         assert int(kv["evens"]) == r.evens
 
 
+U30 = [1, 7, 11, 13, 17, 19, 23, 29]
+
+
+@pytest.mark.parametrize("a,tile_log2", [(10**12, 20), (4 * 10**18, 16), (6, 18), (9223372036853775808, 20),
+                                         (gbc.MAX_LIMIT - 2_000_000, 20)])
+def test_class_map_bit_exact(a, tile_log2):
+    """Every bit of a batch's class map against Miller-Rabin (the
+    reference's debug_map validator): the sieve stages may not lose or add a
+    mark anywhere, including q < 67 at the bottom and 2^64 - 2^40 at the top."""
+    seg = 500_000
+    b = a + 2 * seg - 2
+    segs = gbc.segments_of(a, b, seg)
+    with gbc.Context(limit=b, segment_even=seg, max_batch=len(segs), tile_log2=tile_log2, p_mid=1 << 18) as c:
+        c.enqueue_batch(0, segs, b)
+        c.collect(0, len(segs))
+        base, nblk, wpc, w = c.map(0)
+    bad = []
+    for k in range(8):
+        for t in range(nblk):
+            q = base + 30 * t + U30[k]
+            if ((w[k * wpc + (t >> 5)] >> (t & 31)) & 1) != oracle.is_prime(q):
+                bad.append(q)
+    assert not bad, bad[:8]
+
+
 def test_batched_equals_plain():
     a, b = 4_000_000_000_000_000_000, 4_000_000_000_060_000_000
     lines = []
