@@ -157,6 +157,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.max_batch) cfg.max_batch = 8;
     if (!cfg.tile_log2) cfg.tile_log2 = 20;
     if (!cfg.p_mid) cfg.p_mid = 1u << 22;
+    if (!cfg.large_pass_mb) cfg.large_pass_mb = 4096;  // one pass: the per-prime setup outweighs L2 misses
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
@@ -405,10 +406,7 @@ extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bou
     gbh::launch_tile(bp, ctx->gi, st);
     ctx->launches += 2;
     CK(cudaEventRecord(s.ev[1], st));
-    if (bp.n_all > bp.n_mid) {
-        gbh::launch_large(bp, st);
-        ctx->launches += 1;
-    }
+    ctx->launches += gbh::launch_large(bp, ctx->cfg.large_pass_mb, st);
     CK(cudaEventRecord(s.ev[2], st));
     for (int i = 0; i < nseg; ++i) {
         gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);

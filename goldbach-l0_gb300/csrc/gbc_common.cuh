@@ -183,7 +183,7 @@ __device__ inline bool is_prime_u64_dev(uint64_t n)
 namespace gbh {
 void launch_xfirst(const gbk::BatchParams &bp, cudaStream_t st);
 void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st);
-void launch_large(const gbk::BatchParams &bp, cudaStream_t st);
+int launch_large(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st);
 void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
                   cudaStream_t st);
 void launch_retry(const gbk::SegParams &sp, cudaStream_t st);

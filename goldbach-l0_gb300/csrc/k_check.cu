@@ -27,15 +27,41 @@ __device__ __forceinline__ void append_leftover(gbc_segment_result *res, uint64_
 }
 
 constexpr int kCheckThreads = 256;
+constexpr int kCheckWarps = kCheckThreads / 32;
+constexpr uint32_t kWin = 80;  // staged words per class array per warp: 64 + span of the candidates + 2
 
+// valid-even mask of word j of a class with ecount evens
+__device__ __forceinline__ uint32_t word_mask(uint32_t j, uint64_t ecount)
+{
+    const uint64_t e0 = uint64_t(j) * 32;
+    if (e0 >= ecount) return 0u;
+    return (ecount - e0 >= 32) ? ~0u : ((1u << uint32_t(ecount - e0)) - 1u);
+}
+
+__device__ __forceinline__ void write_pn(uint16_t *pn, uint32_t idx0, uint32_t j, uint32_t h, uint16_t pv)
+{
+    while (h) {
+        const uint32_t b = __ffs(h) - 1u;
+        pn[idx0 + 15u * (32u * j + b)] = pv;
+        h &= h - 1u;
+    }
+}
+
+// One CTA per (chunk column, class r); each warp takes 64 consecutive words
+// (2048 evens) of class r at a time, stages the 8 class-array windows they
+// read (64 words + the candidates' span) in its own shared memory, and tests
+// the class's useful candidates in ascending order: lane l holds words l and
+// l + 32 of the chunk, so every shared-memory read of the warp is 32
+// consecutive words.
 __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegParams sp, CheckTables ct)
 {
-    __shared__ uint32_t s_pos[GBC_NCAND];   // bit offset D of the candidate's window at word 0
-    __shared__ uint32_t s_koff[GBC_NCAND];  // word offset of its class array
+    __shared__ uint32_t s_ent[GBC_NCAND];   // word offset | shift << 8 | class array << 13
     __shared__ uint16_t s_p[GBC_NCAND];
     __shared__ uint16_t s_ci[GBC_NCAND];
     __shared__ uint32_t s_hist[GBC_NCAND];
     __shared__ uint32_t s_first[GBC_NCAND];
+    __shared__ uint32_t s_win[kCheckWarps][8 * kWin];
+    __shared__ uint32_t s_dmin, s_dmax;
 
     const uint32_t cr = blockIdx.y, r = 2 * cr;
     const uint64_t seg_start = sp.seg_start;
@@ -44,16 +70,31 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
     const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
     const uint32_t nwords = uint32_t((ecount + 31) / 32);
     const uint32_t ncand = ct.cnt[cr];
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
+    if (tid == 0) {
+        s_dmin = kNone;
+        s_dmax = 0;
+    }
+    __syncthreads();
+    // q = n0 + 30 t - p = base + 30 (D + t) + u: D is the bit of the
+    // candidate's window at word 0 of class r
+    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+        const uint32_t ci = ct.list[ct.off[cr] + c];
+        const uint32_t p = ct.cand[ci];
+        const uint32_t D = uint32_t((n0 - bp.base - p - (r + 30 - p % 30) % 30) / 30);
+        atomicMin(&s_dmin, D);
+        atomicMax(&s_dmax, D);
+    }
+    __syncthreads();
+    const uint32_t dlo = s_dmin & ~31u;                 // staged windows start at word dlo / 32 + J
+    const uint32_t nstage = (s_dmax - dlo) / 32 + 66;   // words per class array (<= kWin)
     for (uint32_t c = tid; c < ncand; c += blockDim.x) {
         const uint32_t ci = ct.list[ct.off[cr] + c];
         const uint32_t p = ct.cand[ci];
         const uint32_t u = (r + 30 - p % 30) % 30;
-        const uint32_t k = class_of(u);
-        // q = n0 + 30 t - p = base + 30 (D + t) + u
-        s_pos[c] = uint32_t((n0 - bp.base - p - u) / 30);
-        s_koff[c] = k * bp.wpc;
+        const uint32_t d = uint32_t((n0 - bp.base - p - u) / 30) - dlo;
+        s_ent[c] = (d >> 5) | ((d & 31) << 8) | (class_of(u) << 13);
         s_p[c] = uint16_t(p);
         s_ci[c] = uint16_t(ci);
         s_hist[c] = 0;
@@ -62,48 +103,53 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
     __syncthreads();
 
     const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
-    const uint32_t *map = bp.map;
-    for (uint32_t ch = blockIdx.x * nw + warp; ch * 32 < nwords; ch += gridDim.x * nw) {
-        const uint32_t j = ch * 32 + lane;  // this lane's word of class r: evens n0 + 30 (32 j + b)
-        uint32_t unres = 0;
-        if (j < nwords) {
-            const uint64_t e0 = uint64_t(j) * 32;
-            unres = (ecount - e0 >= 32) ? ~0u : ((1u << uint32_t(ecount - e0)) - 1u);
-        }
+    uint32_t *win = s_win[warp];
+    for (uint32_t ch = blockIdx.x * kCheckWarps + warp; ch * 64 < nwords; ch += gridDim.x * kCheckWarps) {
+        const uint32_t J = ch * 64;
+        // stage the windows: class array k, words dlo / 32 + J + [0, nstage)
+        const uint32_t *src = bp.map + (dlo >> 5) + J;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            for (uint32_t i = lane; i < nstage; i += 32) win[k * kWin + i] = __ldg(src + size_t(k) * bp.wpc + i);
+        __syncwarp();
+        const uint32_t jA = J + lane, jB = J + 32 + lane;
+        uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+        const uint32_t chunk_min = idx0 + 15u * 32u * J;  // smallest even index of this chunk
         for (uint32_t c = 0; c < ncand; ++c) {
-            if (!__any_sync(~0u, unres)) break;
-            const uint32_t pos = s_pos[c] + 32 * j;
-            const uint32_t *wk = map + s_koff[c] + (pos >> 5);
-            const uint32_t lo = __ldg(wk);
-            uint32_t hi = __shfl_down_sync(~0u, lo, 1);
-            if (lane == 31) hi = __ldg(wk + 1);
-            const uint32_t w = __funnelshift_r(lo, hi, pos & 31);
-            const uint32_t hit = unres & w;
-            const uint32_t cnt = __reduce_add_sync(~0u, __popc(hit));
+            if (!__any_sync(~0u, uA | uB)) break;
+            const uint32_t e = s_ent[c];
+            const uint32_t *wk = win + (e >> 13) * kWin + (e & 0xFF) + lane;
+            const uint32_t sh = (e >> 8) & 31;
+            const uint32_t hA = uA & __funnelshift_r(wk[0], wk[1], sh);
+            const uint32_t hB = uB & __funnelshift_r(wk[32], wk[33], sh);
+            const uint32_t cnt = __reduce_add_sync(~0u, __popc(hA) + __popc(hB));
             if (cnt) {
-                const uint32_t mine = hit ? idx0 + 15u * (32u * j + __ffs(hit) - 1u) : kNone;
-                const uint32_t mn = __reduce_min_sync(~0u, mine);
-                if (lane == 0) {
-                    atomicAdd(&s_hist[c], cnt);
-                    if (mn < s_first[c]) atomicMin(&s_first[c], mn);
+                if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
+                    const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
+                                             : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
+                    const uint32_t mn = __reduce_min_sync(~0u, mine);
+                    if (lane == 0) atomicMin(&s_first[c], mn);
                 }
+                if (lane == 0) atomicAdd(&s_hist[c], cnt);
                 if (sp.pn) {
-                    const uint16_t pv = s_p[c];
-                    uint32_t h = hit;
-                    while (h) {
-                        const uint32_t b = __ffs(h) - 1u;
-                        sp.pn[idx0 + 15u * (32u * j + b)] = pv;
-                        h &= h - 1u;
-                    }
+                    write_pn(sp.pn, idx0, jA, hA, s_p[c]);
+                    write_pn(sp.pn, idx0, jB, hB, s_p[c]);
                 }
-                unres &= ~hit;
+                uA &= ~hA;
+                uB &= ~hB;
             }
         }
-        while (unres) {
-            const uint32_t b = __ffs(unres) - 1u;
-            append_leftover(sp.res, n0 + 30ull * (32ull * j + b));
-            unres &= unres - 1u;
+        while (uA) {
+            const uint32_t b = __ffs(uA) - 1u;
+            append_leftover(sp.res, n0 + 30ull * (32ull * jA + b));
+            uA &= uA - 1u;
         }
+        while (uB) {
+            const uint32_t b = __ffs(uB) - 1u;
+            append_leftover(sp.res, n0 + 30ull * (32ull * jB + b));
+            uB &= uB - 1u;
+        }
+        __syncwarp();
     }
     __syncthreads();
     for (uint32_t c = tid; c < ncand; c += blockDim.x) {
@@ -193,10 +239,10 @@ void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gb
         gbk::k_check_low<<<uint32_t(blocks), 256, 0, st>>>(bp, sp, ct.cand);
         return;
     }
-    // words per class ~ evens / 15 / 32; 8 warps per CTA, a few chunks each
+    // words per class ~ evens / 15 / 32; 8 warps per CTA, chunks of 64 words
     const uint64_t words = (evens / 15 + 32) / 32 + 1;
-    uint64_t bx = (words + 8 * 32 - 1) / (8 * 32);
-    const uint64_t cap = uint64_t(sm_count) * 4;  // per class: the 15 classes share the GPU
+    uint64_t bx = (words + gbk::kCheckWarps * 64 - 1) / (gbk::kCheckWarps * 64);
+    const uint64_t cap = uint64_t(sm_count) * 2;  // per class: the 15 classes share the GPU
     if (bx > cap) bx = cap;
     if (bx < 1) bx = 1;
     dim3 grid(uint32_t(bx), GBC_NCLASS);

@@ -19,6 +19,8 @@
 //             and the 17..29 skip of goldbach.cl:638-748).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "gbc_common.cuh"
 
 namespace gbk {
@@ -147,6 +149,61 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
     for (uint32_t i = tid; i < tw / 4; i += bs) dst[i] = src[i];
 }
 
+// x mod p, exactly, for x < p * 2^32 and 2^7 <= p < 2^32, without a
+// division: a float estimate of the quotient (error below 2^10 for these
+// bounds), an exact 64-bit remainder, a second float estimate of the now
+// small quotient (error below 1), and a final +-p correction. rp = 1/p
+// rounded to nearest.
+__device__ __forceinline__ uint32_t mod_below(uint64_t x, uint32_t p, float rp)
+{
+    const uint32_t qe = __float2uint_rz(__ull2float_rz(x) * rp);
+    int64_t r = int64_t(x - uint64_t(qe) * p);
+    const int32_t q2 = __float2int_rn(__ll2float_rz(r) * rp);
+    r -= int64_t(q2) * p;
+    if (r < 0) r += p;
+    if (r >= int64_t(p)) r -= p;
+    return uint32_t(r);
+}
+
+// a + d mod p for a, d < p without overflow
+__device__ __forceinline__ uint32_t addmod(uint32_t a, uint32_t d, uint32_t p)
+{
+    return a >= p - d ? a - (p - d) : a + d;
+}
+
+// Marks class k's multiples p m of the pass, m coprime to 30 and to 7..23,
+// from class bit t on: read the word, clear with an atomic AND only if the
+// bit is still set.
+template <uint32_t K>
+__device__ __forceinline__ void large_walk(const BatchParams &bp, uint32_t t, uint32_t p, uint32_t pi1, uint32_t pi2,
+                                           uint32_t bm1, uint32_t bm2, const uint32_t *s_skip)
+{
+    constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
+    constexpr uint32_t u = (0x1D1713110D0B0701ull >> (8 * K)) & 0xFF;
+    const uint32_t nblk = bp.nblk;
+    if (t >= nblk) return;
+    uint32_t *wk = bp.map + size_t(K) * bp.wpc;
+    // multiplier m = q / p modulo 1001 and 7429: m = q p^-1, q = base + 30 t + u
+    uint32_t m1 = (bm1 + (30 * (t % kSkip1) + u) % kSkip1) % kSkip1 * pi1 % kSkip1;
+    uint32_t m2 = (bm2 + (30 * (t % kSkip2) + u) % kSkip2) % kSkip2 * pi2 % kSkip2;
+    for (;;) {
+        const uint32_t sk = ((s_skip[m1 >> 5] >> (m1 & 31)) | (s_skip[kW1 + (m2 >> 5)] >> (m2 & 31))) & 1u;
+        if (!sk) {
+            uint32_t *a = wk + (t >> 5);
+            const uint32_t bit = 1u << (t & 31);
+            if (__ldcg(a) & bit) atomicAnd(a, ~bit);
+        }
+        if (nblk - t <= p) break;
+        t += p;
+        m1 += 30;
+        if (m1 >= kSkip1) m1 -= kSkip1;
+        m2 += 30;
+        if (m2 >= kSkip2) m2 -= kSkip2;
+    }
+}
+
+// One pass of the large primes over class bits [0, nblk) of the map at
+// bp.map (bp.base already moved to the pass's first block).
 __global__ void __launch_bounds__(256) k_large(BatchParams bp)
 {
     __shared__ uint32_t s_skip[(kSkip1 + 31) / 32 + (kSkip2 + 31) / 32];
@@ -155,38 +212,53 @@ __global__ void __launch_bounds__(256) k_large(BatchParams bp)
     for (uint32_t i = threadIdx.x; i < kW1 + (kSkip2 + 31) / 32; i += blockDim.x) s_skip[i] = bp.skip_tab[i];
     for (uint32_t i = threadIdx.x; i < kSkip1 + kSkip2; i += blockDim.x) s_inv[i] = bp.inv_tab[i];
     __syncthreads();
-    const uint32_t bm1 = uint32_t(bp.base % kSkip1), bm2 = uint32_t(bp.base % kSkip2);
-    const uint32_t nblk = bp.nblk;
+    const uint64_t base = bp.base;
+    const uint32_t bm1 = uint32_t(base % kSkip1), bm2 = uint32_t(base % kSkip2);
+    const uint32_t bhi = uint32_t(base >> 32), blo = uint32_t(base);
     for (uint32_t i = bp.n_mid + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_all;
          i += gridDim.x * blockDim.x) {
         const uint32_t p = bp.primes[i];
-        uint32_t x[8];
-        first_bits8(bp.base, nblk, p, x);
+        const float rp = __frcp_rn(float(p));
+        // r = base mod p by two base-2^32 digits
+        uint32_t r = mod_below(bhi, p, rp);
+        r = mod_below((uint64_t(r) << 32) | blo, p, rp);
+        const uint32_t iv = inv30_mod(p);
+        // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
+        const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
+        const uint32_t d2 = addmod(iv, iv, p), d4 = addmod(d2, d2, p), d6 = addmod(d4, d2, p);
         const uint32_t pi1 = s_inv[p % kSkip1], pi2 = s_inv[kSkip1 + p % kSkip2];
-#pragma unroll 1
+        const bool need_pp = uint64_t(p) * p > base;  // only near the bottom of the range
+        uint32_t c = iv;
+        uint32_t t[8];
+#pragma unroll
         for (uint32_t k = 0; k < 8; ++k) {
-            uint32_t t = x[k];
-            if (t == kNone) continue;
-            uint32_t *wk = bp.map + size_t(k) * bp.wpc;
-            const uint32_t u = unit30(k);
-            // multiplier m = q / p modulo 1001 and 7429: m = q p^-1
-            uint32_t m1 = (bm1 + uint32_t((30ull * t + u) % kSkip1)) % kSkip1 * pi1 % kSkip1;
-            uint32_t m2 = (bm2 + uint32_t((30ull * t + u) % kSkip2)) % kSkip2 * pi2 % kSkip2;
-            for (;;) {
-                const uint32_t sk = ((s_skip[m1 >> 5] >> (m1 & 31)) | (s_skip[kW1 + (m2 >> 5)] >> (m2 & 31))) & 1u;
-                if (!sk) {
-                    uint32_t *a = wk + (t >> 5);
-                    const uint32_t bit = 1u << (t & 31);
-                    if (__ldcg(a) & bit) atomicAnd(a, ~bit);
+            uint32_t x = tb - c;
+            if (tb < c) x += p;
+            t[k] = x;
+            const uint32_t d = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
+            c = addmod(c, d, p);
+        }
+        if (need_pp) {
+            const uint64_t pp = uint64_t(p) * p;
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                const uint64_t u = unit30(k);
+                const uint64_t q = base + 30ull * t[k] + u;
+                if (q < pp) {
+                    const uint64_t tmin = (pp - base - u + 29) / 30;
+                    const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
+                    t[k] = tt < bp.nblk ? uint32_t(tt) : kNone;
                 }
-                if (nblk - t <= p) break;
-                t += p;
-                m1 += 30;
-                if (m1 >= kSkip1) m1 -= kSkip1;
-                m2 += 30;
-                if (m2 >= kSkip2) m2 -= kSkip2;
             }
         }
+        large_walk<0>(bp, t[0], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<1>(bp, t[1], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<2>(bp, t[2], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<3>(bp, t[3], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<4>(bp, t[4], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<5>(bp, t[5], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<6>(bp, t[6], p, pi1, pi2, bm1, bm2, s_skip);
+        large_walk<7>(bp, t[7], p, pi1, pi2, bm1, bm2, s_skip);
     }
 }
 
@@ -228,14 +300,27 @@ void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStrea
     gbk::k_tile<<<grid, 1024, smem, st>>>(bp, gi);
 }
 
-void launch_large(const gbk::BatchParams &bp, cudaStream_t st)
+int launch_large(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st)
 {
-    if (bp.n_all <= bp.n_mid) return;
+    if (bp.n_all <= bp.n_mid) return 0;
     const uint32_t n = bp.n_all - bp.n_mid;
     uint32_t blocks = uint32_t(sm_count_cached()) * 8;
     const uint32_t need = (n + 255) / 256;
     if (blocks > need) blocks = need;
-    gbk::k_large<<<blocks, 256, 0, st>>>(bp);
+    // passes of pass_mb megabytes of map (8 class slices of pass bits / 8
+    // bytes each), so the random marks of a pass stay in L2
+    uint64_t pass_bits = (uint64_t(pass_mb ? pass_mb : 48) << 20) & ~uint64_t(31);
+    if (pass_bits < 32) pass_bits = 32;
+    int launches = 0;
+    for (uint64_t lo = 0; lo < bp.nblk; lo += pass_bits) {
+        gbk::BatchParams q = bp;
+        q.base = bp.base + 30 * lo;
+        q.nblk = uint32_t(std::min<uint64_t>(bp.nblk - lo, pass_bits));
+        q.map = bp.map + (lo >> 5);
+        gbk::k_large<<<blocks, 256, 0, st>>>(q);
+        ++launches;
+    }
+    return launches;
 }
 
 }  // namespace gbh

@@ -59,7 +59,10 @@ typedef struct gbc_config {
     uint32_t p_mid;          /* primes <= p_mid: shared-memory tiles; above: large-prime kernel (default 2^22) */
     uint32_t want_pn;        /* 1: slots also hold a per-even u16 p(n) buffer */
     int32_t device;          /* CUDA device ordinal (default 0) */
-    uint32_t reserved[7];
+    uint32_t large_pass_mb;  /* class-map megabytes one pass of the large-prime kernel covers (default
+                                4096: one pass per batch; smaller passes keep the marks in L2 but repeat
+                                the per-prime setup) */
+    uint32_t reserved[6];
 } gbc_config;
 
 typedef struct gbc_ctx gbc_ctx;
