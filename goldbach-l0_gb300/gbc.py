@@ -76,6 +76,9 @@ SIGNATURES = {
     "gbc_launch_count": (C.c_uint64, [C.c_void_p]),
     "gbc_verify_range": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(RunResult), C.c_char_p,
                                    C.c_uint64, C.POINTER(C.c_uint16)]),
+    "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                        C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 
 _lib = None

@@ -21,6 +21,7 @@
 #ifndef GBC_H
 #define GBC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -190,6 +191,44 @@ typedef struct gbc_run_result {
  * in flight, fail closed on any error. */
 int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gbc_run_result *res, char *line,
                      uint64_t line_cap, uint16_t *pn);
+
+/* ---- allocation-free class map ---------------------------------------------
+ * This entry point has no counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: code running while a CUDA stream
+ * is being captured (an allocation there breaks or invalidates the capture),
+ * code inside another framework's memory pool with a fixed device budget,
+ * and latency-critical paths where cudaMalloc's implicit device-wide
+ * synchronization is not acceptable. It needs no gbc_ctx.
+ *
+ * Builds the exact mod-30 class map of q in [q_lo, q_hi] (the tile sieve's
+ * output: bit t of class array k <-> q = base + 30 t + u_k, u = 1, 7, 11,
+ * 13, 17, 19, 23, 29, class k at d_map + k * wpc) into d_map, a device
+ * buffer of map_words u32 the caller owns, on the given CUDA stream (a
+ * cudaStream_t; NULL = the default stream). d_primes (device, caller-owned)
+ * holds the odd primes 3, 5, 7, ... ascending, nprimes of them, the last
+ * one max_prime, and max_prime^2 >= q_hi. *base_out, *nblk_out and *wpc_out
+ * (each may be NULL) receive the layout; the call returns them and
+ * GBC_E_ARG without launching anything when map_words < 8 * wpc, so a
+ * caller can size d_map first. err (may be NULL) receives a message on any
+ * error.
+ *
+ * Limits: nprimes <= GBC_NOALLOC_MAX_PRIMES (131072 primes: q_hi up to
+ * about 3e12) and q_hi - q_lo <= GBC_NOALLOC_MAX_SPAN (2^30); larger
+ * requests are rejected with GBC_E_ARG. The sieve's scratch (pattern
+ * words, a reciprocal and eight first class bits per prime: 4.5 MiB) is a
+ * fixed device array inside this library, which every GPU that loads the
+ * library keeps until the process exits. The first call on a device looks
+ * up that array's address and writes its constant part, so make the first
+ * call on each device before any stream capture. Every call uses the same
+ * array: calls whose kernels overlap on the GPU (two streams, or two
+ * threads) race on it and must be ordered by the caller. This function
+ * calls no cudaMalloc, cudaFree or other allocating routine. */
+#define GBC_NOALLOC_MAX_PRIMES 131072u
+#define GBC_NOALLOC_MAX_SPAN 1073741824ull
+int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_t *d_primes, uint32_t nprimes,
+                          uint32_t max_prime, uint32_t *d_map, uint64_t map_words, uint64_t *base_out,
+                          uint32_t *nblk_out, uint32_t *wpc_out, void *stream, char *err, size_t err_cap);
 
 #ifdef __cplusplus
 }
