@@ -150,7 +150,7 @@ def main():
     ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--p-mid", type=int, default=0)
     ap.add_argument("--large-pass-mb", type=int, default=0)

@@ -94,7 +94,8 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
         const uint32_t p = ct.cand[ci];
         const uint32_t u = (r + 30 - p % 30) % 30;
         const uint32_t d = uint32_t((n0 - bp.base - p - u) / 30) - dlo;
-        s_ent[c] = (d >> 5) | ((d & 31) << 8) | (class_of(u) << 13);
+        // word offset of the window in the warp's staging area | shift << 16
+        s_ent[c] = (class_of(u) * kWin + (d >> 5)) | ((d & 31) << 16);
         s_p[c] = uint16_t(p);
         s_ci[c] = uint16_t(ci);
         s_hist[c] = 0;
@@ -115,29 +116,52 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
         const uint32_t jA = J + lane, jB = J + 32 + lane;
         uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
         const uint32_t chunk_min = idx0 + 15u * 32u * J;  // smallest even index of this chunk
-        for (uint32_t c = 0; c < ncand; ++c) {
-            if (!__any_sync(~0u, uA | uB)) break;
-            const uint32_t e = s_ent[c];
-            const uint32_t *wk = win + (e >> 13) * kWin + (e & 0xFF) + lane;
-            const uint32_t sh = (e >> 8) & 31;
-            const uint32_t hA = uA & __funnelshift_r(wk[0], wk[1], sh);
-            const uint32_t hB = uB & __funnelshift_r(wk[32], wk[33], sh);
-            const uint32_t cnt = __reduce_add_sync(~0u, __popc(hA) + __popc(hB));
-            if (cnt) {
-                if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
-                    const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
-                                             : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
-                    const uint32_t mn = __reduce_min_sync(~0u, mine);
-                    if (lane == 0) atomicMin(&s_first[c], mn);
-                }
-                if (lane == 0) atomicAdd(&s_hist[c], cnt);
-                if (sp.pn) {
-                    write_pn(sp.pn, idx0, jA, hA, s_p[c]);
-                    write_pn(sp.pn, idx0, jB, hB, s_p[c]);
-                }
-                uA &= ~hA;
-                uB &= ~hB;
+        const uint32_t *wl = win + lane;
+        // records the hits hA / hB of candidate c (uA / uB already updated)
+        auto record = [&](uint32_t c, uint32_t hA, uint32_t hB, uint32_t cnt) {
+            if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
+                const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
+                                         : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
+                const uint32_t mn = __reduce_min_sync(~0u, mine);
+                if (lane == 0) atomicMin(&s_first[c], mn);
             }
+            if (lane == 0) atomicAdd(&s_hist[c], cnt);
+            if (sp.pn) {
+                write_pn(sp.pn, idx0, jA, hA, s_p[c]);
+                write_pn(sp.pn, idx0, jB, hB, s_p[c]);
+            }
+        };
+        uint32_t c = 0;
+        // two candidates per trip: their window reads are independent; the
+        // second one only tests what the first one left
+        for (; c + 1 < ncand; c += 2) {
+            if (!__any_sync(~0u, uA | uB)) break;
+            const uint32_t e0 = s_ent[c], e1 = s_ent[c + 1];
+            const uint32_t *w0 = wl + (e0 & 0xFFFF), *w1 = wl + (e1 & 0xFFFF);
+            const uint32_t s0 = e0 >> 16, s1 = e1 >> 16;
+            const uint32_t a0 = __funnelshift_r(w0[0], w0[1], s0), b0 = __funnelshift_r(w0[32], w0[33], s0);
+            const uint32_t a1 = __funnelshift_r(w1[0], w1[1], s1), b1 = __funnelshift_r(w1[32], w1[33], s1);
+            const uint32_t hA0 = uA & a0, hB0 = uB & b0;
+            uA ^= hA0;
+            uB ^= hB0;
+            const uint32_t hA1 = uA & a1, hB1 = uB & b1;
+            uA ^= hA1;
+            uB ^= hB1;
+            const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
+            const uint32_t cnt1 = __reduce_add_sync(~0u, __popc(hA1) + __popc(hB1));
+            if (cnt0) record(c, hA0, hB0, cnt0);
+            if (cnt1) record(c + 1, hA1, hB1, cnt1);
+        }
+        if (c < ncand && __any_sync(~0u, uA | uB)) {
+            const uint32_t e0 = s_ent[c];
+            const uint32_t *w0 = wl + (e0 & 0xFFFF);
+            const uint32_t s0 = e0 >> 16;
+            const uint32_t hA0 = uA & __funnelshift_r(w0[0], w0[1], s0);
+            const uint32_t hB0 = uB & __funnelshift_r(w0[32], w0[33], s0);
+            uA ^= hA0;
+            uB ^= hB0;
+            const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
+            if (cnt0) record(c, hA0, hB0, cnt0);
         }
         while (uA) {
             const uint32_t b = __ffs(uA) - 1u;

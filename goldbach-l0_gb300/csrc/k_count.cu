@@ -165,6 +165,20 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegPara
     }
     if (err) atomicOr(&sp.res->err, err);
 
+    // warp reductions of the 64-bit values first (shared 64-bit min / max /
+    // add contended by a whole CTA would serialize), then one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long hs = __shfl_xor_sync(~0u, hsum, o);
+        const unsigned long long gm = __shfl_xor_sync(~0u, gmax, o);
+        const unsigned long long cf = __shfl_xor_sync(~0u, cfirst, o);
+        const unsigned long long cl = __shfl_xor_sync(~0u, clast, o);
+        hsum += hs;
+        if (gm > gmax) gmax = gm;
+        if (cf < cfirst) cfirst = cf;
+        if (cl > clast) clast = cl;
+    }
+
     // block reductions
     const uint32_t r0 = __reduce_add_sync(~0u, __popc(c[0])), r1 = __reduce_add_sync(~0u, __popc(c[1]));
     const uint32_t r2 = __reduce_add_sync(~0u, __popc(c[2])), r3 = __reduce_add_sync(~0u, __popc(c[3]));
@@ -185,11 +199,11 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegPara
         atomicAdd(&s_cnt[9], t1);
         atomicAdd(&s_cnt[10], t2);
         atomicAdd(&s_nprime, (unsigned long long)nhs);
+        atomicAdd(&s_hash, (unsigned long long)hsum);
+        if (gmax) atomicMax(&s_gmax, gmax);
+        if (cfirst != ~0ull) atomicMin(&s_first, cfirst);
+        if (clast) atomicMax(&s_last, clast);
     }
-    atomicAdd(&s_hash, (unsigned long long)hsum);
-    if (gmax) atomicMax(&s_gmax, gmax);
-    if (cfirst != ~0ull) atomicMin(&s_first, cfirst);
-    if (clast) atomicMax(&s_last, clast);
     __syncthreads();
     gbc_segment_result *res = sp.res;
     for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x)
