@@ -154,6 +154,8 @@ def main():
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--p-mid", type=int, default=0)
     ap.add_argument("--large-pass-mb", type=int, default=0)
+    ap.add_argument("--hl-mode", type=int, default=0)
+    ap.add_argument("--hl-pass-mb", type=int, default=0)
     ap.add_argument("--ref-evens", type=int, default=1_000_000)
     ap.add_argument("--cpu-evens", type=int, default=4_000_000)
     ap.add_argument("--no-cpu", action="store_true")
@@ -171,7 +173,8 @@ def main():
     limit = allb[-1][-1][1]
     evens_per_step = sum((e - s) // 2 + 1 for s, e in allb[0])
     with gbc.Context(limit=limit, segment_even=SEG, max_batch=args.batch, tile_log2=args.tile_log2,
-                     p_mid=args.p_mid, large_pass_mb=args.large_pass_mb) as ctx:
+                     p_mid=args.p_mid, large_pass_mb=args.large_pass_mb, hl_mode=args.hl_mode,
+                     hl_pass_mb=args.hl_pass_mb) as ctx:
         # ---- device-time value: one slot, steps back to back, CUDA events of the launching stream
         for i in range(args.warmup):
             ctx.enqueue_batch(0, allb[i], limit)

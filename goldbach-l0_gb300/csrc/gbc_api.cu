@@ -158,6 +158,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.tile_log2) cfg.tile_log2 = 20;
     if (!cfg.p_mid) cfg.p_mid = 1u << 22;
     if (!cfg.large_pass_mb) cfg.large_pass_mb = 4096;  // one pass: the per-prime setup outweighs L2 misses
+    if (!cfg.mtab_max_gb) cfg.mtab_max_gb = 48;
+    if (!cfg.hl_pass_mb) cfg.hl_pass_mb = 4096;  // one pass: the divisions outweigh L2 misses
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
@@ -195,6 +197,22 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (ctx->i_warp > ctx->n_mid) ctx->i_warp = ctx->n_mid;
     std::vector<uint32_t> magic(ctx->n_mid);
     for (uint32_t i = 0; i < ctx->n_mid; ++i) magic[i] = uint32_t((1ull << 32) / pr[i]);
+    // hit lists: every prime >= p_hl, p_hl above p_mid, above the cube root
+    // of the largest q (the prime-multiplier rule needs p >= cbrt(q)), and
+    // high enough that the table of multipliers m <= limit / p_hl fits the
+    // HBM budget
+    {
+        uint64_t c = uint64_t(std::cbrt(double(cfg.limit + 3))) + 2;
+        while (c * c * c < cfg.limit + 3) ++c;
+        const uint64_t budget_m = uint64_t(cfg.mtab_max_gb) * 1000000000ull * 30;
+        const uint64_t by_budget = (cfg.limit + 3) / budget_m + 1;
+        ctx->p_hl = std::max<uint64_t>({uint64_t(cfg.p_mid) + 1, c, by_budget});
+        ctx->n_hl = uint32_t(std::lower_bound(pr.begin(), pr.end(), ctx->p_hl) - pr.begin());
+        if (ctx->n_hl < ctx->n_mid) ctx->n_hl = ctx->n_mid;
+        const bool wide = double(cfg.max_batch) * double(cfg.segment_even) >= 1e9;
+        ctx->hl_on = cfg.hl_mode == 1 || (cfg.hl_mode == 0 && wide);
+        if (ctx->n_hl >= pr.size()) ctx->hl_on = false;
+    }
 
     // pattern groups (primes 7..67): canonical bit y = (y mod P coprime to P)
     std::vector<uint32_t> pat;
@@ -289,6 +307,7 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
         cudaFree(s.pn);
         if (s.st) cudaStreamDestroy(s.st);
     }
+    cudaFree(ctx->mtab);
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_magic);
     cudaFree(ctx->d_pat);
@@ -365,6 +384,7 @@ int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl,
     bp.n_mid = std::min(ctx->n_mid, bp.n_all);
     if (bp.n_mid < bp.i0) bp.n_mid = bp.i0;
     bp.i_warp = std::min(std::max(ctx->i_warp, bp.i0), bp.n_mid);
+    bp.n_hl = ctx->hl_on ? std::min(std::max(ctx->n_hl, bp.n_mid), bp.n_all) : bp.n_all;
 
     s.segs.assign(nseg, gbk::SegParams{});
     for (int i = 0; i < nseg; ++i) {
@@ -385,6 +405,80 @@ int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl,
     return GBC_OK;
 }
 
+// Makes the prime-multiplier table cover the multipliers [need0, need1]:
+// the primes m of the range, one byte per block of 30 (bit k <-> m = m0 +
+// 30 i + u_k), sieved by the batch kernels themselves in chunks and
+// rewritten to bytes (the reference's mt_build, src/verifier.cpp:1444-1508,
+// goldbach.cl:3181-3242). Rebuilt only when a batch needs multipliers
+// outside it; both slots are drained first (they read the table).
+static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
+{
+    if (ctx->mtab && ctx->mtab_m0 <= need0 && need1 <= ctx->mtab_m1) return GBC_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (auto &s : ctx->slot) CK(cudaStreamSynchronize(s.st));
+    const uint64_t cap_bytes = uint64_t(ctx->cfg.mtab_max_gb) * 1000000000ull;
+    // headroom for the batches that follow (a slice moves need1 by ~1e-4 per batch)
+    uint64_t lo = need0 - need0 / 64, hi = need1 + need1 / 64 + (1u << 20);
+    if ((hi - lo) / 30 + 1 > cap_bytes) {
+        lo = need0;
+        hi = need1;
+    }
+    lo = lo / 30 * 30;
+    const uint64_t nbytes = ((hi - lo) / 30 + 1 + 31) / 32 * 32;
+    if (nbytes > cap_bytes) return fail(ctx, GBC_E_ARG, "prime-multiplier table above its HBM budget");
+    hi = lo + 30 * nbytes - 1;
+    cudaFree(ctx->mtab);
+    ctx->mtab = nullptr;
+    CK(cudaMalloc(&ctx->mtab, nbytes + 64));
+    // sieve [lo, hi] in chunks through a temporary class map
+    const uint32_t tb = 1u << ctx->cfg.tile_log2, tw = tb / 32;
+    const uint64_t chunk = uint64_t(1) << 28;  // blocks (bytes) per chunk, a multiple of 32
+    const uint64_t tiles = (chunk + 64 + tb - 1) / tb;
+    uint32_t *tmp = nullptr, *xf = nullptr;
+    CK(cudaMalloc(&tmp, size_t(8) * tiles * tw * 4 + kMapPadBytes));
+    CK(cudaMalloc(&xf, std::max<size_t>(size_t(8) * ctx->n_mid * 4, 4)));
+    cudaStream_t st = ctx->slot[0].st;
+    const auto &pr = ctx->primes;
+    for (uint64_t off = 0; off < nbytes; off += chunk) {
+        gbk::BatchParams b{};
+        b.base = lo + 30 * off;
+        b.nblk = uint32_t(std::min(chunk, nbytes - off));
+        b.qmax = b.base + 30ull * b.nblk;
+        b.tiles_pc = uint32_t((b.nblk + 64 + tb - 1) / tb);
+        b.wpc = b.tiles_pc * tw;
+        b.map = tmp;
+        b.primes = ctx->d_primes;
+        b.magic = ctx->d_magic;
+        b.xfirst = xf;
+        b.tile_log2 = ctx->cfg.tile_log2;
+        b.pat = ctx->d_pat;
+        b.skip_tab = ctx->d_skip;
+        b.inv_tab = ctx->d_inv;
+        b.err = ctx->slot[0].err;
+        uint64_t root = uint64_t(std::sqrt(double(b.qmax)));
+        while (root * root > b.qmax) --root;
+        while ((root + 1) * (root + 1) <= b.qmax) ++root;
+        b.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
+        b.i0 = std::min(ctx->i0, b.n_all);
+        b.n_mid = std::max(std::min(ctx->n_mid, b.n_all), b.i0);
+        b.i_warp = std::min(std::max(ctx->i_warp, b.i0), b.n_mid);
+        b.n_hl = b.n_all;
+        gbh::launch_xfirst(b, st);
+        gbh::launch_tile(b, ctx->gi, st);
+        gbh::launch_large(b, ctx->cfg.large_pass_mb, st);
+        gbh::launch_wheel_bytes(b, ctx->mtab + off / 4, st);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    cudaFree(tmp);
+    cudaFree(xf);
+    ctx->mtab_m0 = lo;
+    ctx->mtab_m1 = hi;
+    ctx->mtab_builds += 1;
+    ctx->mtab_build_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return GBC_OK;
+}
+
 extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags,
                                  int nseg, uint64_t limit)
 {
@@ -393,9 +487,20 @@ extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bou
     if (s.pending) return fail(ctx, GBC_E_STATE, "slot already holds an uncollected batch");
     gbk::BatchParams bp{};
     if (int r = gbh_plan_batch(ctx, s, seg_bounds, seg_flags, nseg, limit, bp)) return r;
+    if (bp.n_hl < bp.n_all) {
+        // multipliers of the batch's q range for its hit-listed primes
+        const uint64_t q1 = bp.base + 30ull * bp.nblk - 1;
+        const uint64_t need0 = bp.base / ctx->primes[bp.n_all - 1];
+        const uint64_t need1 = q1 / ctx->primes[bp.n_hl];
+        if (int r = ensure_mtab(ctx, need0, need1)) return r;
+        bp.mtab = ctx->mtab;
+        bp.m0 = ctx->mtab_m0;
+        bp.m1 = ctx->mtab_m1;
+    }
     s.bp = bp;
     s.nseg = nseg;
     cudaStream_t st = s.st;
+    CK(cudaMemsetAsync(s.err, 0, 4, st));
     CK(cudaMemsetAsync(s.res, 0, size_t(nseg) * sizeof(gbc_segment_result), st));
     for (int i = 0; i < nseg; ++i) {
         CK(cudaMemsetAsync(s.res[i].first, 0xFF, sizeof(s.res[i].first), st));
@@ -407,6 +512,7 @@ extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bou
     ctx->launches += 2;
     CK(cudaEventRecord(s.ev[1], st));
     ctx->launches += gbh::launch_large(bp, ctx->cfg.large_pass_mb, st);
+    ctx->launches += gbh::launch_hitlist(bp, ctx->cfg.hl_pass_mb, st);
     CK(cudaEventRecord(s.ev[2], st));
     for (int i = 0; i < nseg; ++i) {
         gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);
@@ -442,7 +548,14 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
         std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     CK(cudaMemcpy(out, s.res, size_t(nseg) * sizeof(gbc_segment_result), cudaMemcpyDeviceToHost));
+    uint32_t berr = 0;
+    CK(cudaMemcpy(&berr, s.err, 4, cudaMemcpyDeviceToHost));
     s.pending = false;
+    if (berr) {
+        char m[96];
+        std::snprintf(m, sizeof m, "device error flags 0x%x in the batch's sieve", berr);
+        return fail(ctx, GBC_E_DEVICE, m);
+    }
     if (times) {
         float a = 0, b = 0, c = 0, d = 0;
         cudaEventElapsedTime(&a, s.ev[0], s.ev[1]);

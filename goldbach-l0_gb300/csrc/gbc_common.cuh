@@ -77,6 +77,10 @@ struct BatchParams {
     const uint32_t *skip_tab; // bit tables: multipliers to skip (1001 then 7429 bits)
     const uint16_t *inv_tab;  // inverses mod 1001 then mod 7429 (0: none)
     uint32_t *err;            // device error word of the slot
+    // prime-multiplier table: primes [n_hl, n_all) mark only p m with m prime
+    uint32_t n_hl;            // first hit-listed prime (n_all: none)
+    const uint32_t *mtab;     // bit k of byte i <-> m = m0 + 30 i + u_k is prime
+    uint64_t m0, m1;          // the table covers m in [m0, m1]
 };
 
 struct GroupInfo {
@@ -112,6 +116,7 @@ constexpr uint32_t kErrTailOverflow = 1u << 1;
 constexpr uint32_t kErrGapRange = 1u << 2;
 constexpr uint32_t kErrNoPred = 1u << 3;
 constexpr uint32_t kErrRetry = 1u << 4;
+constexpr uint32_t kErrTable = 1u << 5;   // a multiplier outside the prime-multiplier table
 
 // ---------------------------------------------------------------------------
 // 64-bit Miller-Rabin in Montgomery form (the GPU retry of evens without a
@@ -184,6 +189,8 @@ namespace gbh {
 void launch_xfirst(const gbk::BatchParams &bp, cudaStream_t st);
 void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st);
 int launch_large(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st);
+int launch_hitlist(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st);
+void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st);
 void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
                   cudaStream_t st);
 void launch_retry(const gbk::SegParams &sp, cudaStream_t st);

@@ -42,6 +42,14 @@ struct gbc_ctx {
     Slot slot[2];
     std::string err;
     uint64_t launches = 0;
+    // prime-multiplier table (hit lists for the primes >= p_hl)
+    bool hl_on = false;
+    uint64_t p_hl = 0;
+    uint32_t n_hl = 0;                 // index of the first prime >= p_hl
+    uint32_t *mtab = nullptr;          // wheel-30 bytes of the primes in [mtab_m0, mtab_m1]
+    uint64_t mtab_m0 = 0, mtab_m1 = 0;
+    uint64_t mtab_builds = 0;
+    double mtab_build_ms = 0;
 };
 
 std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n);

@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256) k_large(BatchParams bp)
     const uint64_t base = bp.base;
     const uint32_t bm1 = uint32_t(base % kSkip1), bm2 = uint32_t(base % kSkip2);
     const uint32_t bhi = uint32_t(base >> 32), blo = uint32_t(base);
-    for (uint32_t i = bp.n_mid + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_all;
+    for (uint32_t i = bp.n_mid + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_hl;
          i += gridDim.x * blockDim.x) {
         const uint32_t p = bp.primes[i];
         const float rp = __frcp_rn(float(p));
@@ -262,9 +262,143 @@ __global__ void __launch_bounds__(256) k_large(BatchParams bp)
     }
 }
 
+// floor(x / p) and x mod p for any 64-bit x and 2^7 <= p < 2^32, without a
+// division: two base-2^32 digits, each remainder by mod_below, each digit
+// of the quotient exactly as (digit - remainder) * p^-1 mod 2^32 (the
+// quotient digit is below 2^32, so the multiple of p divides exactly).
+__device__ __forceinline__ uint64_t divmod_u64(uint64_t x, uint32_t p, float rp, uint32_t pinv, uint32_t &rem)
+{
+    const uint32_t hi = uint32_t(x >> 32), lo = uint32_t(x);
+    const uint32_t rh = mod_below(hi, p, rp);
+    const uint32_t qh = (hi - rh) * pinv;
+    const uint64_t x2 = (uint64_t(rh) << 32) | lo;
+    rem = mod_below(x2, p, rp);
+    const uint32_t ql = uint32_t(x2 - rem) * pinv;
+    return (uint64_t(qh) << 32) | ql;
+}
+
+// p^-1 mod 2^32 for odd p (Newton: the correct low bits double each step)
+__device__ __forceinline__ uint32_t inv_mod_2_32(uint32_t p)
+{
+    uint32_t x = p;  // p * p = 1 (mod 8)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x *= 2u - p * x;
+    return x;
+}
+
+// Hit lists through the prime-multiplier table (the reference's mt_build /
+// hl_harvest_mt / hl_apply, kernels/goldbach.cl:3181-3471): for a prime
+// p >= cbrt(q), a composite multiplier m of q = p m has a prime factor below
+// p, which marks q already, so only prime m matter. One thread per prime
+// p: the primes m in [ceil(Q0 / p), floor(Q1 / p)] are one contiguous run of
+// bytes of the table; each gives q = p m, whose class bit is cleared with an
+// atomic AND. Every such q is a semiprime whose factors are both above the
+// sieving bound of the other stages, so the bit is set and no read is needed.
+__global__ void __launch_bounds__(256) k_hitlist(BatchParams bp)
+{
+    // class array of q = p m from the classes of p and of m
+    __shared__ uint8_t s_cls[8][8];
+    if (threadIdx.x < 64) {
+        const uint32_t a = threadIdx.x >> 3, b = threadIdx.x & 7;
+        s_cls[a][b] = uint8_t(class_of(unit30(a) * unit30(b) % 30));
+    }
+    __syncthreads();
+    const uint64_t q0 = bp.base, q1 = bp.base + 30ull * bp.nblk - 1;
+    const uint64_t m0 = bp.m0;
+    for (uint32_t i = bp.n_hl + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_all;
+         i += gridDim.x * blockDim.x) {
+        const uint32_t p = bp.primes[i];
+        const float rp = __frcp_rn(float(p));
+        const uint32_t pinv = inv_mod_2_32(p);
+        uint32_t r0, r1;
+        uint64_t mlo = divmod_u64(q0, p, rp, pinv, r0);
+        mlo += r0 ? 1 : 0;
+        const uint64_t mhi = divmod_u64(q1, p, rp, pinv, r1);
+        if (mhi < mlo) continue;
+        if (mlo < m0 || mhi > bp.m1) {
+            atomicOr(bp.err, kErrTable);
+            continue;
+        }
+        const uint32_t kp = class_of(p % 30);
+        const uint64_t b0 = (mlo - m0) / 30, b1 = (mhi - m0) / 30;
+        for (uint64_t w = b0 >> 2; w <= (b1 >> 2); ++w) {
+            uint32_t v = bp.mtab[w];
+            while (v) {
+                const uint32_t j = __ffs(v) - 1u;
+                v &= v - 1u;
+                const uint32_t k = j & 7;
+                const uint64_t m = m0 + 30 * (4 * w + (j >> 3)) + unit30(k);
+                if (m < mlo || m > mhi) continue;
+                const uint64_t t = (uint64_t(p) * m - bp.base) / 30;
+                atomicAnd(bp.map + size_t(s_cls[kp][k]) * bp.wpc + (t >> 5), ~(1u << (t & 31)));
+            }
+        }
+    }
+}
+
+// The class arrays of a sieved range, rewritten as one byte per block of 30
+// (bit k = class k): one thread per class-array word, 32 bytes out.
+__global__ void __launch_bounds__(256) k_wheel_bytes(BatchParams bp, uint32_t *out)
+{
+    const uint32_t nw = (bp.nblk + 31) / 32;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
+        uint32_t a[8];
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) a[k] = bp.map[size_t(k) * bp.wpc + w];
+        const uint32_t valid = (w + 1) * 32 <= bp.nblk ? 32u : bp.nblk - w * 32;
+#pragma unroll
+        for (uint32_t o = 0; o < 8; ++o) {
+            uint32_t word = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+                const uint32_t b = 4 * o + j;
+                uint32_t byte = 0;
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) byte |= ((a[k] >> b) & 1u) << k;
+                if (b >= valid) byte = 0;
+                word |= byte << (8 * j);
+            }
+            out[size_t(w) * 8 + o] = word;
+        }
+    }
+}
+
 }  // namespace gbk
 
 namespace gbh {
+
+static int sm_count_cached();
+
+int launch_hitlist(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st)
+{
+    if (bp.n_all <= bp.n_hl) return 0;
+    const uint32_t n = bp.n_all - bp.n_hl;
+    uint32_t blocks = uint32_t(sm_count_cached()) * 8;
+    const uint32_t need = (n + 255) / 256;
+    if (blocks > need) blocks = need;
+    // passes over pass_mb megabytes of map: each prime redoes its two
+    // divisions per pass, and the pass's atomic marks stay in L2
+    uint64_t pass_bits = (uint64_t(pass_mb ? pass_mb : 48) << 20) & ~uint64_t(31);
+    if (pass_bits < 32) pass_bits = 32;
+    int launches = 0;
+    for (uint64_t lo = 0; lo < bp.nblk; lo += pass_bits) {
+        gbk::BatchParams q = bp;
+        q.base = bp.base + 30 * lo;
+        q.nblk = uint32_t(std::min<uint64_t>(bp.nblk - lo, pass_bits));
+        q.map = bp.map + (lo >> 5);
+        gbk::k_hitlist<<<blocks, 256, 0, st>>>(q);
+        ++launches;
+    }
+    return launches;
+}
+
+void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st)
+{
+    const uint32_t nw = (bp.nblk + 31) / 32;
+    uint32_t blocks = (nw + 255) / 256;
+    if (blocks > 65535) blocks = 65535;
+    gbk::k_wheel_bytes<<<blocks, 256, 0, st>>>(bp, out);
+}
 
 static int sm_count_cached()
 {

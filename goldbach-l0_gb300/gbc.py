@@ -28,7 +28,8 @@ ERRORS = {0: "ok", -1: "argument", -2: "cuda", -3: "device flag", -4: "timeout",
 class Config(C.Structure):
     _fields_ = [("limit", C.c_uint64), ("segment_even", C.c_uint64), ("max_batch", C.c_uint32),
                 ("tile_log2", C.c_uint32), ("p_mid", C.c_uint32), ("want_pn", C.c_uint32),
-                ("device", C.c_int32), ("large_pass_mb", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+                ("device", C.c_int32), ("large_pass_mb", C.c_uint32), ("hl_mode", C.c_uint32),
+                ("mtab_max_gb", C.c_uint32), ("hl_pass_mb", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class SegmentResult(C.Structure):
@@ -119,10 +120,11 @@ class Context:
     segments of `segment_even` integers."""
 
     def __init__(self, limit, segment_even=DEFAULT_SEGMENT, max_batch=8, tile_log2=0, p_mid=0, want_pn=False,
-                 device=0, large_pass_mb=0):
+                 device=0, large_pass_mb=0, hl_mode=0, mtab_max_gb=0, hl_pass_mb=0):
         self.lib = load()
         cfg = Config(limit=limit, segment_even=segment_even, max_batch=max_batch, tile_log2=tile_log2,
-                     p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, large_pass_mb=large_pass_mb)
+                     p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, large_pass_mb=large_pass_mb,
+                     hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, hl_pass_mb=hl_pass_mb)
         h = C.c_void_p()
         rc = self.lib.gbc_create(C.byref(cfg), C.byref(h))
         self.h = h

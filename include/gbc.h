@@ -63,7 +63,14 @@ typedef struct gbc_config {
     uint32_t large_pass_mb;  /* class-map megabytes one pass of the large-prime kernel covers (default
                                 4096: one pass per batch; smaller passes keep the marks in L2 but repeat
                                 the per-prime setup) */
-    uint32_t reserved[6];
+    uint32_t hl_mode;        /* prime-multiplier hit lists: 0 auto (on when a batch spans >= 1e9
+                                integers), 1 on, 2 off */
+    uint32_t mtab_max_gb;    /* HBM budget of the prime-multiplier table (default 48 GB); primes below
+                                limit / (30 * budget) keep the read-before-mark kernel */
+    uint32_t hl_pass_mb;     /* class-map megabytes one hit-list pass covers (default 4096: one pass;
+                                smaller passes keep the atomic marks in L2 but redo the per-prime
+                                divisions) */
+    uint32_t reserved[3];
 } gbc_config;
 
 typedef struct gbc_ctx gbc_ctx;

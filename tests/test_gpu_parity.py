@@ -97,6 +97,34 @@ def test_class_map_bit_exact(a, tile_log2):
     assert not bad, bad[:8]
 
 
+@pytest.mark.parametrize("a", [4 * 10**18, 9223372036853775808, gbc.MAX_LIMIT - 3_000_000])
+def test_hit_list_class_map_bit_exact(a):
+    """The prime-multiplier hit lists (every prime above ~1.7e7 marks only
+    p m with m prime) leave the same exact map: every bit against
+    Miller-Rabin."""
+    seg = 500_000
+    b = a + 2 * seg - 2
+    segs = gbc.segments_of(a, b, seg)
+    with gbc.Context(limit=b, segment_even=seg, max_batch=len(segs), hl_mode=1, mtab_max_gb=8) as c:
+        c.enqueue_batch(0, segs, b)
+        c.collect(0, len(segs))
+        base, nblk, wpc, w = c.map(0)
+    bad = []
+    for k in range(8):
+        for t in range(nblk):
+            q = base + 30 * t + U30[k]
+            if ((w[k * wpc + (t >> 5)] >> (t & 31)) & 1) != oracle.is_prime(q):
+                bad.append(q)
+    assert not bad, bad[:8]
+
+
+@pytest.mark.parametrize("idx", [2, 4, 5, 6, 7])
+def test_hit_list_stats_windows(idx):
+    start, limit, line = stats_windows()[idx]
+    with gbc.Context(limit=limit, segment_even=1_000_000, max_batch=4, hl_mode=1, mtab_max_gb=8) as c:
+        assert c.verify_range(start, limit)[1] == line
+
+
 def test_batched_equals_plain():
     a, b = 4_000_000_000_000_000_000, 4_000_000_000_060_000_000
     lines = []
