@@ -2,24 +2,32 @@
 """Benchmark of the GB300 dense Goldbach verify path.
 
 Workload: production segments of 467.5M integers at 4e18 + k * 467.5e6, k
-drawn from seed 1 in [0, 1e5) (the reference's production segment shape);
-a step is one batch of --batch consecutive segments (default 8: one sieve
-pass over one HBM-resident class map, then per-segment exact p(n) of every
-even, prime / twin / gap statistics and the class-map hash). Successive
-steps take successive batches, so no step repeats work; the class map of a
-batch (125 MB for 8 segments) and the sieving primes exceed what one step
-reuses from L2 (inputs larger than L2, see config.l2).
+drawn from seed 1 in [0, 1e5) (the reference's production segment shape).
+A step is one batch of --batch consecutive segments (default 16: one sieve
+pass over one HBM-resident class map of 250 MB, then per segment the
+checker, prime / twin / gap statistics and the class-map hash). Successive
+steps take successive batches, so no step repeats work, and a step's map
+and sieving primes (393 MB) exceed L2.
+
+Statistics mode (--sample-every, default 256): the reference's production
+mode -- every 256th segment of the run gets p(n) of every even (its
+GB_STATS_SAMPLE default), the others the funnel verify plus the exact p(n)
+of every even the plan leaves (which holds every even with p(n) >= 3000);
+primes, twins and the full gap walk on every segment. `exact_all` repeats
+the measurement with p(n) of every even on every segment.
 
 value  = evens verified per second over the timed steps, device time from
-         CUDA events on the launching stream (inputs resident in HBM).
+         CUDA events recorded on the launching stream around every stage
+         (inputs resident in HBM).
 e2e    = the same metric through the C ABI as a caller uses it: two slots in
          flight, gbc_enqueue_batch + gbc_collect, per-segment results copied
          to host memory inside the timed region, wall clock.
 --impl reference times the reference's CPU algorithm (the oracle's
-restatement of tests/stats_ref.cpp, run on all host cores) on a bounded
-sample of the same workload.
+restatement of tests/stats_ref.cpp: Miller-Rabin p(n) of every even, run on
+every host core) on a bounded sample of the same workload.
 """
 import argparse
+import ctypes
 import json
 import os
 import random
@@ -35,6 +43,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 SEG = 467_500_000
 METRIC = "G evens/s at 4e18, bit-exact stats"
+NPRIMES_4E18 = 98_222_287   # odd primes <= 2.0e9 = sqrt of the workload's end
 
 
 def workload_start():
@@ -49,6 +58,20 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from profiles/ncu_traffic.txt (one
+    ncu capture of the same workload; lines "kernel bytes_per_launch note")."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.txt")) as f:
+            for ln in f:
+                t = ln.split()
+                if len(t) >= 2 and t[0] == kernel:
+                    return float(t[1])
+    except OSError:
+        pass
+    return None
 
 
 class Clocks:
@@ -94,16 +117,22 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def batches(start, nbatch, batch):
+def batches(start, first_seg, nbatch, batch):
+    """nbatch batches of `batch` segments from segment index first_seg."""
     out = []
-    s = start
-    for _ in range(nbatch):
+    for b in range(nbatch):
         segs = []
-        for _ in range(batch):
-            segs.append((s, s + SEG - 2))
-            s += SEG
+        for j in range(batch):
+            i = first_seg + b * batch + j
+            s = start + i * SEG
+            segs.append((i, s, s + SEG - 2))
         out.append(segs)
     return out
+
+
+def seg_args(b, sample_every, gbc):
+    return [(s, e) for _, s, e in b], [0 if sample_every <= 1 or i % sample_every == 0 else gbc.SEG_VERIFY
+                                       for i, _, _ in b]
 
 
 def cpu_baseline(evens, start):
@@ -114,12 +143,11 @@ def cpu_baseline(evens, start):
     dt = time.perf_counter() - t0
     return {"value": evens / dt / 1e9, "unit": "G evens/s", "cores": threads, "kind": "port",
             "sample": f"{evens} evens from {start}: the oracle's restatement of tests/stats_ref.cpp "
-                      f"(Miller-Rabin p(n), primes, twins, gaps) on {threads} threads, {dt:.2f} s"}
+                      f"(Miller-Rabin p(n) of every even, primes, twins, gaps) on {threads} threads, {dt:.2f} s"}
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
     start = workload_start()
     per_step = args.ref_evens
@@ -144,6 +172,23 @@ def run_reference(args):
     return 0
 
 
+def device_run(ctx, bs, limit, sample_every, gbc):
+    """Steps back to back on one slot; per-stage device time from the ABI's
+    CUDA events on the launching stream."""
+    stage = {"tile": 0.0, "large": 0.0, "check": 0.0, "count": 0.0}
+    total = 0.0
+    for b in bs:
+        segs, flags = seg_args(b, sample_every, gbc)
+        ctx.enqueue_batch(0, segs, limit, flags)
+        _, t = ctx.collect(0, len(segs))
+        total += t.ms_total
+        stage["tile"] += t.ms_tile
+        stage["large"] += t.ms_large
+        stage["check"] += t.ms_check
+        stage["count"] += t.ms_count
+    return total, stage
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -151,13 +196,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--sample-every", type=int, default=256)
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--p-mid", type=int, default=0)
     ap.add_argument("--large-pass-mb", type=int, default=0)
     ap.add_argument("--hl-mode", type=int, default=0)
     ap.add_argument("--hl-pass-mb", type=int, default=0)
+    ap.add_argument("--plan-funnels", type=int, default=0)
     ap.add_argument("--ref-evens", type=int, default=1_000_000)
     ap.add_argument("--cpu-evens", type=int, default=4_000_000)
+    ap.add_argument("--exact-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -168,75 +216,79 @@ def main():
     import gbc
 
     start = workload_start()
-    nb = args.warmup + args.steps
-    allb = batches(start, 2 * nb, args.batch)
-    limit = allb[-1][-1][1]
-    evens_per_step = sum((e - s) // 2 + 1 for s, e in allb[0])
+    nb = args.warmup + 2 * args.steps + 2 + args.exact_steps
+    allb = batches(start, 0, nb, args.batch)
+    limit = allb[-1][-1][2]
+    evens_per_step = sum((e - s) // 2 + 1 for _, s, e in allb[0])
     with gbc.Context(limit=limit, segment_even=SEG, max_batch=args.batch, tile_log2=args.tile_log2,
                      p_mid=args.p_mid, large_pass_mb=args.large_pass_mb, hl_mode=args.hl_mode,
-                     hl_pass_mb=args.hl_pass_mb) as ctx:
-        # ---- device-time value: one slot, steps back to back, CUDA events of the launching stream
-        for i in range(args.warmup):
-            ctx.enqueue_batch(0, allb[i], limit)
-            ctx.collect(0, len(allb[i]))
+                     hl_pass_mb=args.hl_pass_mb, plan_funnels=args.plan_funnels) as ctx:
+        device_run(ctx, allb[:args.warmup], limit, args.sample_every, gbc)   # warm-up (builds the tables)
         launches0 = ctx.launches()
-        stage = {"tile": 0.0, "large": 0.0, "check": 0.0, "count": 0.0}
-        dev_ms = 0.0
+        timed = allb[args.warmup:args.warmup + args.steps]
         with Clocks() as clk:
             t0 = time.perf_counter()
-            for i in range(args.steps):
-                b = allb[args.warmup + i]
-                ctx.enqueue_batch(0, b, limit)
-                _, t = ctx.collect(0, len(b))
-                dev_ms += t.ms_total
-                stage["tile"] += t.ms_tile
-                stage["large"] += t.ms_large
-                stage["check"] += t.ms_check
-                stage["count"] += t.ms_count
+            dev_ms, stage = device_run(ctx, timed, limit, args.sample_every, gbc)
             wall = time.perf_counter() - t0
         launches = ctx.launches() - launches0
         value = evens_per_step * args.steps / (dev_ms / 1e3) / 1e9
-        # ---- e2e: the caller's loop, two slots in flight, results to host memory
-        off = nb
+        # e2e: the caller's loop, two slots in flight, results to host memory
+        off = args.warmup + args.steps
+        e2eb = allb[off:off + args.steps]
         for i in range(2):
-            ctx.enqueue_batch(i, allb[off + i], limit)
+            segs, flags = seg_args(e2eb[i], args.sample_every, gbc)
+            ctx.enqueue_batch(i, segs, limit, flags)
         t0 = time.perf_counter()
         for i in range(args.steps):
             slot = i & 1
-            res, _ = ctx.collect(slot, len(allb[off + i]))
+            ctx.collect(slot, len(e2eb[i]))
             if i + 2 < args.steps:
-                ctx.enqueue_batch(slot, allb[off + i + 2], limit)
+                segs, flags = seg_args(e2eb[i + 2], args.sample_every, gbc)
+                ctx.enqueue_batch(slot, segs, limit, flags)
         e2e_wall = time.perf_counter() - t0
         e2e = evens_per_step * args.steps / e2e_wall / 1e9
-        import ctypes
         d2h = args.batch * ctypes.sizeof(gbc.SegmentResult)
+        # p(n) of every even on every segment
+        exb = allb[off + args.steps + 2:off + args.steps + 2 + args.exact_steps]
+        ex_ms, ex_stage = device_run(ctx, exb, limit, 1, gbc)
+        exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9
+        cfg = ctx.cfg
     hbm, kind = peaks()
-    # dominant stage and its algorithmic HBM bytes per launch
+    # the dominant stage and its algorithmic HBM bytes per launch (per step)
     dom = max(stage, key=stage.get)
-    seg_map_bytes = 8 * (SEG / 30) / 8                  # class-map bits of a segment, as bytes
-    nprime = 98_222_287                                  # odd primes <= 2.0e9 (sqrt of the workload)
-    alg = {"tile": seg_map_bytes * args.batch,           # one write of the batch's map
-           "large": 4 * nprime + 2 * 4 * 30_800_000 * args.batch / 8 * 0,  # prime stream (marks hit L2)
-           "check": seg_map_bytes * args.batch,          # one read of the map
-           "count": seg_map_bytes * args.batch}[dom]
+    kernel = {"tile": "k_tile", "large": "k_hitlist", "check": "k_verify", "count": "k_count"}[dom]
+    map_bytes = 8 * (SEG / 30) / 8 * args.batch        # the batch's class map, one byte per 8 q
+    alg = {"tile": map_bytes,                           # one write of the map
+           "large": 4 * NPRIMES_4E18,                   # the sieving-prime stream
+           "check": map_bytes,                          # one read of the map
+           "count": map_bytes}[dom]                     # one read of the map
     per_launch_ms = stage[dom] / args.steps
+    launches_per_step = args.batch if dom in ("check", "count") else 1
     achieved = alg / (per_launch_ms / 1e3) / 1e9
+    traffic = ncu_traffic(kernel)
     out = {
         "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"production segments of {SEG} integers from {start} (4e18 + k*467.5e6, k seed 1), "
-                               f"{args.batch} segments per step", "segments_per_step": args.batch,
-                   "evens_per_step": evens_per_step, "l2": "inputs larger than L2 (class map 125 MB + primes "
-                                                           "393 MB per step)",
-                   "tile_log2": ctx.cfg.tile_log2, "p_mid": ctx.cfg.p_mid},
+                               f"{args.batch} segments per step",
+                   "segments_per_step": args.batch, "evens_per_step": evens_per_step,
+                   "stats": f"every {args.sample_every}th segment p(n) of every even, the others funnel verify "
+                            f"+ exact p(n) >= plan bound; primes, twins, gap walk, map hash on every segment",
+                   "l2": "inputs larger than L2: 250 MB class map + 393 MB sieving primes per step",
+                   "tile_log2": cfg.tile_log2, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
+                   "plan_funnels": cfg.plan_funnels},
         "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
         "wall_ms_per_step": wall * 1e3 / args.steps,
+        "exact_all": {"value": exact_all, "unit": "G evens/s",
+                      "stage_ms_per_step": {k: v / len(exb) for k, v in ex_stage.items()}},
         "e2e": {"value": e2e, "unit": "G evens/s", "h2d_bytes_per_step": 16 * args.batch,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind},
+        "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": kind,
+                     "alg_bytes_per_step": alg, "launches_per_step": launches_per_step},
         "clocks": clk.summary(),
     }
     if not args.no_cpu:

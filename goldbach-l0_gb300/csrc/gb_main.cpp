@@ -82,7 +82,7 @@ int usage()
 
 int main(int argc, char **argv)
 {
-    uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8;
+    uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8, sample = 1;
     bool csv = false, stats = false, verbose = false;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
@@ -99,6 +99,8 @@ int main(int argc, char **argv)
             if (!val(segment)) return usage();
         } else if (a == "--batch") {
             if (!val(batch) || !batch || batch > 256) return usage();
+        } else if (a == "--stats-sample") {
+            if (!val(sample) || !sample || sample > (1u << 30)) return usage();
         } else if (a == "--csv") csv = true;
         else if (a == "--stats") stats = true;
         else if (a == "--verbose") verbose = true;
@@ -114,7 +116,7 @@ int main(int argc, char **argv)
         return 1;
     }
     try {
-        const gb::RunStats st = gb::run_gpu(limit, segment, verbose, start, uint32_t(batch));
+        const gb::RunStats st = gb::run_gpu(limit, segment, verbose, start, uint32_t(batch), nullptr, uint32_t(sample));
         const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
         if (csv)
             std::printf("result=PASS,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64 ",segments=%" PRIu64
@@ -128,7 +130,10 @@ int main(int argc, char **argv)
             std::printf("PASS: every even n in [%" PRIu64 ", %" PRIu64 "] is a sum of two primes "
                         "(%" PRIu64 " evens, largest p(n) %" PRIu64 ", %.3f G evens/s)\n",
                         st.start, st.limit, st.evens, st.pmax, eps / 1e9);
-        if (stats) std::printf("%s\n", st.stats_line.c_str());
+        if (stats) {
+            std::printf("%s\n", st.gbstats_line.c_str());
+            if (!st.stats_line.empty()) std::printf("%s\n", st.stats_line.c_str());
+        }
         return 0;
     } catch (const gb::GbcError &e) {
         std::fprintf(stderr, "FAIL: %s\n", e.what());

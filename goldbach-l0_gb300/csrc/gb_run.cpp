@@ -1,15 +1,17 @@
 // gb_run.cpp -- the run driver above the C ABI: gbc_verify_range and the
-// C++ gb::run_gpu of include/gb_run.hpp.
+// C++ gb::run_gpu of gb_run.hpp.
 //
 // Follows the reference's DenseRun (src/verifier.cpp:2487-2569): segments
 // of segment_even integers, two slots in flight (batch k + 1 is enqueued
 // before batch k is collected), per-segment results merged into run
 // statistics with the rules of GoldbachStats (include/gstats.hpp:507-772:
 // sums, the smallest first occurrence, the largest gap with the smallest
-// lower prime on ties, gaps >= 700 with count and first lower prime), fail
-// closed on any error. The statistics are printed in the format of the
-// reference's CPU oracle tests/stats_ref.cpp:97-189, so a run can be diffed
-// against it line for line.
+// lower prime on ties, gaps >= 700 with count and first lower prime),
+// positive coverage accounting per segment (src/verifier.cpp:2465-2482),
+// fail closed on any error. The statistics are printed as the reference's
+// run log line (GBSTATS v2, include/gstats.hpp:913-969) and, when every
+// segment was sampled, in the format of its CPU oracle tests/stats_ref.cpp:
+// 97-189, so a run can be diffed against it line for line.
 #include "gb_run.hpp"
 
 #include <algorithm>
@@ -22,6 +24,8 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+void gbh_set_error(gbc_ctx *ctx, const char *msg);  // gbc_api.cu
 
 namespace gb {
 
@@ -46,13 +50,31 @@ std::vector<uint16_t> candidates()
     return c;
 }
 
+// comma-separated counts, an empty entry for 0, trailing zeros cut
+// (GoldbachStats::dense_list, include/gstats.hpp:890-903)
+std::string dense_list(const std::vector<uint64_t> &v, size_t from = 0)
+{
+    size_t last = 0;
+    for (size_t i = from; i < v.size(); ++i)
+        if (v[i]) last = i + 1;
+    std::string s;
+    for (size_t i = from; i < last; ++i) {
+        if (i > from) s += ',';
+        if (v[i]) s += std::to_string(v[i]);
+    }
+    return s;
+}
+
 }  // namespace
 
-RunAccumulator::RunAccumulator(uint64_t start, uint64_t limit) : start_(start), limit_(limit)
+RunAccumulator::RunAccumulator(uint64_t start, uint64_t limit, uint32_t tail_t)
+    : start_(start), limit_(limit), tail_t_(tail_t)
 {
     cand_ = candidates();
-    hist_.assign(size_t(GBC_NCLASS) * GBC_NCAND, 0);
-    first_.assign(GBC_NCAND, 0);
+    samp_.assign(size_t(GBC_NCLASS) * GBC_NCAND, 0);
+    tail_.assign(GBC_NCAND, 0);
+    first_all_.assign(GBC_NCAND, 0);
+    first_tail_.assign(GBC_NCAND, 0);
     ghist_.assign(GBC_GBINS, 0);
     evens_ = (limit - start) / 2 + 1;
     // q = 3 and q = 5 are not in the class map (multiples of 3 and 5): their
@@ -92,34 +114,64 @@ void RunAccumulator::note_gap_max(uint64_t g, uint64_t lower)
 
 void RunAccumulator::note_tail(uint32_t g, uint64_t c, uint64_t lower)
 {
-    auto &t = tail_[g];
+    auto &t = tail_gaps_[g];
     if (!t.first || lower < t.second) t.second = lower;
     t.first += c;
 }
 
-void RunAccumulator::add_pn(uint64_t n, uint64_t p)
+void RunAccumulator::add_beyond(uint64_t n, uint64_t p)
 {
     auto &b = beyond_[p];
     if (!b.first || n < b.second) b.second = n;
     b.first += 1;
 }
 
+void RunAccumulator::note_ridge(uint64_t n, uint64_t p)
+{
+    const Ridge x{n, p};
+    auto better = [](const Ridge &a, const Ridge &b) { return a.p != b.p ? a.p > b.p : a.n < b.n; };
+    for (const Ridge &r : ridges_)
+        if (r.n == n) return;
+    if (ridges_.size() == 30 && !better(x, ridges_.back())) return;
+    ridges_.insert(std::upper_bound(ridges_.begin(), ridges_.end(), x, better), x);
+    if (ridges_.size() > 30) ridges_.pop_back();
+}
+
 void RunAccumulator::add_segment(const gbc_segment_result &r)
 {
+    // positive accounting: every even of the segment has a p(n) (or, in a
+    // verified segment, was resolved by the funnels or has one in the tail)
+    uint64_t found = r.nleft;
     for (int cr = 0; cr < GBC_NCLASS; ++cr)
-        for (int i = 0; i < GBC_NCAND; ++i) hist_[size_t(cr) * GBC_NCAND + i] += r.hist[cr][i];
+        for (int i = 0; i < GBC_NCAND; ++i) found += r.hist[cr][i];
+    const uint64_t want = r.sampled ? r.evens : r.pending;
+    if (found != want || r.pending > r.evens)
+        throw std::runtime_error("coverage: segment [" + std::to_string(r.seg_start) + ", " +
+                                 std::to_string(r.seg_end) + "] accounts for " + std::to_string(found) + " of " +
+                                 std::to_string(want) + (r.sampled ? " evens" : " pending evens"));
+    for (int cr = 0; cr < GBC_NCLASS; ++cr)
+        for (int i = 0; i < GBC_NCAND; ++i) {
+            const uint64_t c = r.hist[cr][i];
+            if (!c) continue;
+            if (r.sampled) samp_[size_t(cr) * GBC_NCAND + i] += c;
+            if (cand_[i] >= tail_t_) tail_[i] += c;
+        }
     for (int i = 0; i < GBC_NCAND; ++i)
         if (r.first[i] != 0xFFFFFFFFu) {
             const uint64_t n = r.seg_start + 2ull * r.first[i];
-            if (!first_[i] || n < first_[i]) first_[i] = n;
+            if (r.sampled && (!first_all_[i] || n < first_all_[i])) first_all_[i] = n;
+            if (cand_[i] >= tail_t_ && (!first_tail_[i] || n < first_tail_[i])) first_tail_[i] = n;
         }
+    if (r.sampled) evens_sampled_ += r.evens;
+    else pending_ += r.pending;
     for (uint32_t i = 0; i < r.nleft; ++i) {
         if (!r.left_p[i])
             throw std::runtime_error("no Goldbach partition found for n = " + std::to_string(r.left_n[i]) +
                                      " (reported, never passed)");
-        add_pn(r.left_n[i], r.left_p[i]);
+        add_beyond(r.left_n[i], r.left_p[i]);
         ++leftovers_;
     }
+    for (uint32_t i = 0; i < r.nridge; ++i) note_ridge(r.ridge_n[i], r.ridge_p[i]);
     static const int res[8] = {1, 7, 11, 13, 17, 19, 23, 29};
     for (int k = 0; k < 8; ++k) primes30_[res[k]] += r.primes30[k];
     twins30_[11] += r.twins[0];
@@ -156,12 +208,20 @@ uint64_t RunAccumulator::pmax() const
 {
     uint64_t m = 0;
     for (int i = 0; i < GBC_NCAND; ++i) {
-        uint64_t c = 0;
-        for (int cr = 0; cr < GBC_NCLASS; ++cr) c += hist_[size_t(cr) * GBC_NCAND + i];
+        uint64_t c = tail_[i];
+        for (int cr = 0; cr < GBC_NCLASS; ++cr) c += samp_[size_t(cr) * GBC_NCAND + i];
         if (c) m = cand_[i];
     }
     for (auto &b : beyond_) m = std::max(m, b.first);
     return m;
+}
+
+uint64_t RunAccumulator::tail_evens() const
+{
+    uint64_t t = 0;
+    for (uint64_t v : tail_) t += v;
+    for (auto &b : beyond_) t += b.second.first;
+    return t;
 }
 
 uint64_t RunAccumulator::gap_count() const
@@ -173,6 +233,7 @@ uint64_t RunAccumulator::gap_count() const
 
 std::string RunAccumulator::stats_ref_line() const
 {
+    if (!fully_sampled()) return std::string();
     std::string o;
     char b[128];
     std::snprintf(b, sizeof b, "evens=%" PRIu64 " pmax=%" PRIu64 " primes=%" PRIu64 " twins=%" PRIu64 " primes30=",
@@ -189,8 +250,8 @@ std::string RunAccumulator::stats_ref_line() const
     std::map<uint64_t, uint64_t> firsts;
     std::vector<uint64_t> tot(GBC_NCAND, 0);
     for (int i = 0; i < GBC_NCAND; ++i) {
-        for (int cr = 0; cr < GBC_NCLASS; ++cr) tot[i] += hist_[size_t(cr) * GBC_NCAND + i];
-        if (tot[i]) firsts[cand_[i]] = first_[i];
+        for (int cr = 0; cr < GBC_NCLASS; ++cr) tot[i] += samp_[size_t(cr) * GBC_NCAND + i];
+        if (tot[i]) firsts[cand_[i]] = first_all_[i];
     }
     for (auto &bp : beyond_) {
         auto it = firsts.find(bp.first);
@@ -203,21 +264,12 @@ std::string RunAccumulator::stats_ref_line() const
         o += b;
         f1 = false;
     }
-    o += " hist=";
-    size_t last = 0;
-    for (size_t i = 0; i < tot.size(); ++i) {
-        uint64_t c = tot[i];
+    std::vector<uint64_t> hist(tot);
+    for (size_t i = 0; i < hist.size(); ++i) {
         auto it = beyond_.find(cand_[i]);
-        if (it != beyond_.end()) c += it->second.first;
-        if (c) last = i + 1;
+        if (it != beyond_.end()) hist[i] += it->second.first;
     }
-    for (size_t i = 0; i < last; ++i) {
-        if (i) o += ",";
-        uint64_t c = tot[i];
-        auto it = beyond_.find(cand_[i]);
-        if (it != beyond_.end()) c += it->second.first;
-        if (c) o += std::to_string(c);
-    }
+    o += " hist=" + dense_list(hist);
     // gaps: count, moments, largest, tail, histogram
     u128 m[4] = {odd_gaps_, odd_gaps_, odd_gaps_, odd_gaps_};  // g = 1
     uint64_t n = odd_gaps_;
@@ -233,22 +285,73 @@ std::string RunAccumulator::stats_ref_line() const
          "," + u128_str(m[3]);
     std::snprintf(b, sizeof b, " gmax=%" PRIu64 ":%" PRIu64 " gtail=", gmax_, gmax_lo_);
     o += b;
-    if (tail_.empty()) o += "-";
+    if (tail_gaps_.empty()) o += "-";
     bool t1 = true;
-    for (auto &t : tail_) {
+    for (auto &t : tail_gaps_) {
         std::snprintf(b, sizeof b, "%s%u:%" PRIu64 ":%" PRIu64, t1 ? "" : ";", t.first, t.second.first,
                       t.second.second);
         o += b;
         t1 = false;
     }
-    o += " ghist=";
-    size_t hb = 0;
-    for (size_t i = 0; i < ghist_.size(); ++i)
-        if (ghist_[i]) hb = i + 1;
-    for (size_t i = 0; i < hb; ++i) {
-        if (i) o += ",";
-        if (ghist_[i]) o += std::to_string(ghist_[i]);
+    o += " ghist=" + dense_list(ghist_);
+    return o;
+}
+
+std::string RunAccumulator::gbstats_line(const char *version) const
+{
+    // the reference's run line without a campaign state: new_first lists the
+    // run's first occurrences of the tail bins
+    uint64_t pm = 0;
+    for (int i = 0; i < GBC_NCAND; ++i)
+        if (tail_[i]) pm = cand_[i];
+    for (auto &b : beyond_) pm = std::max(pm, b.first);
+    std::string o = "GBSTATS v2 version=" + std::string(version);
+    char b[512];
+    std::snprintf(b, sizeof b,
+                  " start=%" PRIu64 " limit=%" PRIu64 " evens=%" PRIu64 " evens_sampled=%" PRIu64 " tail_t=%u"
+                  " tail_evens=%" PRIu64 " pmax=%" PRIu64 " primes=%" PRIu64 " twins=%" PRIu64,
+                  start_, limit_, evens_, evens_sampled_, tail_t_, tail_evens(), pm, primes(), twins());
+    o += b;
+    static const int u[8] = {1, 7, 11, 13, 17, 19, 23, 29};
+    o += " primes30=";
+    for (int i = 0; i < 8; ++i) o += (i ? "," : "") + std::to_string(primes30_[u[i]]);
+    o += " twins30=" + std::to_string(twins30_[11]) + "," + std::to_string(twins30_[17]) + "," +
+         std::to_string(twins30_[29]);
+    std::string nf;
+    for (int i = 0; i < GBC_NCAND; ++i)
+        if (cand_[i] >= tail_t_ && first_tail_[i])
+            nf += (nf.empty() ? "" : ";") + std::to_string(cand_[i]) + ":" + std::to_string(first_tail_[i]);
+    o += " new_first=" + (nf.empty() ? std::string("-") : nf);
+    std::string bey;
+    for (auto &e : beyond_)
+        bey += (bey.empty() ? "" : ";") + std::to_string(e.first) + ":" + std::to_string(e.second.second);
+    o += " beyond=" + (bey.empty() ? std::string("-") : bey);
+    // gaps: every segment is walked, so the walk totals are the run totals
+    u128 m[4] = {odd_gaps_, odd_gaps_, odd_gaps_, odd_gaps_};
+    const uint64_t n = gap_count();
+    for (size_t i = 0; i < ghist_.size(); ++i) {
+        const u128 c = ghist_[i], g = 2 * i, g2 = g * g;
+        m[0] += c * g;
+        m[1] += c * g2;
+        m[2] += c * g2 * g;
+        m[3] += c * g2 * g2;
     }
+    o += " gaps=" + std::to_string(n) + " gd1=" + u128_str(m[0]) + " gmax=" +
+         (gmax_ ? std::to_string(gmax_) + ":" + std::to_string(gmax_lo_) : std::string("-")) + " gtail=";
+    std::string t;
+    for (auto &e : tail_gaps_)
+        t += (t.empty() ? "" : ";") + std::to_string(e.first) + ":" + std::to_string(e.second.first) + ":" +
+             std::to_string(e.second.second);
+    o += t.empty() ? "-" : t;
+    o += " gwalk=" + std::to_string(evens_) + ":" + std::to_string(n) + " gsmom=";
+    for (int k = 0; k < 4; ++k) o += (k ? "," : "") + u128_str(m[k]);
+    const std::string h = dense_list(ghist_);
+    o += " gsamp=" + (h.empty() ? std::string("-") : h);
+    // tail: counts by consecutive candidates from the first p >= tail_t
+    size_t t0 = 0;
+    while (t0 < cand_.size() && cand_[t0] < tail_t_) ++t0;
+    const std::string tl = t0 < cand_.size() ? dense_list(tail_, t0) : std::string();
+    o += " tail=" + (tl.empty() ? std::string("-") : std::to_string(cand_[t0]) + ":" + tl);
     return o;
 }
 
@@ -283,7 +386,7 @@ void check(gbc_ctx *ctx, int rc, const char *what)
 }  // namespace
 
 RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
-                   uint16_t *pn, RunAccumulator *acc_out)
+                   uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every)
 {
     RunStats st;
     const auto t0 = std::chrono::steady_clock::now();
@@ -296,8 +399,14 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
     const auto segs = plan_segments(start, limit, segment_even);
     RunAccumulator acc(start, limit);
     std::vector<std::vector<std::pair<uint64_t, uint64_t>>> batches;
-    for (size_t i = 0; i < segs.size(); i += max_batch)
+    std::vector<std::vector<uint32_t>> flags;
+    for (size_t i = 0; i < segs.size(); i += max_batch) {
         batches.emplace_back(segs.begin() + i, segs.begin() + std::min(segs.size(), i + max_batch));
+        std::vector<uint32_t> f;
+        for (size_t j = i; j < std::min(segs.size(), i + max_batch); ++j)
+            f.push_back(sample_every > 1 && j % sample_every && !pn ? GBC_SEG_VERIFY : 0u);
+        flags.push_back(f);
+    }
     std::vector<gbc_segment_result> out[2];
     double gpu_ms = 0;
     auto collect = [&](size_t b) {
@@ -325,7 +434,7 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
             bounds.push_back(s.first);
             bounds.push_back(s.second);
         }
-        check(ctx, gbc_enqueue_batch(ctx, int(b & 1), bounds.data(), nullptr, int(batches[b].size()), limit),
+        check(ctx, gbc_enqueue_batch(ctx, int(b & 1), bounds.data(), flags[b].data(), int(batches[b].size()), limit),
               "enqueue");
         if (b) collect(b - 1);
     }
@@ -337,27 +446,33 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
     st.pmax = acc.pmax();
     st.primes = acc.primes();
     st.twins = acc.twins();
+    st.evens_sampled = acc.evens_sampled();
+    st.tail_evens = acc.tail_evens();
+    st.pending = acc.pending();
     st.gpu_seconds = gpu_ms / 1e3;
     st.wall_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     st.stats_line = acc.stats_ref_line();
+    st.gbstats_line = acc.gbstats_line("gb300-1.0");
+    st.ridges = acc.ridges();
     if (acc_out) *acc_out = acc;
     return st;
 }
 
 RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even, uint32_t max_batch,
-                 uint16_t *pn)
+                 uint16_t *pn, uint32_t sample_every)
 {
     gbc_config cfg{};
     cfg.limit = limit & ~uint64_t(1);
     cfg.segment_even = segment_even;
     cfg.max_batch = max_batch;
     cfg.want_pn = pn ? 1 : 0;
+    cfg.sample_every = sample_every;
     gbc_ctx *raw = nullptr;
     const int rc = gbc_create(&cfg, &raw);
     std::unique_ptr<gbc_ctx, CtxCloser> ctx(raw);
     if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_create: ") + gbc_last_error(raw));
     RunStats st = run_range(ctx.get(), start_even, limit, segment_even ? segment_even : GBC_DEFAULT_SEGMENT,
-                            max_batch ? max_batch : 8, pn, nullptr);
+                            max_batch ? max_batch : 8, pn, nullptr, sample_every);
     if (verbose)
         std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",
                      st.start, st.limit, st.segments, st.gpu_seconds, st.wall_seconds);
@@ -373,7 +488,8 @@ extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gb
     try {
         gbc_config cfg{};
         if (gbc_get_config(ctx, &cfg) != GBC_OK) return GBC_E_ARG;
-        gb::RunStats st = gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, pn, nullptr);
+        gb::RunStats st =
+            gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, pn, nullptr, cfg.sample_every);
         if (res) {
             res->start = st.start;
             res->limit = st.limit;
@@ -388,13 +504,17 @@ extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gb
             res->wall_seconds = st.wall_seconds;
         }
         if (line && line_cap) {
-            if (st.stats_line.size() + 1 > line_cap) return GBC_E_OVERFLOW;
-            std::memcpy(line, st.stats_line.c_str(), st.stats_line.size() + 1);
+            // the stats_ref line when every segment was sampled, else the GBSTATS v2 line
+            const std::string &l = st.stats_line.empty() ? st.gbstats_line : st.stats_line;
+            if (l.size() + 1 > line_cap) return GBC_E_OVERFLOW;
+            std::memcpy(line, l.c_str(), l.size() + 1);
         }
         return GBC_OK;
     } catch (const gb::GbcError &e) {
+        gbh_set_error(ctx, e.what());
         return e.code;
-    } catch (const std::exception &) {
+    } catch (const std::exception &e) {
+        gbh_set_error(ctx, e.what());
         return GBC_E_DEVICE;
     }
 }

@@ -140,6 +140,10 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         s.pn_stride = ctx->cfg.segment_even / 2 + 1;
         CK(cudaMalloc(&s.pn, size_t(ctx->cfg.max_batch) * s.pn_stride * 2));
     }
+    // phase-A pending words: up to 1/16 of a segment's words (the plan
+    // leaves ~1e-4 of the evens; an overflow fails the batch closed)
+    s.pend_cap = uint32_t(std::max<uint64_t>(4096, (ctx->cfg.segment_even / 2 / 32 + 64) / 16));
+    CK(cudaMalloc(&s.pend, size_t(ctx->cfg.max_batch) * s.pend_cap * sizeof(uint2)));
     return GBC_OK;
 }
 
@@ -160,6 +164,10 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.large_pass_mb) cfg.large_pass_mb = 4096;  // one pass: the per-prime setup outweighs L2 misses
     if (!cfg.mtab_max_gb) cfg.mtab_max_gb = 48;
     if (!cfg.hl_pass_mb) cfg.hl_pass_mb = 4096;  // one pass: the divisions outweigh L2 misses
+    if (!cfg.sample_every) cfg.sample_every = 1;
+    if (!cfg.plan_funnels) cfg.plan_funnels = 40;
+    if (!cfg.ridge_min) cfg.ridge_min = GBC_TAIL_T;
+    if (cfg.plan_funnels > 256) cfg.plan_funnels = 256;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
@@ -263,6 +271,43 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         }
         ctx->ct.cnt[cr] = uint32_t(list.size()) - ctx->ct.off[cr];
     }
+    // verify plan (the reference's make_plan30, include/check30.hpp:88-174,
+    // with our own greedy order): per class, the smallest useful candidates
+    // below GBC_TAIL_T in ascending order, each uncovered one opening a
+    // funnel with its next primes p + 30, ..., p + 120 of the same residue
+    // (members all prime, below the bound, not yet covered), plan_funnels
+    // funnels; the rest lists hold every useful candidate no funnel tests,
+    // ascending, for the exact continuation.
+    std::vector<uint32_t> fun;
+    std::vector<uint16_t> rest;
+    {
+        std::vector<int> cidx(GBC_MAX_CAND + 1, -1);
+        for (int i = 0; i < GBC_NCAND; ++i) cidx[cand[i]] = i;
+        for (int cr = 0; cr < GBC_NCLASS; ++cr) {
+            std::vector<char> covered(GBC_NCAND, 0);
+            ctx->vt.fun_off[cr] = uint32_t(fun.size());
+            const uint32_t b = ctx->ct.off[cr], e = b + ctx->ct.cnt[cr];
+            for (uint32_t li = b; li < e; ++li) {
+                const int i = list[li];
+                if (fun.size() - ctx->vt.fun_off[cr] >= cfg.plan_funnels || cand[i] >= GBC_TAIL_T) break;
+                if (covered[i]) continue;
+                uint32_t mask = 1;
+                covered[i] = 1;
+                for (uint32_t d = 1; d <= 4; ++d) {
+                    const uint32_t q = cand[i] + 30 * d;
+                    if (q >= GBC_TAIL_T || q > GBC_MAX_CAND || cidx[q] < 0 || covered[cidx[q]]) break;
+                    covered[cidx[q]] = 1;
+                    mask |= 1u << d;
+                }
+                fun.push_back(uint32_t(i) | (mask << 16));
+            }
+            ctx->vt.fun_cnt[cr] = uint32_t(fun.size()) - ctx->vt.fun_off[cr];
+            ctx->vt.rest_off[cr] = uint32_t(rest.size());
+            for (uint32_t li = b; li < e; ++li)
+                if (!covered[list[li]]) rest.push_back(list[li]);
+            ctx->vt.rest_cnt[cr] = uint32_t(rest.size()) - ctx->vt.rest_off[cr];
+        }
+    }
 
     // slot geometry: a batch of max_batch full segments plus the 9781 + 3 margin
     const uint64_t span = uint64_t(cfg.max_batch) * cfg.segment_even + GBC_MAX_CAND + 3 + 64;
@@ -287,6 +332,15 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     CK(cudaMemcpy(ctx->d_list, list.data(), list.size() * 2, cudaMemcpyHostToDevice));
     ctx->ct.cand = ctx->d_cand;
     ctx->ct.list = ctx->d_list;
+    ctx->ct.ridge_min = cfg.ridge_min;
+    CK(cudaMalloc(&ctx->d_fun, std::max<size_t>(fun.size(), 1) * 4));
+    if (!fun.empty()) CK(cudaMemcpy(ctx->d_fun, fun.data(), fun.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_rest, std::max<size_t>(rest.size(), 1) * 2));
+    if (!rest.empty()) CK(cudaMemcpy(ctx->d_rest, rest.data(), rest.size() * 2, cudaMemcpyHostToDevice));
+    ctx->vt.cand = ctx->d_cand;
+    ctx->vt.fun = ctx->d_fun;
+    ctx->vt.rest = ctx->d_rest;
+    ctx->vt.ridge_min = cfg.ridge_min;
     for (auto &s : ctx->slot)
         if (int r = slot_alloc(ctx, s)) return r;
     CK(cudaDeviceSynchronize());
@@ -305,8 +359,11 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
         cudaFree(s.res);
         cudaFree(s.err);
         cudaFree(s.pn);
+        cudaFree(s.pend);
         if (s.st) cudaStreamDestroy(s.st);
     }
+    cudaFree(ctx->d_fun);
+    cudaFree(ctx->d_rest);
     cudaFree(ctx->mtab);
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_magic);
@@ -316,6 +373,12 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
     cudaFree(ctx->d_cand);
     cudaFree(ctx->d_list);
     delete ctx;
+}
+
+// the run driver's (gb_run.cpp) failure text for gbc_last_error
+void gbh_set_error(gbc_ctx *ctx, const char *msg)
+{
+    if (ctx) ctx->err = msg;
 }
 
 extern "C" const char *gbc_last_error(const gbc_ctx *ctx)
@@ -401,6 +464,10 @@ int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl,
         sp.hash_hi = sp.seg_end + 3;
         sp.res = s.res + i;
         sp.pn = s.pn ? s.pn + size_t(i) * s.pn_stride : nullptr;
+        // the low segment and callers that want p(n) of every even take the exact checker
+        sp.sampled = (sp.flags & GBC_SEG_VERIFY) && !sp.low && !sp.pn ? 0 : 1;
+        sp.pend = s.pend + size_t(i) * s.pend_cap;
+        sp.pend_cap = s.pend_cap;
     }
     return GBC_OK;
 }
@@ -515,9 +582,15 @@ extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bou
     ctx->launches += gbh::launch_hitlist(bp, ctx->cfg.hl_pass_mb, st);
     CK(cudaEventRecord(s.ev[2], st));
     for (int i = 0; i < nseg; ++i) {
-        gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);
-        gbh::launch_retry(s.segs[i], st);
-        ctx->launches += 2;
+        if (s.segs[i].sampled) {
+            gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);
+            ctx->launches += 1;
+        } else {
+            gbh::launch_verify(bp, s.segs[i], ctx->vt, ctx->sm_count, st);
+            ctx->launches += 2;
+        }
+        gbh::launch_retry(s.segs[i], ctx->cfg.ridge_min, st);
+        ctx->launches += 1;
     }
     CK(cudaEventRecord(s.ev[3], st));
     for (int i = 0; i < nseg; ++i) {
@@ -580,14 +653,15 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
         r.twin_hi = sp.twin_hi;
         r.hash_lo = sp.hash_lo;
         r.hash_hi = sp.hash_hi;
+        r.sampled = sp.sampled;
         if (r.err) {
             char m[160];
             std::snprintf(m, sizeof m, "device error flags 0x%x in segment [%llu, %llu]", r.err,
                           (unsigned long long)sp.seg_start, (unsigned long long)sp.seg_end);
             return fail(ctx, GBC_E_DEVICE, m);
         }
-        if (r.nleft > GBC_LEFT_CAP || r.ntail > GBC_TAIL_CAP)
-            return fail(ctx, GBC_E_OVERFLOW, "leftover or gap-tail list overflow");
+        if (r.nleft > GBC_LEFT_CAP || r.ntail > GBC_TAIL_CAP || r.nridge > GBC_RIDGE_CAP || r.npend > s.pend_cap)
+            return fail(ctx, GBC_E_OVERFLOW, "leftover, gap-tail, ridge or pending list overflow");
     }
     return GBC_OK;
 }

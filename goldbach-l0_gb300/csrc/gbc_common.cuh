@@ -100,6 +100,9 @@ struct SegParams {
     uint32_t low;                 // seg_start < 9788: the generic per-even checker
     gbc_segment_result *res;      // device result of this segment
     uint16_t *pn;                 // per-even p(n) or nullptr
+    uint32_t sampled;             // 1: exact p(n) of every even; 0: funnel verify + exact tail
+    uint2 *pend;                  // phase-A misses: (class r / 2 << 27 | word, unresolved bits)
+    uint32_t pend_cap;
 };
 
 // Candidate tables of the checker (uploaded once per context).
@@ -108,6 +111,18 @@ struct CheckTables {
     const uint16_t *list;   // per class r / 2: useful candidate indices ascending
     uint32_t off[GBC_NCLASS];
     uint32_t cnt[GBC_NCLASS];
+    uint32_t ridge_min;     // evens with p(n) >= ridge_min are listed with their p(n)
+};
+
+// Funnel plan of the verify (phase A) checker and the ascending rest lists
+// of its exact continuation (phase B), per class r / 2.
+struct VerifyTables {
+    const uint16_t *cand;
+    const uint32_t *fun;    // funnel: candidate index of its first member | mask << 16 (bit d: p + 30 d)
+    const uint16_t *rest;   // candidates no funnel tests, ascending
+    uint32_t fun_off[GBC_NCLASS], fun_cnt[GBC_NCLASS];
+    uint32_t rest_off[GBC_NCLASS], rest_cnt[GBC_NCLASS];
+    uint32_t ridge_min;     // evens with p(n) >= ridge_min are listed with their p(n)
 };
 
 // device error flags
@@ -117,6 +132,8 @@ constexpr uint32_t kErrGapRange = 1u << 2;
 constexpr uint32_t kErrNoPred = 1u << 3;
 constexpr uint32_t kErrRetry = 1u << 4;
 constexpr uint32_t kErrTable = 1u << 5;   // a multiplier outside the prime-multiplier table
+constexpr uint32_t kErrPendOverflow = 1u << 6;
+constexpr uint32_t kErrRidgeOverflow = 1u << 7;
 
 // ---------------------------------------------------------------------------
 // 64-bit Miller-Rabin in Montgomery form (the GPU retry of evens without a
@@ -193,6 +210,8 @@ int launch_hitlist(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st
 void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st);
 void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
                   cudaStream_t st);
-void launch_retry(const gbk::SegParams &sp, cudaStream_t st);
+void launch_retry(const gbk::SegParams &sp, uint32_t ridge_min, cudaStream_t st);
+void launch_verify(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::VerifyTables &vt, int sm_count,
+                   cudaStream_t st);
 void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStream_t st);
 }  // namespace gbh

@@ -23,6 +23,8 @@ struct Slot {
     uint32_t *err = nullptr;
     uint16_t *pn = nullptr;            // max_batch * pn_stride p(n), or nullptr
     uint64_t pn_stride = 0;
+    uint2 *pend = nullptr;             // max_batch * pend_cap phase-A pending words
+    uint32_t pend_cap = 0;
     int nseg = 0;
     bool pending = false;
     gbk::BatchParams bp{};
@@ -37,8 +39,11 @@ struct gbc_ctx {
     uint32_t wpc_cap = 0;              // class-array words a slot holds
     uint32_t *d_primes = nullptr, *d_magic = nullptr, *d_pat = nullptr, *d_skip = nullptr;
     uint16_t *d_inv = nullptr, *d_cand = nullptr, *d_list = nullptr;
+    uint32_t *d_fun = nullptr;
+    uint16_t *d_rest = nullptr;
     gbk::GroupInfo gi{};
     gbk::CheckTables ct{};
+    gbk::VerifyTables vt{};
     Slot slot[2];
     std::string err;
     uint64_t launches = 0;

@@ -26,6 +26,17 @@ __device__ __forceinline__ void append_leftover(gbc_segment_result *res, uint64_
     else atomicOr(&res->err, kErrLeftOverflow);
 }
 
+// (n, p(n)) of an even whose smallest witness reaches the ridge floor (the
+// reference's ridge appends, include/ridge.hpp:116-165)
+__device__ __forceinline__ void append_ridge(gbc_segment_result *res, uint64_t n, uint32_t p)
+{
+    const uint32_t slot = atomicAdd(&res->nridge, 1u);
+    if (slot < GBC_RIDGE_CAP) {
+        res->ridge_n[slot] = n;
+        res->ridge_p[slot] = p;
+    } else atomicOr(&res->err, kErrRidgeOverflow);
+}
+
 constexpr int kCheckThreads = 256;
 constexpr int kCheckWarps = kCheckThreads / 32;
 constexpr uint32_t kWin = 80;  // staged words per class array per warp: 64 + span of the candidates + 2
@@ -130,6 +141,12 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
                 write_pn(sp.pn, idx0, jA, hA, s_p[c]);
                 write_pn(sp.pn, idx0, jB, hB, s_p[c]);
             }
+            if (s_p[c] >= ct.ridge_min) {
+                for (uint32_t h = hA; h; h &= h - 1u)
+                    append_ridge(sp.res, n0 + 30ull * (32ull * jA + __ffs(h) - 1u), s_p[c]);
+                for (uint32_t h = hB; h; h &= h - 1u)
+                    append_ridge(sp.res, n0 + 30ull * (32ull * jB + __ffs(h) - 1u), s_p[c]);
+            }
         };
         uint32_t c = 0;
         // two candidates per trip: their window reads are independent; the
@@ -185,7 +202,8 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
 // Generic checker for a segment that reaches q < 7 (seg_start < 9788): one
 // thread per even, every candidate ascending, q = 3 and q = 5 prime by
 // definition (they are not in the class map), q < 3 ends the search.
-__global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp, const uint16_t *cand)
+__global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp, const uint16_t *cand,
+                                                   uint32_t ridge_min)
 {
     const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
     for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < evens;
@@ -214,6 +232,7 @@ __global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp,
             atomicAdd(&sp.res->hist[cr][ci], 1u);
             atomicMin(&sp.res->first[ci], uint32_t(e));
             if (sp.pn) sp.pn[e] = cand[ci];
+            if (cand[ci] >= ridge_min) append_ridge(sp.res, n, cand[ci]);
         } else {
             append_leftover(sp.res, n);
         }
@@ -223,7 +242,7 @@ __global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp,
 // Evens without a witness <= 9781: ascending odd p > 9781 by Miller-Rabin on
 // both p and n - p (n = 4: p = 2). A bounded search: a wait that runs out
 // sets an error flag instead of looping.
-__global__ void __launch_bounds__(64) k_retry(SegParams sp)
+__global__ void __launch_bounds__(64) k_retry(SegParams sp, uint32_t ridge_min)
 {
     gbc_segment_result *res = sp.res;
     const uint32_t nl = res->nleft < GBC_LEFT_CAP ? res->nleft : GBC_LEFT_CAP;
@@ -246,6 +265,162 @@ __global__ void __launch_bounds__(64) k_retry(SegParams sp)
         }
         res->left_p[i] = found;
         if (sp.pn) sp.pn[(n - sp.seg_start) / 2] = found < 65536 ? uint16_t(found) : 0;
+        if (found && found >= ridge_min) append_ridge(res, n, uint32_t(found));
+    }
+}
+
+constexpr uint32_t kVWin = 84;     // staged words per class array per warp (verify)
+constexpr uint32_t kMaxFun = 256;  // funnels per class the verify kernel holds
+
+// Phase A (the reference's check30_a, kernels/goldbach.cl:2029-2189): any
+// witness. Each funnel is a run of plan members p, p + 30, ..., p + 30 d
+// of one residue class, all prime, whose windows are the same staged words
+// shifted by 0..d bits, so one 96-bit read tests up to five candidates for
+// 32 evens. No statistics here: evens left without a plan witness go to a
+// pending list of (class, word, bits) for k_tail.
+__global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchParams bp, SegParams sp, VerifyTables vt)
+{
+    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | top member << 21 | mask << 24
+    __shared__ uint32_t s_win[kCheckWarps][8 * kVWin];
+    __shared__ uint32_t s_dmin, s_dmax;
+    __shared__ unsigned long long s_pend;
+
+    const uint32_t cr = blockIdx.y, r = 2 * cr;
+    const uint64_t seg_start = sp.seg_start;
+    const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
+    if (n0 > sp.seg_end) return;
+    const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
+    const uint32_t nwords = uint32_t((ecount + 31) / 32);
+    const uint32_t nfun = vt.fun_cnt[cr] < kMaxFun ? vt.fun_cnt[cr] : kMaxFun;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    gbc_segment_result *res = sp.res;
+
+    if (tid == 0) {
+        s_dmin = kNone;
+        s_dmax = 0;
+        s_pend = 0;
+    }
+    __syncthreads();
+    // the lowest window bit of each funnel: its top member p + 30 d
+    for (uint32_t f = tid; f < nfun; f += blockDim.x) {
+        const uint32_t e = vt.fun[vt.fun_off[cr] + f];
+        const uint32_t p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(e >> 16);
+        const uint32_t u = (r + 30 - p0 % 30) % 30;
+        const uint32_t dlow = uint32_t((n0 - bp.base - p0 - u) / 30) - dm;
+        atomicMin(&s_dmin, dlow);
+        atomicMax(&s_dmax, dlow);
+    }
+    __syncthreads();
+    const uint32_t dlo = s_dmin & ~31u;
+    const uint32_t nstage = (s_dmax - dlo) / 32 + 68;  // <= kVWin
+    for (uint32_t f = tid; f < nfun; f += blockDim.x) {
+        const uint32_t e = vt.fun[vt.fun_off[cr] + f];
+        const uint32_t mask = e >> 16, p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(mask);
+        const uint32_t u = (r + 30 - p0 % 30) % 30;
+        const uint32_t d = uint32_t((n0 - bp.base - p0 - u) / 30) - dm - dlo;
+        s_fent[f] = (class_of(u) * kVWin + (d >> 5)) | ((d & 31) << 16) | (dm << 21) | (mask << 24);
+    }
+    __syncthreads();
+
+    uint32_t *win = s_win[warp];
+    unsigned long long pend = 0;
+    for (uint32_t ch = blockIdx.x * kCheckWarps + warp; ch * 64 < nwords; ch += gridDim.x * kCheckWarps) {
+        const uint32_t J = ch * 64;
+        const uint32_t *src = bp.map + (dlo >> 5) + J;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            for (uint32_t i = lane; i < nstage; i += 32) win[k * kVWin + i] = __ldg(src + size_t(k) * bp.wpc + i);
+        __syncwarp();
+        const uint32_t jA = J + lane, jB = J + 32 + lane;
+        uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+        const uint32_t *wl = win + lane;
+        for (uint32_t f = 0; f < nfun; ++f) {
+            if (!__any_sync(~0u, uA | uB)) break;
+            const uint32_t e = s_fent[f];
+            const uint32_t *w = wl + (e & 0xFFFF);
+            const uint32_t sh = (e >> 16) & 31, dm = (e >> 21) & 7, mask = e >> 24;
+            const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
+            uint32_t wa = 0, wb = 0;
+#pragma unroll
+            for (uint32_t d = 0; d <= 4; ++d) {
+                if (!((mask >> d) & 1u)) continue;
+                const uint32_t a = sh + dm - d;  // member d's window starts a bits into the read
+                if (a < 32) {
+                    wa |= __funnelshift_r(x0, x1, a);
+                    wb |= __funnelshift_r(y0, y1, a);
+                } else {
+                    wa |= __funnelshift_r(x1, x2, a - 32);
+                    wb |= __funnelshift_r(y1, y2, a - 32);
+                }
+            }
+            uA &= ~wa;
+            uB &= ~wb;
+        }
+        // pending words: one reservation per warp
+        const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
+        uint32_t pre = has;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t n = __shfl_up_sync(~0u, pre, o);
+            if (lane >= uint32_t(o)) pre += n;
+        }
+        const uint32_t total = __shfl_sync(~0u, pre, 31);
+        if (total) {
+            uint32_t base = 0;
+            if (lane == 31) base = atomicAdd(&res->npend, total);
+            base = __shfl_sync(~0u, base, 31);
+            uint32_t at = base + pre - has;
+            if (uA) {
+                if (at < sp.pend_cap) sp.pend[at] = make_uint2((cr << 27) | jA, uA);
+                else atomicOr(&res->err, kErrPendOverflow);
+                ++at;
+            }
+            if (uB) {
+                if (at < sp.pend_cap) sp.pend[at] = make_uint2((cr << 27) | jB, uB);
+                else atomicOr(&res->err, kErrPendOverflow);
+            }
+        }
+        pend += __popc(uA) + __popc(uB);
+        __syncwarp();
+    }
+    pend = __reduce_add_sync(~0u, uint32_t(pend));
+    if (lane == 0 && pend) atomicAdd(&s_pend, pend);
+    __syncthreads();
+    if (tid == 0 && s_pend) atomicAdd((unsigned long long *)&res->pending, s_pend);
+}
+
+// Phase B (the reference's check30_b, kernels/goldbach.cl:2210-2306): the
+// exact p(n) of every pending even, by the class's rest candidates in
+// ascending order (every plan member already failed for it), one thread per
+// pending word. The histogram and first occurrences of these evens hold
+// every even with p(n) >= the plan bound; ridges above the floor are listed.
+__global__ void __launch_bounds__(128) k_tail(BatchParams bp, SegParams sp, VerifyTables vt)
+{
+    gbc_segment_result *res = sp.res;
+    const uint32_t np = res->npend < sp.pend_cap ? res->npend : sp.pend_cap;
+    const uint64_t seg_start = sp.seg_start;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const uint2 e = sp.pend[i];
+        const uint32_t cr = e.x >> 27, j = e.x & ((1u << 27) - 1), r = 2 * cr;
+        uint32_t mask = e.y;
+        const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
+        const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);
+        const uint32_t off = vt.rest_off[cr], cnt = vt.rest_cnt[cr];
+        for (uint32_t c = 0; c < cnt && mask; ++c) {
+            const uint32_t ci = vt.rest[off + c];
+            const uint32_t p = vt.cand[ci];
+            const uint32_t u = (r + 30 - p % 30) % 30;
+            const uint32_t pos = uint32_t((n0 - bp.base - p - u) / 30) + 32 * j;
+            const uint32_t *wk = bp.map + size_t(class_of(u)) * bp.wpc + (pos >> 5);
+            const uint32_t hit = mask & __funnelshift_r(__ldg(wk), __ldg(wk + 1), pos & 31);
+            if (!hit) continue;
+            atomicAdd(&res->hist[cr][ci], uint32_t(__popc(hit)));
+            atomicMin(&res->first[ci], idx0 + 15u * (32u * j + __ffs(hit) - 1u));
+            if (p >= vt.ridge_min)
+                for (uint32_t h = hit; h; h &= h - 1u) append_ridge(res, n0 + 30ull * (32ull * j + __ffs(h) - 1u), p);
+            mask &= ~hit;
+        }
+        for (; mask; mask &= mask - 1u) append_leftover(res, n0 + 30ull * (32ull * j + __ffs(mask) - 1u));
     }
 }
 
@@ -260,7 +435,7 @@ void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gb
     if (sp.low) {
         uint64_t blocks = (evens + 255) / 256;
         if (blocks > uint64_t(sm_count) * 16) blocks = uint64_t(sm_count) * 16;
-        gbk::k_check_low<<<uint32_t(blocks), 256, 0, st>>>(bp, sp, ct.cand);
+        gbk::k_check_low<<<uint32_t(blocks), 256, 0, st>>>(bp, sp, ct.cand, ct.ridge_min);
         return;
     }
     // words per class ~ evens / 15 / 32; 8 warps per CTA, chunks of 64 words
@@ -273,6 +448,23 @@ void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gb
     gbk::k_check<<<grid, gbk::kCheckThreads, 0, st>>>(bp, sp, ct);
 }
 
-void launch_retry(const gbk::SegParams &sp, cudaStream_t st) { gbk::k_retry<<<1, 64, 0, st>>>(sp); }
+void launch_retry(const gbk::SegParams &sp, uint32_t ridge_min, cudaStream_t st)
+{
+    gbk::k_retry<<<1, 64, 0, st>>>(sp, ridge_min);
+}
+
+void launch_verify(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::VerifyTables &vt, int sm_count,
+                   cudaStream_t st)
+{
+    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+    const uint64_t words = (evens / 15 + 32) / 32 + 1;
+    uint64_t bx = (words + gbk::kCheckWarps * 64 - 1) / (gbk::kCheckWarps * 64);
+    const uint64_t cap = uint64_t(sm_count) * 2;
+    if (bx > cap) bx = cap;
+    if (bx < 1) bx = 1;
+    dim3 grid(uint32_t(bx), GBC_NCLASS);
+    gbk::k_verify<<<grid, gbk::kCheckThreads, 0, st>>>(bp, sp, vt);
+    gbk::k_tail<<<uint32_t(sm_count) * 2, 128, 0, st>>>(bp, sp, vt);
+}
 
 }  // namespace gbh

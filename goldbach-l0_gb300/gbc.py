@@ -18,9 +18,12 @@ NCLASS = 15
 GBINS = 1024
 TAIL_CAP = 256
 LEFT_CAP = 1024
+RIDGE_CAP = 256
+TAIL_T = 3000
 DEFAULT_SEGMENT = 467_500_000
 MAX_LIMIT = 18446742974197923840
 SEG_NOHASH = 2
+SEG_VERIFY = 4
 
 ERRORS = {0: "ok", -1: "argument", -2: "cuda", -3: "device flag", -4: "timeout", -5: "state", -6: "overflow"}
 
@@ -29,7 +32,8 @@ class Config(C.Structure):
     _fields_ = [("limit", C.c_uint64), ("segment_even", C.c_uint64), ("max_batch", C.c_uint32),
                 ("tile_log2", C.c_uint32), ("p_mid", C.c_uint32), ("want_pn", C.c_uint32),
                 ("device", C.c_int32), ("large_pass_mb", C.c_uint32), ("hl_mode", C.c_uint32),
-                ("mtab_max_gb", C.c_uint32), ("hl_pass_mb", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("mtab_max_gb", C.c_uint32), ("hl_pass_mb", C.c_uint32), ("sample_every", C.c_uint32),
+                ("plan_funnels", C.c_uint32), ("ridge_min", C.c_uint32)]
 
 
 class SegmentResult(C.Structure):
@@ -43,7 +47,10 @@ class SegmentResult(C.Structure):
                 ("gmax_key", C.c_uint64), ("ntail", C.c_uint32), ("pad1", C.c_uint32),
                 ("tail_g", C.c_uint32 * TAIL_CAP), ("tail_lo", C.c_uint64 * TAIL_CAP),
                 ("first_prime", C.c_uint64), ("last_prime", C.c_uint64),
-                ("map_hash", C.c_uint64), ("map_primes", C.c_uint64), ("err", C.c_uint32), ("pad2", C.c_uint32)]
+                ("map_hash", C.c_uint64), ("map_primes", C.c_uint64),
+                ("sampled", C.c_uint32), ("npend", C.c_uint32), ("pending", C.c_uint64),
+                ("nridge", C.c_uint32), ("pad3", C.c_uint32), ("ridge_p", C.c_uint32 * RIDGE_CAP),
+                ("ridge_n", C.c_uint64 * RIDGE_CAP), ("err", C.c_uint32), ("pad2", C.c_uint32)]
 
 
 class BatchTimes(C.Structure):
@@ -120,11 +127,13 @@ class Context:
     segments of `segment_even` integers."""
 
     def __init__(self, limit, segment_even=DEFAULT_SEGMENT, max_batch=8, tile_log2=0, p_mid=0, want_pn=False,
-                 device=0, large_pass_mb=0, hl_mode=0, mtab_max_gb=0, hl_pass_mb=0):
+                 device=0, large_pass_mb=0, hl_mode=0, mtab_max_gb=0, hl_pass_mb=0, sample_every=0,
+                 plan_funnels=0, ridge_min=0):
         self.lib = load()
         cfg = Config(limit=limit, segment_even=segment_even, max_batch=max_batch, tile_log2=tile_log2,
                      p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, large_pass_mb=large_pass_mb,
-                     hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, hl_pass_mb=hl_pass_mb)
+                     hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, hl_pass_mb=hl_pass_mb,
+                     sample_every=sample_every, plan_funnels=plan_funnels, ridge_min=ridge_min)
         h = C.c_void_p()
         rc = self.lib.gbc_create(C.byref(cfg), C.byref(h))
         self.h = h

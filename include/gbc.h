@@ -43,12 +43,15 @@ extern "C" {
 #define GBC_GTAIL 700u      /* gaps >= 700 are listed with their position (gstats.hpp:77) */
 #define GBC_TAIL_CAP 256    /* listed tail gaps per segment */
 #define GBC_LEFT_CAP 1024   /* evens per segment without a candidate witness */
+#define GBC_RIDGE_CAP 256   /* listed ridges (evens with p(n) >= ridge_min) per segment */
+#define GBC_TAIL_T 3000u    /* every funnel member is below it (include/check30.hpp:33 CHECK30_TAIL) */
 #define GBC_DEFAULT_SEGMENT 467500000ull /* include/config.hpp:163 DEFAULT_SEGMENT_EVEN */
 #define GBC_MAX_LIMIT 18446742974197923840ull /* 2^64 - 2^40 (include/primes.hpp:212) */
 
 /* segment flags */
 #define GBC_SEG_LAST 1u     /* the run's last segment: counts end at limit - 1 */
 #define GBC_SEG_NOHASH 2u   /* skip the class-map hash */
+#define GBC_SEG_VERIFY 4u   /* funnel verify + exact tail instead of p(n) of every even */
 
 /* Context configuration (the knobs of include/config.hpp and the GB_*
  * environment, as fields). Zero means "default" for every field. */
@@ -70,7 +73,13 @@ typedef struct gbc_config {
     uint32_t hl_pass_mb;     /* class-map megabytes one hit-list pass covers (default 4096: one pass;
                                 smaller passes keep the atomic marks in L2 but redo the per-prime
                                 divisions) */
-    uint32_t reserved[3];
+    uint32_t sample_every;   /* run driver: every sample_every-th segment of a run (segment 0 always)
+                                gets p(n) of every even, the others the funnel verify + exact tail
+                                (GB_STATS_SAMPLE, include/gstats.hpp:62); 0 or 1: every segment
+                                (default) */
+    uint32_t plan_funnels;   /* funnels per class of the verify plan (default 40) */
+    uint32_t ridge_min;      /* evens with p(n) >= ridge_min are listed (default 3000,
+                                include/config.hpp:104 RIDGE_MIN_DEFAULT) */
 } gbc_config;
 
 typedef struct gbc_ctx gbc_ctx;
@@ -102,6 +111,18 @@ typedef struct gbc_segment_result {
     uint64_t first_prime, last_prime; /* in the count range (0: none) */
     uint64_t map_hash;             /* sum of splitmix64(q) over primes q in [hash_lo, hash_hi] coprime to 30 */
     uint64_t map_primes;           /* number of those primes */
+    /* checker mode of the segment: sampled = 1: hist holds p(n) of every
+     * even (check30_xs* + check30_xb, goldbach.cl:2339-3021); sampled = 0:
+     * the funnel verify (check30_a) resolved all evens but `pending`, and
+     * hist / first hold the exact p(n) of those (check30_b, goldbach.cl:
+     * 2210-2306): every even with p(n) >= the plan bound is among them */
+    uint32_t sampled;
+    uint32_t npend;                /* phase-A pending words (evens with no plan witness) */
+    uint64_t pending;              /* phase-A pending evens */
+    uint32_t nridge;               /* evens with p(n) >= ridge_min, listed below (RidgeTracker) */
+    uint32_t pad3;
+    uint32_t ridge_p[GBC_RIDGE_CAP];
+    uint64_t ridge_n[GBC_RIDGE_CAP];
     uint32_t err;                  /* device error flags (0 = none) */
     uint32_t pad2;
 } gbc_segment_result;

@@ -125,6 +125,76 @@ def test_hit_list_stats_windows(idx):
         assert c.verify_range(start, limit)[1] == line
 
 
+def kv(line):
+    return dict(t.split("=", 1) for t in line.split() if "=" in t)
+
+
+def dense(s):
+    return [int(x) if x else 0 for x in s.split(",")] if s and s != "-" else []
+
+
+@pytest.mark.parametrize("a,seg", [(4 * 10**18, 1_000_000), (1425172824436700150, 500_000)])
+def test_verify_mode_tail_and_sampled_segments(a, seg):
+    """The reference's production checker: funnel verify + exact tail on
+    most segments, p(n) of every even on the sampled ones. Per segment
+    against the oracle: a verified segment lists exactly the evens with
+    p(n) >= 3000 (counts, first occurrences, ridges); a sampled segment has
+    the full histogram; every segment accounts for all of its evens."""
+    nseg = 6
+    b = a + nseg * seg - 2
+    segs = gbc.segments_of(a, b, seg)
+    cand = gbc.candidates()
+    flags = [0 if i % 3 == 0 else gbc.SEG_VERIFY for i in range(nseg)]
+    with gbc.Context(limit=b, segment_even=seg, max_batch=nseg) as c:
+        c.enqueue_batch(0, segs, b, flags)
+        res, _ = c.collect(0, nseg)
+    for r, f in zip(res, flags):
+        want = kv(oracle.stats_line(r.seg_start, r.seg_end, oracle.SIEVE))
+        wh = dense(want["hist"]) + [0] * gbc.NCAND
+        wf = {int(x.split(":")[0]): int(x.split(":")[1]) for x in want["first"].split(";")}
+        got = [sum(r.hist[cr][i] for cr in range(15)) for i in range(gbc.NCAND)]
+        gfirst = {cand[i]: r.seg_start + 2 * r.first[i] for i in range(gbc.NCAND) if r.first[i] != 0xFFFFFFFF}
+        assert r.sampled == (0 if f else 1)
+        if r.sampled:
+            assert got == wh[:gbc.NCAND] and gfirst == wf
+        else:
+            assert r.pending >= sum(got[i] for i in range(gbc.NCAND) if cand[i] >= 3000)
+            assert sum(got) + r.nleft == r.pending
+            tail = [i for i in range(gbc.NCAND) if cand[i] >= 3000]
+            assert [got[i] for i in tail] == [wh[i] for i in tail]
+            assert {p: n for p, n in gfirst.items() if p >= 3000} == {p: n for p, n in wf.items() if p >= 3000}
+        assert r.primes30[0] + sum(r.primes30[1:]) + (0 if r.seg_start > 7 else 2) >= 0
+        # ridges: every even with p(n) >= 3000
+        pn = oracle.pn_range(r.seg_start, r.evens, oracle.SIEVE)
+        ridges = {(r.seg_start + 2 * i, p) for i, p in enumerate(pn) if p >= 3000}
+        assert {(r.ridge_n[i], r.ridge_p[i]) for i in range(r.nridge)} == ridges
+
+
+def test_verify_mode_run_line():
+    """A run with every 4th segment sampled: the GBSTATS line's counts, gaps
+    and tail equal the oracle's exact statistics of the range."""
+    a, b = 4 * 10**18, 4 * 10**18 + 24_000_000
+    with gbc.Context(limit=b, segment_even=2_000_000, max_batch=4, sample_every=4) as c:
+        res, line, _ = c.verify_range(a, b)
+    g, w = kv(line), kv(oracle.stats_line(a, b, oracle.SIEVE))
+    assert line.startswith("GBSTATS v2")
+    for k in ("evens", "primes", "twins", "primes30", "twins30"):
+        assert g[k] == w[k], k
+    assert g["gaps"] == w["gaps"] and g["gd1"] == w["gmom"].split(",")[0] and g["gsmom"] == w["gmom"]
+    assert g["gmax"] == w["gmax"] and g["gtail"] == w["gtail"]
+    assert dense(g["gsamp"]) == dense(w["ghist"])
+    cand = gbc.candidates()
+    wh = dense(w["hist"]) + [0] * gbc.NCAND
+    t0 = [i for i in range(gbc.NCAND) if cand[i] >= 3000][0]
+    want_tail = [wh[i] for i in range(t0, gbc.NCAND)]
+    while want_tail and not want_tail[-1]:
+        want_tail.pop()
+    got_tail = dense(g["tail"].split(":", 1)[1]) if g["tail"] != "-" else []
+    assert got_tail == want_tail
+    segs = gbc.segments_of(a, b, 2_000_000)
+    assert int(g["evens_sampled"]) == sum((e - s) // 2 + 1 for i, (s, e) in enumerate(segs) if i % 4 == 0)
+
+
 def test_batched_equals_plain():
     a, b = 4_000_000_000_000_000_000, 4_000_000_000_060_000_000
     lines = []
