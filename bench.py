@@ -235,7 +235,7 @@ def main():
         # e2e: the caller's loop, two slots in flight, results to host memory
         off = args.warmup + args.steps
         e2eb = allb[off:off + args.steps]
-        for i in range(2):
+        for i in range(min(2, args.steps)):
             segs, flags = seg_args(e2eb[i], args.sample_every, gbc)
             ctx.enqueue_batch(i, segs, limit, flags)
         t0 = time.perf_counter()

@@ -274,10 +274,10 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     // verify plan (the reference's make_plan30, include/check30.hpp:88-174,
     // with our own greedy order): per class, the smallest useful candidates
     // below GBC_TAIL_T in ascending order, each uncovered one opening a
-    // funnel with its next primes p + 30, ..., p + 120 of the same residue
-    // (members all prime, below the bound, not yet covered), plan_funnels
-    // funnels; the rest lists hold every useful candidate no funnel tests,
-    // ascending, for the exact continuation.
+    // funnel with the uncovered primes among p + 30, ..., p + 120 of the same
+    // residue (all below the bound), plan_funnels funnels; the rest lists
+    // hold every useful candidate no funnel tests, ascending, for the exact
+    // continuation.
     std::vector<uint32_t> fun;
     std::vector<uint16_t> rest;
     {
@@ -293,9 +293,11 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
                 if (covered[i]) continue;
                 uint32_t mask = 1;
                 covered[i] = 1;
+                // every uncovered prime among p + 30, ..., p + 120 joins (gaps allowed:
+                // the window read covers all five positions)
                 for (uint32_t d = 1; d <= 4; ++d) {
                     const uint32_t q = cand[i] + 30 * d;
-                    if (q >= GBC_TAIL_T || q > GBC_MAX_CAND || cidx[q] < 0 || covered[cidx[q]]) break;
+                    if (q >= GBC_TAIL_T || q > GBC_MAX_CAND || cidx[q] < 0 || covered[cidx[q]]) continue;
                     covered[cidx[q]] = 1;
                     mask |= 1u << d;
                 }

@@ -8,10 +8,15 @@
 // reaches 9781 below its first even and 3 above its last one, so every gap
 // of a prime counted in the segment has its lower prime inside the map and
 // needs no stitching: one thread per 32 blocks of 30 (8 words, one per class
-// array), primes visited in natural order, a block-wide max-scan of the
-// last prime position to give each thread its predecessor, a backward word
-// search for the first thread of a CTA.
+// array); the 8 x 32 bits are transposed to one byte per block so the primes
+// come out in natural order; a block-wide max-scan of the last prime
+// position gives each thread its predecessor, a backward word search the
+// first thread's. Positions are 32-bit offsets from the CTA's first block.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <initializer_list>
 
 #include "gbc_common.cuh"
 
@@ -36,173 +41,196 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t q)
     return z ^ (z >> 31);
 }
 
+// transpose of an 8 x 8 bit matrix: bit 8 i + j -> bit 8 j + i (the
+// delta-swap method of Warren, Hacker's Delight, section 7-3)
+__device__ __forceinline__ uint64_t transpose8(uint64_t x)
+{
+    uint64_t t;
+    t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+    x = x ^ t ^ (t << 7);
+    t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+    x = x ^ t ^ (t << 14);
+    t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+    x = x ^ t ^ (t << 28);
+    return x;
+}
+
+// x - q0 as int32, clamped to +-2^30
+__device__ __forceinline__ int32_t rel_clamp(uint64_t x, uint64_t q0)
+{
+    if (x >= q0) {
+        const uint64_t d = x - q0;
+        return d > (1u << 30) ? (1 << 30) : int32_t(d);
+    }
+    const uint64_t d = q0 - x;
+    return d > (1u << 30) ? -(1 << 30) : -int32_t(d);
+}
+
+// residue of class k (0..7) by one byte permute
+__device__ __forceinline__ uint32_t unit_of(uint32_t k) { return __byte_perm(0x0D0B0701u, 0x1D171311u, k) & 0xFF; }
+
 struct CountRanges {
     uint32_t hash_t[8][2];  // per class: bits of the hashed q range (inclusive)
     uint32_t cnt_t[8][2];   // bits of the counted primes
     uint32_t twin_t[8][2];  // bits of the counted lower twin primes
     uint32_t w_lo, w_hi;    // words covering the hashed range
+    uint32_t in_lo, in_hi;  // words inside all three ranges for every class (in_hi < in_lo: none)
 };
 
 constexpr int kCountThreads = 256;
+constexpr int32_t kNoPos = INT32_MIN;
 
 __global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegParams sp, CountRanges cr)
 {
     __shared__ uint32_t s_ghist[GBC_GBINS];
-    __shared__ unsigned long long s_gmax, s_hash, s_first, s_last, s_prev0, s_nprime;
-    __shared__ unsigned long long s_wlast[kCountThreads / 32];
-    __shared__ uint32_t s_cnt[8 + 3];
+    __shared__ int32_t s_wlast[kCountThreads / 32];
+    __shared__ int32_t s_prev0;
+    __shared__ uint32_t s_cnt[8 + 3 + 1];
+    __shared__ uint32_t s_key;
+    __shared__ int32_t s_first, s_last;
+    __shared__ unsigned long long s_hash;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x) s_ghist[i] = 0;
-    if (tid < 11) s_cnt[tid] = 0;
+    if (tid < 12) s_cnt[tid] = 0;
     const uint32_t wc0 = cr.w_lo + blockIdx.x * blockDim.x;  // first word of the CTA
+    const uint64_t q0 = bp.base + 30ull * 32ull * wc0;         // q of relative position 0
     if (tid == 0) {
-        s_gmax = 0;
+        s_key = 0;
+        s_first = INT32_MAX;
+        s_last = kNoPos;
         s_hash = 0;
-        s_nprime = 0;
-        s_first = ~0ull;
-        s_last = 0;
-        // last hashed prime before the CTA's first word (pos + 1; 0 = none)
-        unsigned long long pv = 0;
-        for (int64_t ww = int64_t(wc0) - 1; ww >= int64_t(cr.w_lo) && !pv; --ww) {
+        // last hashed prime before the CTA's first word (negative position)
+        int32_t pv = kNoPos;
+        for (int64_t ww = int64_t(wc0) - 1; ww >= int64_t(cr.w_lo) && pv == kNoPos; --ww) {
             for (uint32_t k = 0; k < 8; ++k) {
                 const uint32_t v = bp.map[size_t(k) * bp.wpc + ww] &
                                    range_mask(uint32_t(ww), cr.hash_t[k][0], cr.hash_t[k][1]);
                 if (v) {
-                    const uint64_t pos = 30ull * (32ull * uint64_t(ww) + 31 - __clz(v)) + unit30(k);
-                    if (pos + 1 > pv) pv = pos + 1;
+                    const int32_t pos =
+                        int32_t(30 * (32 * (ww - int64_t(wc0)) + 31 - __clz(v))) + int32_t(unit_of(k));
+                    if (pos > pv) pv = pos;
                 }
             }
         }
         s_prev0 = pv;
     }
+    // the counted range as positions relative to q0 (the CTA's positions
+    // stay within +-2^20, so clamping at +-2^30 changes nothing)
+    const int32_t clo = rel_clamp(sp.cnt_lo, q0), chi = rel_clamp(sp.cnt_hi, q0);
+
     const uint32_t w = wc0 + tid;
     const bool valid = w <= cr.w_hi;
+    const bool inner = w >= cr.in_lo && w <= cr.in_hi;
     uint32_t h[8], c[8], raw[8];
 #pragma unroll
     for (uint32_t k = 0; k < 8; ++k) {
         raw[k] = valid ? bp.map[size_t(k) * bp.wpc + w] : 0u;
-        h[k] = raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
-        c[k] = raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]);
+        h[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
+        c[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]);
     }
     // twins (11, 13), (17, 19) inside a block; (29, 31) into the next block
     const uint32_t next0 = valid ? bp.map[w + 1] : 0u;  // class 0, word w + 1
     const uint32_t up29 = (raw[0] >> 1) | (next0 << 31);
-    const uint32_t tw0 = __popc(raw[2] & raw[3] & range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1]));
-    const uint32_t tw1 = __popc(raw[4] & raw[5] & range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1]));
-    const uint32_t tw2 = __popc(raw[7] & up29 & range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1]));
+    const uint32_t tw0 = __popc(raw[2] & raw[3] & (inner ? ~0u : range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1])));
+    const uint32_t tw1 = __popc(raw[4] & raw[5] & (inner ? ~0u : range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1])));
+    const uint32_t tw2 = __popc(raw[7] & up29 & (inner ? ~0u : range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1])));
 
-    // first / last hashed prime of this thread's chunk (pos + 1; 0 = none)
-    unsigned long long mylast = 0;
-    uint64_t hsum = 0;
-    uint32_t nh = 0;
-    uint32_t occ = 0;
+    // one byte per block, natural order: word i of T holds blocks 4 i .. 4 i + 3
+    uint32_t T[8];
 #pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) {
-        occ |= h[k];
-        nh += __popc(h[k]);
-        if (h[k]) {
-            const uint64_t pl = 30ull * (32ull * w + 31 - __clz(h[k])) + unit30(k) + 1;
-            if (pl > mylast) mylast = pl;
-        }
-        uint32_t v = (sp.flags & GBC_SEG_NOHASH) ? 0u : h[k];
-        while (v) {
-            const uint32_t b = __ffs(v) - 1u;
-            hsum += splitmix64(bp.base + 30ull * (32ull * w + b) + unit30(k));
-            v &= v - 1u;
-        }
+    for (uint32_t g = 0; g < 4; ++g) {
+        const uint32_t sel = g | ((g + 4) << 4);
+        const uint32_t lo = __byte_perm(__byte_perm(h[0], h[1], sel), __byte_perm(h[2], h[3], sel), 0x5410);
+        const uint32_t hi = __byte_perm(__byte_perm(h[4], h[5], sel), __byte_perm(h[6], h[7], sel), 0x5410);
+        const uint64_t t = transpose8((uint64_t(hi) << 32) | lo);
+        T[2 * g] = uint32_t(t);
+        T[2 * g + 1] = uint32_t(t >> 32);
     }
+    const int32_t cbase = int32_t(960 * tid);  // position of this thread's first block
+    int32_t mylast = kNoPos;
+    uint32_t nh = 0;
+#pragma unroll
+    for (int i = 7; i >= 0; --i)
+        if (T[i] && mylast == kNoPos) {
+            const uint32_t b = 31 - __clz(T[i]);
+            mylast = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+        }
     // exclusive max-scan of mylast over the CTA
-    unsigned long long v = mylast;
+    int32_t v = mylast;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long n = __shfl_up_sync(~0u, v, o);
+        const int32_t n = __shfl_up_sync(~0u, v, o);
         if (lane >= uint32_t(o) && n > v) v = n;
     }
-    unsigned long long excl = __shfl_up_sync(~0u, v, 1);
-    if (lane == 0) excl = 0;
+    int32_t excl = __shfl_up_sync(~0u, v, 1);
+    if (lane == 0) excl = kNoPos;
     if (lane == 31) s_wlast[warp] = v;
     __syncthreads();
-    unsigned long long prev = s_prev0;
+    int32_t prev = s_prev0;
     if (excl > prev) prev = excl;
     for (uint32_t i = 0; i < warp; ++i)
         if (s_wlast[i] > prev) prev = s_wlast[i];
 
-    // gaps of the counted primes, in natural order
-    unsigned long long gmax = 0, cfirst = ~0ull, clast = 0;
-    uint32_t err = 0;
-    while (occ) {
-        const uint32_t b = __ffs(occ) - 1u;
-        occ &= occ - 1u;
+    // the primes in natural order: gaps of the counted ones, the hash of all
+    const bool hash = !(sp.flags & GBC_SEG_NOHASH);
+    uint64_t hsum = 0;
+    uint32_t key = 0, err = 0;
+    int32_t cfirst = INT32_MAX, clast = kNoPos;
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
-            if (!((h[k] >> b) & 1u)) continue;
-            const uint64_t pos = 30ull * (32ull * w + b) + unit30(k);
-            if ((c[k] >> b) & 1u) {
-                const uint64_t q = bp.base + pos;
-                if (q < cfirst) cfirst = q;
-                if (q > clast) clast = q;
-                if (prev) {
-                    const uint64_t g = pos + 1 - prev;
-                    const uint64_t lower = q - g;
+    for (uint32_t i = 0; i < 8; ++i) {
+        uint32_t x = T[i];
+        nh += __popc(x);
+        while (x) {
+            const uint32_t b = __ffs(x) - 1u;
+            x &= x - 1u;
+            const int32_t pos = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+            if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
+            if (pos >= clo && pos <= chi) {
+                if (pos < cfirst) cfirst = pos;
+                clast = pos;
+                if (prev != kNoPos) {
+                    const uint32_t g = uint32_t(pos - prev);
                     if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
                     else atomicAdd(&s_ghist[g / 2], 1u);
-                    const unsigned long long key =
-                        (g << 32) | (0xFFFFFFFFull - uint32_t(lower - sp.hash_lo));
-                    if (key > gmax) gmax = key;
+                    // largest gap, the smallest lower prime on ties: g << 21 | ~(lower + 2^20)
+                    const uint32_t k2 = (g << 21) | (0x1FFFFFu - uint32_t(prev + (1 << 20)));
+                    if (k2 > key) key = k2;
                     if (g >= GBC_GTAIL) {
                         const uint32_t slot = atomicAdd(&sp.res->ntail, 1u);
                         if (slot < GBC_TAIL_CAP) {
-                            sp.res->tail_g[slot] = uint32_t(g);
-                            sp.res->tail_lo[slot] = lower;
+                            sp.res->tail_g[slot] = g;
+                            sp.res->tail_lo[slot] = q0 + uint64_t(int64_t(prev));
                         } else err |= kErrTailOverflow;
                     }
-                } else if (q > 7) {
+                } else if (q0 + uint64_t(int64_t(pos)) > 7) {
                     err |= kErrNoPred;
                 }
             }
-            prev = pos + 1;
+            prev = pos;
         }
     }
     if (err) atomicOr(&sp.res->err, err);
 
-    // warp reductions of the 64-bit values first (shared 64-bit min / max /
-    // add contended by a whole CTA would serialize), then one atomic per warp
+    // warp reductions, then one shared atomic per warp
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long hs = __shfl_xor_sync(~0u, hsum, o);
-        const unsigned long long gm = __shfl_xor_sync(~0u, gmax, o);
-        const unsigned long long cf = __shfl_xor_sync(~0u, cfirst, o);
-        const unsigned long long cl = __shfl_xor_sync(~0u, clast, o);
-        hsum += hs;
-        if (gm > gmax) gmax = gm;
-        if (cf < cfirst) cfirst = cf;
-        if (cl > clast) clast = cl;
-    }
-
-    // block reductions
-    const uint32_t r0 = __reduce_add_sync(~0u, __popc(c[0])), r1 = __reduce_add_sync(~0u, __popc(c[1]));
-    const uint32_t r2 = __reduce_add_sync(~0u, __popc(c[2])), r3 = __reduce_add_sync(~0u, __popc(c[3]));
-    const uint32_t r4 = __reduce_add_sync(~0u, __popc(c[4])), r5 = __reduce_add_sync(~0u, __popc(c[5]));
-    const uint32_t r6 = __reduce_add_sync(~0u, __popc(c[6])), r7 = __reduce_add_sync(~0u, __popc(c[7]));
-    const uint32_t t0 = __reduce_add_sync(~0u, tw0), t1 = __reduce_add_sync(~0u, tw1);
-    const uint32_t t2 = __reduce_add_sync(~0u, tw2), nhs = __reduce_add_sync(~0u, nh);
+    for (int o = 16; o > 0; o >>= 1) hsum += __shfl_xor_sync(~0u, hsum, o);
+    key = __reduce_max_sync(~0u, key);
+    cfirst = __reduce_min_sync(~0u, cfirst);
+    clast = __reduce_max_sync(~0u, clast);
+    uint32_t r8[12];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r8[k] = __reduce_add_sync(~0u, __popc(c[k]));
+    r8[8] = __reduce_add_sync(~0u, tw0);
+    r8[9] = __reduce_add_sync(~0u, tw1);
+    r8[10] = __reduce_add_sync(~0u, tw2);
+    r8[11] = __reduce_add_sync(~0u, nh);
     if (lane == 0) {
-        atomicAdd(&s_cnt[0], r0);
-        atomicAdd(&s_cnt[1], r1);
-        atomicAdd(&s_cnt[2], r2);
-        atomicAdd(&s_cnt[3], r3);
-        atomicAdd(&s_cnt[4], r4);
-        atomicAdd(&s_cnt[5], r5);
-        atomicAdd(&s_cnt[6], r6);
-        atomicAdd(&s_cnt[7], r7);
-        atomicAdd(&s_cnt[8], t0);
-        atomicAdd(&s_cnt[9], t1);
-        atomicAdd(&s_cnt[10], t2);
-        atomicAdd(&s_nprime, (unsigned long long)nhs);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) atomicAdd(&s_cnt[k], r8[k]);
         atomicAdd(&s_hash, (unsigned long long)hsum);
-        if (gmax) atomicMax(&s_gmax, gmax);
-        if (cfirst != ~0ull) atomicMin(&s_first, cfirst);
-        if (clast) atomicMax(&s_last, clast);
+        atomicMax(&s_key, key);
+        atomicMin(&s_first, cfirst);
+        atomicMax(&s_last, clast);
     }
     __syncthreads();
     gbc_segment_result *res = sp.res;
@@ -213,13 +241,20 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegPara
     } else if (tid < 11) {
         if (s_cnt[tid]) atomicAdd((unsigned long long *)&res->twins[tid - 8], (unsigned long long)s_cnt[tid]);
     } else if (tid == 11) {
-        atomicAdd((unsigned long long *)&res->map_hash, s_hash);
-        atomicAdd((unsigned long long *)&res->map_primes, s_nprime);
+        if (hash) atomicAdd((unsigned long long *)&res->map_hash, s_hash);
+        atomicAdd((unsigned long long *)&res->map_primes, (unsigned long long)s_cnt[11]);
     } else if (tid == 12) {
-        if (s_gmax) atomicMax((unsigned long long *)&res->gmax_key, s_gmax);
+        if (s_key) {
+            const uint64_t g = s_key >> 21;
+            const uint64_t lower = q0 + uint64_t(int64_t(int32_t(0x1FFFFFu - (s_key & 0x1FFFFFu)) - (1 << 20)));
+            const unsigned long long k64 = (g << 32) | (0xFFFFFFFFull - uint32_t(lower - sp.hash_lo));
+            atomicMax((unsigned long long *)&res->gmax_key, k64);
+        }
     } else if (tid == 13) {
-        if (s_first != ~0ull) atomicMin((unsigned long long *)&res->first_prime, s_first);
-        if (s_last) atomicMax((unsigned long long *)&res->last_prime, s_last);
+        if (s_first != INT32_MAX)
+            atomicMin((unsigned long long *)&res->first_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_first))));
+        if (s_last != kNoPos)
+            atomicMax((unsigned long long *)&res->last_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_last))));
     }
 }
 
@@ -250,6 +285,29 @@ static void class_range(uint64_t base, uint64_t a, uint64_t b, uint32_t out[8][2
     }
 }
 
+// words [lo, hi] fully inside the bit ranges of every class (hi < lo: none)
+static void inner_words(const uint32_t t[8][2], uint32_t &lo, uint32_t &hi)
+{
+    uint64_t l = 0, h = UINT32_MAX;
+    for (int k = 0; k < 8; ++k) {
+        if (t[k][1] < t[k][0]) {
+            lo = 1;
+            hi = 0;
+            return;
+        }
+        l = std::max<uint64_t>(l, (uint64_t(t[k][0]) + 31) / 32);
+        const uint64_t e = (uint64_t(t[k][1]) + 1) / 32;  // first word not entirely inside
+        h = std::min<uint64_t>(h, e == 0 ? 0 : e - 1);
+        if (e == 0) {
+            lo = 1;
+            hi = 0;
+            return;
+        }
+    }
+    lo = uint32_t(l);
+    hi = uint32_t(h);
+}
+
 void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStream_t st)
 {
     gbk::CountRanges cr;
@@ -265,6 +323,12 @@ void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStre
     if (tlo > thi) return;
     cr.w_lo = tlo / 32;
     cr.w_hi = thi / 32;
+    uint32_t a0, a1, b0, b1, c0, c1;
+    inner_words(cr.hash_t, a0, a1);
+    inner_words(cr.cnt_t, b0, b1);
+    inner_words(cr.twin_t, c0, c1);
+    cr.in_lo = std::max({a0, b0, c0});
+    cr.in_hi = std::min({a1, b1, c1});
     const uint32_t nw = cr.w_hi - cr.w_lo + 1;
     const uint32_t blocks = (nw + gbk::kCountThreads - 1) / gbk::kCountThreads;
     gbk::k_count<<<blocks, gbk::kCountThreads, 0, st>>>(bp, sp, cr);

@@ -156,9 +156,14 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
 // rounded to nearest.
 __device__ __forceinline__ uint32_t mod_below(uint64_t x, uint32_t p, float rp)
 {
-    const uint32_t qe = __float2uint_rz(__ull2float_rz(x) * rp);
+    // float(x) from its two 32-bit halves (32-bit conversions only: 64-bit
+    // integer <-> float conversions are multi-instruction sequences)
+    const float xf = fmaf(__uint2float_rz(uint32_t(x >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(x)));
+    const uint32_t qe = __float2uint_rz(xf * rp);
     int64_t r = int64_t(x - uint64_t(qe) * p);
-    const int32_t q2 = __float2int_rn(__ll2float_rz(r) * rp);
+    // |r| < 2^42: float(r) from its halves, exactly as above
+    const float rf = fmaf(float(int32_t(r >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(r)));
+    const int32_t q2 = __float2int_rn(rf * rp);
     r -= int64_t(q2) * p;
     if (r < 0) r += p;
     if (r >= int64_t(p)) r -= p;
