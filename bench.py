@@ -254,17 +254,23 @@ def main():
         exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9
         cfg = ctx.cfg
     hbm, kind = peaks()
-    # the dominant stage and its algorithmic HBM bytes per launch (per step)
-    dom = max(stage, key=stage.get)
-    kernel = {"tile": "k_tile", "large": "k_hitlist", "check": "k_verify", "count": "k_count"}[dom]
-    map_bytes = 8 * (SEG / 30) / 8 * args.batch        # the batch's class map, one byte per 8 q
-    alg = {"tile": map_bytes,                           # one write of the map
-           "large": 4 * NPRIMES_4E18,                   # the sieving-prime stream
-           "check": map_bytes,                          # one read of the map
-           "count": map_bytes}[dom]                     # one read of the map
-    per_launch_ms = stage[dom] / args.steps
-    launches_per_step = args.batch if dom in ("check", "count") else 1
-    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    # per stage: launches per step and algorithmic HBM bytes per launch
+    seg_map = 8 * (SEG / 30) / 8                        # a segment's class map: one bit per q coprime to 30
+    per_stage = {
+        "tile": (1, seg_map * args.batch),              # one write of the batch's map
+        "large": (1, 4 * NPRIMES_4E18),                 # the sieving-prime stream (hit lists / large primes)
+        "check": (args.batch, seg_map),                 # one read of the segment's map
+        "count": (args.batch, seg_map),                 # one read of the segment's map
+    }
+    kernels = {"tile": "k_tile", "large": "k_hitlist", "check": "k_verify", "count": "k_count"}
+    stage_bw = {}
+    for s, (nl, b) in per_stage.items():
+        ms = stage[s] / args.steps / nl
+        stage_bw[s] = {"kernel": kernels[s], "ms_per_launch": ms, "alg_bytes_per_launch": b,
+                       "achieved_gbs": b / (ms / 1e3) / 1e9 if ms > 0 else None}
+    dom = max(stage, key=stage.get)                     # the stage with the most device time per step
+    kernel = kernels[dom]
+    achieved = stage_bw[dom]["achieved_gbs"]
     traffic = ncu_traffic(kernel)
     out = {
         "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": 1, "steps": args.steps,
@@ -286,9 +292,9 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": kind,
-                     "alg_bytes_per_step": alg, "launches_per_step": launches_per_step},
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic, "peak_kind": kind,
+                     "alg_bytes_per_launch": stage_bw[dom]["alg_bytes_per_launch"],
+                     "ms_per_launch": stage_bw[dom]["ms_per_launch"], "stages": stage_bw},
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
