@@ -199,9 +199,8 @@ def main():
     ap.add_argument("--sample-every", type=int, default=256)
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--p-mid", type=int, default=0)
-    ap.add_argument("--large-pass-mb", type=int, default=0)
     ap.add_argument("--hl-mode", type=int, default=0)
-    ap.add_argument("--hl-pass-mb", type=int, default=0)
+    ap.add_argument("--launch-mode", type=int, default=0)
     ap.add_argument("--plan-funnels", type=int, default=0)
     ap.add_argument("--ref-evens", type=int, default=1_000_000)
     ap.add_argument("--cpu-evens", type=int, default=4_000_000)
@@ -221,8 +220,8 @@ def main():
     limit = allb[-1][-1][2]
     evens_per_step = sum((e - s) // 2 + 1 for _, s, e in allb[0])
     with gbc.Context(limit=limit, segment_even=SEG, max_batch=args.batch, tile_log2=args.tile_log2,
-                     p_mid=args.p_mid, large_pass_mb=args.large_pass_mb, hl_mode=args.hl_mode,
-                     hl_pass_mb=args.hl_pass_mb, plan_funnels=args.plan_funnels) as ctx:
+                     p_mid=args.p_mid, hl_mode=args.hl_mode, launch_mode=args.launch_mode,
+                     plan_funnels=args.plan_funnels) as ctx:
         device_run(ctx, allb[:args.warmup], limit, args.sample_every, gbc)   # warm-up (builds the tables)
         launches0 = ctx.launches()
         timed = allb[args.warmup:args.warmup + args.steps]

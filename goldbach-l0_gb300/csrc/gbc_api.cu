@@ -1,18 +1,22 @@
 // gbc_api.cu -- the per-segment C ABI (include/gbc.h): context, tables,
-// slots, batch enqueue and bounded-wait collect.
+// slots, batch planning, graph capture and replay, bounded-wait collect.
 //
 // Replaces the reference's Level Zero run driver plumbing
 // (src/verifier.cpp:346-354 construction, 633-692 base primes, 853-1001
 // buffer sizing, 1361-1440 table upload, 1741-2146 per-segment enqueue,
-// 2402-2444 collect) for one CUDA device: two slots, each with its own
-// stream, class map, first-bit table and result area; a batch is enqueued
-// on a slot and collected later, so the host's work on batch k overlaps the
-// GPU's work on batch k + 1.
+// 2402-2444 collect) for one CUDA device: nslots slots, each with its own
+// stream, class-map buffer, first-bit table, result area and batch
+// descriptor. A batch is planned on the host into the slot's pinned
+// descriptor image; one host-to-device copy of it and a fixed sequence of
+// persistent kernels (captured once per slot as a CUDA graph, then
+// replayed) run the whole pipeline; it is collected later, so the host's
+// work on batch k overlaps the GPU's work on batch k + 1.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -55,7 +59,52 @@ uint32_t inv_mod_small(uint32_t a, uint32_t m)  // a^-1 mod m, 0 if none
     return uint32_t(t);
 }
 
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
 }  // namespace
+
+DescLayout::DescLayout(uint32_t nrun_cap, uint32_t nseg_cap)
+{
+    size_t o = align_up(sizeof(gbk::BatchHeader), 64);
+    runs = o;
+    o = align_up(o + size_t(nrun_cap) * sizeof(gbk::BatchParams), 64);
+    segs = o;
+    o = align_up(o + size_t(nseg_cap) * sizeof(gbk::SegParams), 64);
+    tile_pref = o;
+    o = align_up(o + size_t(nrun_cap + 1) * 4, 64);
+    chk_pref = o;
+    o = align_up(o + size_t(nseg_cap + 1) * 4, 64);
+    ver_pref = o;
+    o = align_up(o + size_t(nseg_cap + 1) * 4, 64);
+    cnt_pref = o;
+    o = align_up(o + size_t(nseg_cap + 1) * 4, 64);
+    bytes = o;
+}
+
+gbk::BatchDesc DescLayout::device(const uint8_t *b) const
+{
+    gbk::BatchDesc d;
+    d.h = reinterpret_cast<const gbk::BatchHeader *>(b);
+    d.work = const_cast<uint32_t *>(d.h->work);
+    d.runs = reinterpret_cast<const gbk::BatchParams *>(b + runs);
+    d.segs = reinterpret_cast<const gbk::SegParams *>(b + segs);
+    d.tile_pref = reinterpret_cast<const uint32_t *>(b + tile_pref);
+    d.chk_pref = reinterpret_cast<const uint32_t *>(b + chk_pref);
+    d.ver_pref = reinterpret_cast<const uint32_t *>(b + ver_pref);
+    d.cnt_pref = reinterpret_cast<const uint32_t *>(b + cnt_pref);
+    return d;
+}
+
+void DescImage::bind(uint8_t *b, const DescLayout &l)
+{
+    h = reinterpret_cast<gbk::BatchHeader *>(b);
+    runs = reinterpret_cast<gbk::BatchParams *>(b + l.runs);
+    segs = reinterpret_cast<gbk::SegParams *>(b + l.segs);
+    tile_pref = reinterpret_cast<uint32_t *>(b + l.tile_pref);
+    chk_pref = reinterpret_cast<uint32_t *>(b + l.chk_pref);
+    ver_pref = reinterpret_cast<uint32_t *>(b + l.ver_pref);
+    cnt_pref = reinterpret_cast<uint32_t *>(b + l.cnt_pref);
+}
 
 // The odd primes <= n (n < 2^32), by a segmented sieve on all host threads.
 std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n)
@@ -119,6 +168,15 @@ static int fail(gbc_ctx *c, int code, const std::string &msg)
             return fail(ctx, GBC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
     } while (0)
 
+// device allocation counted in the context's footprint
+template <class T>
+static cudaError_t dev_alloc(gbc_ctx *ctx, T **p, size_t bytes)
+{
+    const cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), bytes);
+    if (e == cudaSuccess) ctx->device_bytes += bytes;
+    return e;
+}
+
 extern "C" int gbc_candidates(uint16_t *out, int cap)
 {
     std::vector<uint32_t> p = gbh_odd_primes_upto(GBC_MAX_CAND);
@@ -127,24 +185,60 @@ extern "C" int gbc_candidates(uint16_t *out, int cap)
     return n;
 }
 
+// class-array words of a run of nblk bits: 64 bits of slack for the
+// checkers' window reads, rounded to 32 words (128-byte aligned maps)
+static uint64_t run_wpc(uint64_t nblk) { return align_up((nblk + 64 + 31) / 32, 32); }
+
 static int slot_alloc(gbc_ctx *ctx, Slot &s)
 {
+    const auto &cfg = ctx->cfg;
     CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
     for (auto &e : s.ev) CK(cudaEventCreate(&e));
-    CK(cudaMalloc(&s.map, size_t(8) * ctx->wpc_cap * 4 + kMapPadBytes));
-    CK(cudaMemset(s.map, 0, size_t(8) * ctx->wpc_cap * 4 + kMapPadBytes));
-    CK(cudaMalloc(&s.xfirst, std::max<size_t>(size_t(8) * ctx->n_mid * 4, 4)));
-    CK(cudaMalloc(&s.res, size_t(ctx->cfg.max_batch) * sizeof(gbc_segment_result)));
-    CK(cudaMalloc(&s.err, 4));
-    if (ctx->cfg.want_pn) {
-        s.pn_stride = ctx->cfg.segment_even / 2 + 1;
-        CK(cudaMalloc(&s.pn, size_t(ctx->cfg.max_batch) * s.pn_stride * 2));
+    // max_batch full segments in one run, plus every further run's margin
+    s.map_words = size_t(8) * ctx->wpc_cap + size_t(8) * cfg.max_runs * 448;
+    CK(dev_alloc(ctx, &s.map, s.map_words * 4 + kMapPadBytes));
+    CK(cudaMemset(s.map, 0, s.map_words * 4 + kMapPadBytes));
+    s.xfirst_words = std::max<size_t>(size_t(8) * ctx->n_mid * cfg.max_runs, 1);
+    CK(dev_alloc(ctx, &s.xfirst, s.xfirst_words * 4));
+    CK(dev_alloc(ctx, &s.res, size_t(cfg.max_batch) * sizeof(gbc_segment_result)));
+    CK(dev_alloc(ctx, &s.err, 4));
+    if (cfg.want_pn) {
+        s.pn_stride = cfg.segment_even / 2 + 1;
+        CK(dev_alloc(ctx, &s.pn, size_t(cfg.max_batch) * s.pn_stride * 2));
     }
     // phase-A pending words: up to 1/16 of a segment's words (the plan
     // leaves ~1e-4 of the evens; an overflow fails the batch closed)
-    s.pend_cap = uint32_t(std::max<uint64_t>(4096, (ctx->cfg.segment_even / 2 / 32 + 64) / 16));
-    CK(cudaMalloc(&s.pend, size_t(ctx->cfg.max_batch) * s.pend_cap * sizeof(uint2)));
+    s.pend_cap = uint32_t(std::max<uint64_t>(4096, (cfg.segment_even / 2 / 32 + 64) / 16));
+    CK(dev_alloc(ctx, &s.pend, size_t(cfg.max_batch) * s.pend_cap * sizeof(uint2)));
+    CK(cudaMallocHost(&s.desc_host, ctx->layout.bytes));
+    std::memset(s.desc_host, 0, ctx->layout.bytes);
+    CK(dev_alloc(ctx, &s.desc_dev, ctx->layout.bytes));
+    CK(cudaMemset(s.desc_dev, 0, ctx->layout.bytes));
+    s.img.bind(s.desc_host, ctx->layout);
+    s.dd = ctx->layout.device(s.desc_dev);
     return GBC_OK;
+}
+
+static void slot_free(Slot &s)
+{
+    if (s.st) cudaStreamSynchronize(s.st);
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    for (auto &e : s.ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(s.map);
+    cudaFree(s.xfirst);
+    cudaFree(s.res);
+    cudaFree(s.err);
+    cudaFree(s.pn);
+    cudaFree(s.pend);
+    cudaFree(s.desc_dev);
+    if (s.desc_host) cudaFreeHost(s.desc_host);
+    cudaFree(s.chk_map);
+    cudaFree(s.chk_desc_dev);
+    cudaFree(s.chk_count);
+    if (s.chk_desc_host) cudaFreeHost(s.chk_desc_host);
+    if (s.st) cudaStreamDestroy(s.st);
+    s = Slot{};
 }
 
 extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
@@ -159,20 +253,24 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.segment_even) cfg.segment_even = GBC_DEFAULT_SEGMENT;
     if (cfg.segment_even & 1) cfg.segment_even += 1;
     if (!cfg.max_batch) cfg.max_batch = 8;
+    if (!cfg.max_runs) cfg.max_runs = cfg.max_batch;
     if (!cfg.tile_log2) cfg.tile_log2 = 20;
     if (!cfg.p_mid) cfg.p_mid = 1u << 22;
-    if (!cfg.large_pass_mb) cfg.large_pass_mb = 4096;  // one pass: the per-prime setup outweighs L2 misses
     if (!cfg.mtab_max_gb) cfg.mtab_max_gb = 48;
-    if (!cfg.hl_pass_mb) cfg.hl_pass_mb = 4096;  // one pass: the divisions outweigh L2 misses
+    if (!cfg.nslots) cfg.nslots = 2;
     if (!cfg.sample_every) cfg.sample_every = 1;
     if (!cfg.plan_funnels) cfg.plan_funnels = 40;
     if (!cfg.ridge_min) cfg.ridge_min = GBC_TAIL_T;
+    if (!cfg.launch_mode) cfg.launch_mode = 1;
     if (cfg.plan_funnels > 256) cfg.plan_funnels = 256;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
         rc = fail(ctx, GBC_E_ARG, "segment_even outside [1000, 2^33]");
     else if (cfg.max_batch > 256) rc = fail(ctx, GBC_E_ARG, "max_batch above 256");
+    else if (cfg.max_runs > cfg.max_batch) rc = fail(ctx, GBC_E_ARG, "max_runs above max_batch");
+    else if (cfg.nslots < 2 || cfg.nslots > GBC_MAX_SLOTS) rc = fail(ctx, GBC_E_ARG, "nslots outside [2, 8]");
+    else if (cfg.launch_mode > 2) rc = fail(ctx, GBC_E_ARG, "launch_mode outside [0, 2]");
     else if (cfg.tile_log2 < 14 || cfg.tile_log2 > 20) rc = fail(ctx, GBC_E_ARG, "tile_log2 outside [14, 20]");
     else if (cfg.p_mid < 128) rc = fail(ctx, GBC_E_ARG, "p_mid below 128");
     else if (uint64_t(cfg.max_batch) * cfg.segment_even / 30 > (1ull << 31))
@@ -189,8 +287,9 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         return fail(ctx, GBC_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     }
     int dev = cfg.device;
-    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (ctx->sm_count <= 0) ctx->sm_count = 1;
+    cudaDeviceGetAttribute(&ctx->grids.sm, cudaDevAttrMultiProcessorCount, dev);
+    if (ctx->grids.sm <= 0) ctx->grids.sm = 1;
+    ctx->grids.max_seg = int(cfg.max_batch);
 
     // sieving primes: every odd prime <= floor(sqrt(limit + 3)) + 16, saturated below 2^32
     // (the reference's base_prime_bound, include/primes.hpp:222-225)
@@ -200,7 +299,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     const auto &pr = ctx->primes;
     ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
     ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());
-    const uint32_t tb = 1u << cfg.tile_log2, tw = tb / 32;
+    const uint32_t tb = 1u << cfg.tile_log2;
     ctx->i_warp = uint32_t(std::lower_bound(pr.begin(), pr.end(), std::max(tb / 64, 72u)) - pr.begin());
     if (ctx->i_warp > ctx->n_mid) ctx->i_warp = ctx->n_mid;
     std::vector<uint32_t> magic(ctx->n_mid);
@@ -213,7 +312,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         uint64_t c = uint64_t(std::cbrt(double(cfg.limit + 3))) + 2;
         while (c * c * c < cfg.limit + 3) ++c;
         const uint64_t budget_m = uint64_t(cfg.mtab_max_gb) * 1000000000ull * 30;
-        const uint64_t by_budget = (cfg.limit + 3) / budget_m + 1;
+        // (a little under the budget: the table is rounded up to 32-byte words)
+        const uint64_t by_budget = (cfg.limit + 3) / (budget_m - budget_m / 1024) + 1;
         ctx->p_hl = std::max<uint64_t>({uint64_t(cfg.p_mid) + 1, c, by_budget});
         ctx->n_hl = uint32_t(std::lower_bound(pr.begin(), pr.end(), ctx->p_hl) - pr.begin());
         if (ctx->n_hl < ctx->n_mid) ctx->n_hl = ctx->n_mid;
@@ -311,38 +411,42 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         }
     }
 
-    // slot geometry: a batch of max_batch full segments plus the 9781 + 3 margin
+    // one run of max_batch full segments plus the 9781 + 3 margin
     const uint64_t span = uint64_t(cfg.max_batch) * cfg.segment_even + GBC_MAX_CAND + 3 + 64;
     const uint64_t nblk_cap = span / 30 + 4;
-    const uint64_t tiles_cap = (nblk_cap + 64 + tb - 1) / tb;
-    ctx->wpc_cap = uint32_t(tiles_cap * tw);
+    ctx->wpc_cap = uint32_t(std::max<uint64_t>(run_wpc(nblk_cap), align_up(run_wpc(nblk_cap), tb / 32)));
+    ctx->layout = DescLayout(cfg.max_runs, cfg.max_batch);
 
     *out = ctx;
-    CK(cudaMalloc(&ctx->d_primes, std::max<size_t>(pr.size(), 1) * 4));
+    gbh::tile_attributes(cfg.tile_log2, ctx->gi);
+    gbh::query_check_grids(ctx->grids);
+    gbh::query_count_grids(ctx->grids);
+    CK(dev_alloc(ctx, &ctx->d_primes, std::max<size_t>(pr.size(), 1) * 4));
     CK(cudaMemcpy(ctx->d_primes, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_magic, std::max<size_t>(magic.size(), 1) * 4));
+    CK(dev_alloc(ctx, &ctx->d_magic, std::max<size_t>(magic.size(), 1) * 4));
     if (!magic.empty()) CK(cudaMemcpy(ctx->d_magic, magic.data(), magic.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_pat, pat.size() * 4));
+    CK(dev_alloc(ctx, &ctx->d_pat, pat.size() * 4));
     CK(cudaMemcpy(ctx->d_pat, pat.data(), pat.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_skip, skip.size() * 4));
+    CK(dev_alloc(ctx, &ctx->d_skip, skip.size() * 4));
     CK(cudaMemcpy(ctx->d_skip, skip.data(), skip.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_inv, inv.size() * 2));
+    CK(dev_alloc(ctx, &ctx->d_inv, inv.size() * 2));
     CK(cudaMemcpy(ctx->d_inv, inv.data(), inv.size() * 2, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_cand, cand.size() * 2));
+    CK(dev_alloc(ctx, &ctx->d_cand, cand.size() * 2));
     CK(cudaMemcpy(ctx->d_cand, cand.data(), cand.size() * 2, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_list, list.size() * 2));
+    CK(dev_alloc(ctx, &ctx->d_list, list.size() * 2));
     CK(cudaMemcpy(ctx->d_list, list.data(), list.size() * 2, cudaMemcpyHostToDevice));
     ctx->ct.cand = ctx->d_cand;
     ctx->ct.list = ctx->d_list;
     ctx->ct.ridge_min = cfg.ridge_min;
-    CK(cudaMalloc(&ctx->d_fun, std::max<size_t>(fun.size(), 1) * 4));
+    CK(dev_alloc(ctx, &ctx->d_fun, std::max<size_t>(fun.size(), 1) * 4));
     if (!fun.empty()) CK(cudaMemcpy(ctx->d_fun, fun.data(), fun.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&ctx->d_rest, std::max<size_t>(rest.size(), 1) * 2));
+    CK(dev_alloc(ctx, &ctx->d_rest, std::max<size_t>(rest.size(), 1) * 2));
     if (!rest.empty()) CK(cudaMemcpy(ctx->d_rest, rest.data(), rest.size() * 2, cudaMemcpyHostToDevice));
     ctx->vt.cand = ctx->d_cand;
     ctx->vt.fun = ctx->d_fun;
     ctx->vt.rest = ctx->d_rest;
     ctx->vt.ridge_min = cfg.ridge_min;
+    ctx->slot.resize(cfg.nslots);
     for (auto &s : ctx->slot)
         if (int r = slot_alloc(ctx, s)) return r;
     CK(cudaDeviceSynchronize());
@@ -352,18 +456,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
 extern "C" void gbc_destroy(gbc_ctx *ctx)
 {
     if (!ctx) return;
-    for (auto &s : ctx->slot) {
-        if (s.st) cudaStreamSynchronize(s.st);
-        for (auto &e : s.ev)
-            if (e) cudaEventDestroy(e);
-        cudaFree(s.map);
-        cudaFree(s.xfirst);
-        cudaFree(s.res);
-        cudaFree(s.err);
-        cudaFree(s.pn);
-        cudaFree(s.pend);
-        if (s.st) cudaStreamDestroy(s.st);
-    }
+    for (auto &s : ctx->slot) slot_free(s);
     cudaFree(ctx->d_fun);
     cudaFree(ctx->d_rest);
     cudaFree(ctx->mtab);
@@ -396,64 +489,144 @@ extern "C" int gbc_get_config(const gbc_ctx *ctx, gbc_config *out)
     return GBC_OK;
 }
 
+static bool bad_slot(const gbc_ctx *ctx, int slot) { return !ctx || slot < 0 || slot >= int(ctx->slot.size()); }
+
 extern "C" void *gbc_stream(gbc_ctx *ctx, int slot)
 {
-    if (!ctx || slot < 0 || slot > 1) return nullptr;
+    if (bad_slot(ctx, slot)) return nullptr;
     return ctx->slot[slot].st;
 }
 
 extern "C" uint64_t gbc_launch_count(const gbc_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
-// Batch geometry and the per-segment kernel parameters (the reference's
-// segment_geometry / class_geometry / seg30 / count30_limits,
-// src/host_math.cpp:13-78, include/check30.hpp:196-210,
-// include/gstats.hpp:272-296, for the batch map layout).
-int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl, int nseg, uint64_t limit,
-                   gbk::BatchParams &bp)
+extern "C" int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out)
 {
-    const auto &cfg = ctx->cfg;
-    if (nseg < 1 || uint32_t(nseg) > cfg.max_batch) return fail(ctx, GBC_E_ARG, "nseg outside [1, max_batch]");
-    if (limit > cfg.limit || limit & 1) return fail(ctx, GBC_E_ARG, "limit odd or above the context's limit");
-    for (int i = 0; i < nseg; ++i) {
-        const uint64_t a = b[2 * i], e = b[2 * i + 1];
-        if ((a | e) & 1 || a < 4 || e < a || e > limit)
-            return fail(ctx, GBC_E_ARG, "segment bounds must be even with 4 <= start <= end <= limit");
-        if (e - a > cfg.segment_even) return fail(ctx, GBC_E_ARG, "segment longer than segment_even");
-        if (i && a != b[2 * i - 1] + 2) return fail(ctx, GBC_E_ARG, "segments must be consecutive");
-    }
-    const uint64_t s0 = b[0], sN = b[2 * nseg - 1];
+    if (!ctx || !out) return GBC_E_ARG;
+    out->launches = ctx->launches;
+    out->batches = ctx->batches;
+    out->graph_replays = ctx->graph_replays;
+    out->selfchecks = ctx->selfchecks;
+    out->mtab_builds = ctx->mtab_builds;
+    out->mtab_bytes = ctx->mtab_bytes;
+    out->mtab_build_ms = ctx->mtab_build_ms;
+    out->device_bytes = ctx->device_bytes;
+    return GBC_OK;
+}
+
+// One run (class map) of a batch: geometry, primes that reach it, and the
+// shared tables (the reference's segment_geometry / class_geometry,
+// src/host_math.cpp:13-78, for one map per run).
+static void plan_run(const gbc_ctx *ctx, gbk::BatchParams &bp, uint64_t s0, uint64_t sN)
+{
+    const auto &pr = ctx->primes;
     const uint64_t qlo = s0 > GBC_MAX_CAND + 30 ? s0 - GBC_MAX_CAND : 0;
     bp.base = qlo / 30 * 30;
     bp.qmax = sN + 3;
     const uint64_t nblk = (bp.qmax - bp.base) / 30 + 1;
-    const uint32_t tb = 1u << cfg.tile_log2, tw = tb / 32;
-    const uint64_t tiles = (nblk + 64 + tb - 1) / tb;
-    if (tiles * tw > ctx->wpc_cap) return fail(ctx, GBC_E_ARG, "batch wider than the slot's class map");
+    const uint32_t tb = 1u << ctx->cfg.tile_log2;
     bp.nblk = uint32_t(nblk);
-    bp.tiles_pc = uint32_t(tiles);
-    bp.wpc = uint32_t(tiles * tw);
-    bp.map = s.map;
+    bp.wpc = uint32_t(run_wpc(nblk));
+    bp.tiles_pc = uint32_t((uint64_t(bp.wpc) * 32 + tb - 1) / tb);
+    bp.tile_log2 = ctx->cfg.tile_log2;
     bp.primes = ctx->d_primes;
     bp.magic = ctx->d_magic;
-    bp.xfirst = s.xfirst;
-    bp.tile_log2 = cfg.tile_log2;
     bp.pat = ctx->d_pat;
     bp.skip_tab = ctx->d_skip;
     bp.inv_tab = ctx->d_inv;
-    bp.err = s.err;
     const uint64_t root = isqrt64(bp.qmax);
-    const auto &pr = ctx->primes;
     bp.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
-    if (bp.n_all < pr.size() && pr.back() < root) return fail(ctx, GBC_E_ARG, "sieving primes too short");
     bp.i0 = std::min(ctx->i0, bp.n_all);
-    bp.n_mid = std::min(ctx->n_mid, bp.n_all);
-    if (bp.n_mid < bp.i0) bp.n_mid = bp.i0;
+    bp.n_mid = std::max(std::min(ctx->n_mid, bp.n_all), bp.i0);
     bp.i_warp = std::min(std::max(ctx->i_warp, bp.i0), bp.n_mid);
     bp.n_hl = ctx->hl_on ? std::min(std::max(ctx->n_hl, bp.n_mid), bp.n_all) : bp.n_all;
+    bp.bm1 = uint32_t(bp.base % gbk::kSkip1);
+    bp.bm2 = uint32_t(bp.base % gbk::kSkip2);
+}
 
-    s.segs.assign(nseg, gbk::SegParams{});
+// Fills the descriptor prefix arrays and header counts from its runs and
+// segments (img.h->nrun, nseg, runs and segs already set).
+static void finish_desc(const gbc_ctx *ctx, DescImage &img)
+{
+    gbk::BatchHeader &h = *img.h;
+    const uint32_t nrun = h.nrun, nseg = h.nseg;
+    h.tile_items = 0;
+    h.n_mid_max = 0;
+    h.n_mid_min = UINT32_MAX;
+    h.n_hl_max = 0;
+    h.n_hl_min = UINT32_MAX;
+    h.n_all_max = 0;
+    for (uint32_t r = 0; r < nrun; ++r) {
+        const gbk::BatchParams &bp = img.runs[r];
+        img.tile_pref[r] = h.tile_items;
+        h.tile_items += 8 * bp.tiles_pc;
+        h.n_mid_max = std::max(h.n_mid_max, bp.n_mid);
+        h.n_mid_min = std::min(h.n_mid_min, bp.n_mid);
+        h.n_hl_max = std::max(h.n_hl_max, bp.n_hl);
+        h.n_hl_min = std::min(h.n_hl_min, bp.n_hl);
+        h.n_all_max = std::max(h.n_all_max, bp.n_all);
+    }
+    img.tile_pref[nrun] = h.tile_items;
+    if (!nrun) h.n_mid_min = h.n_hl_min = 0;
+    h.chk_vb = h.ver_vb = h.cnt_vb = h.nlow = 0;
+    for (uint32_t i = 0; i < nseg; ++i) {
+        gbk::SegParams &sp = img.segs[i];
+        img.chk_pref[i] = h.chk_vb;
+        img.ver_pref[i] = h.ver_vb;
+        img.cnt_pref[i] = h.cnt_vb;
+        const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+        sp.vbx = gbh::check_vbx(evens, ctx->grids.sm);
+        if (sp.low) ++h.nlow;
+        else if (sp.sampled) h.chk_vb += GBC_NCLASS * sp.vbx;
+        else h.ver_vb += GBC_NCLASS * sp.vbx;
+        h.cnt_vb += gbh::count_ranges(img.runs[sp.run].base, sp, sp.cr);
+    }
+    img.chk_pref[nseg] = h.chk_vb;
+    img.ver_pref[nseg] = h.ver_vb;
+    img.cnt_pref[nseg] = h.cnt_vb;
+}
+
+// Plans a batch into the slot's descriptor image: runs, their maps in the
+// slot's buffer, segments (the reference's prepare_segment_tables, seg30 and
+// count30_limits, src/verifier.cpp:1741-1767, include/check30.hpp:196-210,
+// include/gstats.hpp:272-296).
+static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl, const uint64_t *lim, int nseg)
+{
+    const auto &cfg = ctx->cfg;
+    if (nseg < 1 || uint32_t(nseg) > cfg.max_batch) return fail(ctx, GBC_E_ARG, "nseg outside [1, max_batch]");
     for (int i = 0; i < nseg; ++i) {
-        gbk::SegParams &sp = s.segs[i];
+        const uint64_t a = b[2 * i], e = b[2 * i + 1], l = lim[i];
+        if (l > cfg.limit || l & 1) return fail(ctx, GBC_E_ARG, "limit odd or above the context's limit");
+        if ((a | e) & 1 || a < 4 || e < a || e > l)
+            return fail(ctx, GBC_E_ARG, "segment bounds must be even with 4 <= start <= end <= limit");
+        if (e - a > cfg.segment_even) return fail(ctx, GBC_E_ARG, "segment longer than segment_even");
+    }
+    DescImage &img = s.img;
+    uint32_t nrun = 0;
+    uint64_t map_off = 0, xf_off = 0;
+    for (int i = 0; i < nseg;) {
+        int j = i + 1;
+        while (j < nseg && b[2 * j] == b[2 * j - 1] + 2) ++j;
+        if (nrun == cfg.max_runs) return fail(ctx, GBC_E_ARG, "more runs than max_runs");
+        gbk::BatchParams &bp = img.runs[nrun];
+        bp = gbk::BatchParams{};
+        plan_run(ctx, bp, b[2 * i], b[2 * j - 1]);
+        const uint64_t words = uint64_t(8) * bp.wpc;
+        if (map_off + words > s.map_words) return fail(ctx, GBC_E_ARG, "batch wider than the slot's class map");
+        bp.map = s.map + map_off;
+        bp.xfirst = s.xfirst + xf_off;
+        bp.err = s.err;
+        map_off += words;
+        xf_off += uint64_t(8) * bp.n_mid;
+        for (int k = i; k < j; ++k) img.segs[k].run = nrun;
+        ++nrun;
+        i = j;
+    }
+    for (int i = 0; i < nseg; ++i) {
+        gbk::SegParams &sp = img.segs[i];
+        const uint32_t run = sp.run;
+        sp = gbk::SegParams{};
+        sp.run = run;
+        const uint64_t limit = lim[i];
         sp.seg_start = b[2 * i];
         sp.seg_end = b[2 * i + 1];
         sp.flags = fl ? fl[i] : 0;
@@ -471,6 +644,9 @@ int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl,
         sp.pend = s.pend + size_t(i) * s.pend_cap;
         sp.pend_cap = s.pend_cap;
     }
+    img.h->nrun = nrun;
+    img.h->nseg = uint32_t(nseg);
+    finish_desc(ctx, img);
     return GBC_OK;
 }
 
@@ -479,12 +655,17 @@ int gbh_plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *fl,
 // 30 i + u_k), sieved by the batch kernels themselves in chunks and
 // rewritten to bytes (the reference's mt_build, src/verifier.cpp:1444-1508,
 // goldbach.cl:3181-3242). Rebuilt only when a batch needs multipliers
-// outside it; both slots are drained first (they read the table).
+// outside it; every slot is drained first (they read the table).
 static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
 {
     if (ctx->mtab && ctx->mtab_m0 <= need0 && need1 <= ctx->mtab_m1) return GBC_OK;
     const auto t0 = std::chrono::steady_clock::now();
     for (auto &s : ctx->slot) CK(cudaStreamSynchronize(s.st));
+    if (ctx->mtab) {
+        // keep covering what the old table covered
+        need0 = std::min(need0, ctx->mtab_m0);
+        need1 = std::max(need1, ctx->mtab_m1);
+    }
     const uint64_t cap_bytes = uint64_t(ctx->cfg.mtab_max_gb) * 1000000000ull;
     // headroom for the batches that follow (a slice moves need1 by ~1e-4 per batch)
     uint64_t lo = need0 - need0 / 64, hi = need1 + need1 / 64 + (1u << 20);
@@ -496,51 +677,76 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
     const uint64_t nbytes = ((hi - lo) / 30 + 1 + 31) / 32 * 32;
     if (nbytes > cap_bytes) return fail(ctx, GBC_E_ARG, "prime-multiplier table above its HBM budget");
     hi = lo + 30 * nbytes - 1;
-    cudaFree(ctx->mtab);
+    if (ctx->mtab) {
+        cudaFree(ctx->mtab);
+        ctx->device_bytes -= ctx->mtab_bytes + 64;
+    }
     ctx->mtab = nullptr;
-    CK(cudaMalloc(&ctx->mtab, nbytes + 64));
-    // sieve [lo, hi] in chunks through a temporary class map
-    const uint32_t tb = 1u << ctx->cfg.tile_log2, tw = tb / 32;
+    ctx->mtab_bytes = 0;
+    CK(dev_alloc(ctx, &ctx->mtab, nbytes + 64));
+    ctx->mtab_bytes = nbytes;
+    // sieve [lo, hi] in chunks through a temporary class map, each chunk a
+    // one-run batch of its own descriptor (all uploaded before the first launch)
+    const uint32_t tb = 1u << ctx->cfg.tile_log2;
     const uint64_t chunk = uint64_t(1) << 28;  // blocks (bytes) per chunk, a multiple of 32
-    const uint64_t tiles = (chunk + 64 + tb - 1) / tb;
+    const uint64_t nchunk = (nbytes + chunk - 1) / chunk;
+    const uint64_t wpc = align_up(run_wpc(chunk), tb / 32);
+    const DescLayout lay(1, 1);
+    std::vector<uint8_t> host(lay.bytes * nchunk, 0);
     uint32_t *tmp = nullptr, *xf = nullptr;
-    CK(cudaMalloc(&tmp, size_t(8) * tiles * tw * 4 + kMapPadBytes));
+    uint8_t *ddev = nullptr;
+    CK(cudaMalloc(&tmp, size_t(8) * wpc * 4 + kMapPadBytes));
     CK(cudaMalloc(&xf, std::max<size_t>(size_t(8) * ctx->n_mid * 4, 4)));
-    cudaStream_t st = ctx->slot[0].st;
+    CK(cudaMalloc(&ddev, host.size()));
     const auto &pr = ctx->primes;
-    for (uint64_t off = 0; off < nbytes; off += chunk) {
-        gbk::BatchParams b{};
-        b.base = lo + 30 * off;
-        b.nblk = uint32_t(std::min(chunk, nbytes - off));
-        b.qmax = b.base + 30ull * b.nblk;
-        b.tiles_pc = uint32_t((b.nblk + 64 + tb - 1) / tb);
-        b.wpc = b.tiles_pc * tw;
-        b.map = tmp;
-        b.primes = ctx->d_primes;
-        b.magic = ctx->d_magic;
-        b.xfirst = xf;
-        b.tile_log2 = ctx->cfg.tile_log2;
-        b.pat = ctx->d_pat;
-        b.skip_tab = ctx->d_skip;
-        b.inv_tab = ctx->d_inv;
-        b.err = ctx->slot[0].err;
-        uint64_t root = uint64_t(std::sqrt(double(b.qmax)));
-        while (root * root > b.qmax) --root;
-        while ((root + 1) * (root + 1) <= b.qmax) ++root;
-        b.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
-        b.i0 = std::min(ctx->i0, b.n_all);
-        b.n_mid = std::max(std::min(ctx->n_mid, b.n_all), b.i0);
-        b.i_warp = std::min(std::max(ctx->i_warp, b.i0), b.n_mid);
-        b.n_hl = b.n_all;
-        gbh::launch_xfirst(b, st);
-        gbh::launch_tile(b, ctx->gi, st);
-        gbh::launch_large(b, ctx->cfg.large_pass_mb, st);
-        gbh::launch_wheel_bytes(b, ctx->mtab + off / 4, st);
+    std::vector<gbk::BatchParams> runs(nchunk);
+    for (uint64_t c = 0; c < nchunk; ++c) {
+        DescImage img;
+        img.bind(host.data() + c * lay.bytes, lay);
+        gbk::BatchParams &bb = img.runs[0];
+        const uint64_t off = c * chunk;
+        bb.base = lo + 30 * off;
+        bb.nblk = uint32_t(std::min(chunk, nbytes - off));
+        bb.qmax = bb.base + 30ull * bb.nblk;
+        bb.wpc = uint32_t(wpc);
+        bb.tiles_pc = uint32_t(wpc * 32 / tb);
+        bb.tile_log2 = ctx->cfg.tile_log2;
+        bb.map = tmp;
+        bb.primes = ctx->d_primes;
+        bb.magic = ctx->d_magic;
+        bb.xfirst = xf;
+        bb.pat = ctx->d_pat;
+        bb.skip_tab = ctx->d_skip;
+        bb.inv_tab = ctx->d_inv;
+        bb.err = ctx->slot[0].err;
+        const uint64_t root = isqrt64(bb.qmax);
+        bb.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
+        bb.i0 = std::min(ctx->i0, bb.n_all);
+        bb.n_mid = std::max(std::min(ctx->n_mid, bb.n_all), bb.i0);
+        bb.i_warp = std::min(std::max(ctx->i_warp, bb.i0), bb.n_mid);
+        bb.n_hl = bb.n_all;
+        bb.bm1 = uint32_t(bb.base % gbk::kSkip1);
+        bb.bm2 = uint32_t(bb.base % gbk::kSkip2);
+        img.h->nrun = 1;
+        img.h->nseg = 0;
+        finish_desc(ctx, img);
+        runs[c] = bb;
+    }
+    cudaStream_t st = ctx->slot[0].st;
+    CK(cudaMemcpy(ddev, host.data(), host.size(), cudaMemcpyHostToDevice));
+    for (uint64_t c = 0; c < nchunk; ++c) {
+        const gbk::BatchDesc d = lay.device(ddev + c * lay.bytes);
+        gbh::launch_xfirst(d, ctx->grids, st);
+        gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, ctx->grids, st);
+        gbh::launch_large(d, ctx->grids, st);
+        gbh::launch_wheel_bytes(runs[c], ctx->mtab + c * chunk / 4, st);
+        ctx->launches += 4;
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     cudaFree(tmp);
     cudaFree(xf);
+    cudaFree(ddev);
     ctx->mtab_m0 = lo;
     ctx->mtab_m1 = hi;
     ctx->mtab_builds += 1;
@@ -548,73 +754,208 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
     return GBC_OK;
 }
 
+// multipliers [need0, need1] the hit-listed primes of a set of runs need
+// (need0 > need1: none)
+static void mtab_need(const gbc_ctx *ctx, const gbk::BatchParams *runs, uint32_t nrun, uint64_t &need0,
+                      uint64_t &need1)
+{
+    need0 = UINT64_MAX;
+    need1 = 0;
+    for (uint32_t r = 0; r < nrun; ++r) {
+        const gbk::BatchParams &bp = runs[r];
+        if (bp.n_hl >= bp.n_all) continue;
+        const uint64_t q1 = bp.base + 30ull * bp.nblk - 1;
+        need0 = std::min(need0, bp.base / ctx->primes[bp.n_all - 1]);
+        need1 = std::max(need1, q1 / ctx->primes[bp.n_hl]);
+    }
+}
+
+extern "C" int gbc_prepare(gbc_ctx *ctx, uint64_t lo, uint64_t hi)
+{
+    if (!ctx || lo > hi || hi > ctx->cfg.limit) return fail(ctx, GBC_E_ARG, "need lo <= hi <= limit");
+    if (!ctx->hl_on) return GBC_OK;
+    // a run inside [lo, hi] has q in [base(lo), hi + 3 + 29] and sieving
+    // primes up to sqrt(hi + 3): its hit-listed primes (from p_hl on) need
+    // multipliers in [base(lo) / p_max, (hi + 32) / p_hl]
+    const auto &pr = ctx->primes;
+    const uint64_t qmax = hi + 3;
+    const uint32_t n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), isqrt64(qmax)) - pr.begin());
+    if (ctx->n_hl >= n_all) return GBC_OK;  // no hit-listed prime reaches hi
+    const uint64_t s0 = std::max<uint64_t>(lo, 4);
+    const uint64_t base = (s0 > GBC_MAX_CAND + 30 ? s0 - GBC_MAX_CAND : 0) / 30 * 30;
+    return ensure_mtab(ctx, base / pr[n_all - 1], (qmax + 29) / pr[ctx->n_hl]);
+}
+
+// The pipeline of one batch on the slot's stream (the same calls are
+// captured into the slot's graph): descriptor upload, result init, first
+// bits, tiles | large primes, hit lists | checker | counts.
+static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
+{
+    cudaStream_t st = s.st;
+    const unsigned rec = capture ? cudaEventRecordExternal : cudaEventRecordDefault;
+    const gbk::BatchDesc &d = s.dd;
+    const gbh::Grids &g = ctx->grids;
+    CK(cudaMemcpyAsync(s.desc_dev, s.desc_host, ctx->layout.bytes, cudaMemcpyHostToDevice, st));
+    gbh::launch_init(d, g, st);
+    gbh::launch_xfirst(d, g, st);
+    gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, g, st);
+    CK(cudaEventRecordWithFlags(s.ev[1], st, rec));
+    gbh::launch_large(d, g, st);
+    gbh::launch_hitlist(d, g, st);
+    CK(cudaEventRecordWithFlags(s.ev[2], st, rec));
+    gbh::launch_check(d, ctx->ct, g, st);
+    gbh::launch_verify(d, ctx->vt, g, st);
+    gbh::launch_retry(d, ctx->cfg.ridge_min, g, st);
+    CK(cudaEventRecordWithFlags(s.ev[3], st, rec));
+    gbh::launch_count(d, g, st);
+    CK(cudaEventRecordWithFlags(s.ev[4], st, rec));
+    return GBC_OK;
+}
+
+constexpr int kPipelineKernels = 11;
+
+static int capture_slot(gbc_ctx *ctx, Slot &s)
+{
+    CK(cudaStreamBeginCapture(s.st, cudaStreamCaptureModeThreadLocal));
+    const int r = issue_pipeline(ctx, s, true);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s.st, &graph);
+    if (r) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+    }
+    if (e != cudaSuccess) return fail(ctx, GBC_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    const cudaError_t e2 = cudaGraphInstantiate(&s.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e2 != cudaSuccess) {
+        s.exec = nullptr;
+        return fail(ctx, GBC_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e2));
+    }
+    return GBC_OK;
+}
+
+// Map self-check (the reference's enqueue_bucket_verify + map_compare,
+// src/verifier.cpp:2057-2112): the batch's maps sieved again without hit
+// lists (every prime above p_mid by the read-before-mark kernel) into a
+// scratch buffer, then compared word by word; a mismatch sets an error flag.
+static int issue_selfcheck(gbc_ctx *ctx, Slot &s)
+{
+    if (!s.chk_map) {
+        CK(dev_alloc(ctx, &s.chk_map, s.map_words * 4 + kMapPadBytes));
+        CK(cudaMemset(s.chk_map, 0, s.map_words * 4 + kMapPadBytes));
+        CK(cudaMallocHost(&s.chk_desc_host, ctx->layout.bytes));
+        CK(dev_alloc(ctx, &s.chk_desc_dev, ctx->layout.bytes));
+        CK(dev_alloc(ctx, &s.chk_count, 4));
+        s.chk_img.bind(s.chk_desc_host, ctx->layout);
+        s.chk_dd = ctx->layout.device(s.chk_desc_dev);
+    }
+    std::memcpy(s.chk_desc_host, s.desc_host, ctx->layout.bytes);
+    DescImage &ci = s.chk_img;
+    for (uint32_t r = 0; r < ci.h->nrun; ++r) {
+        gbk::BatchParams &bp = ci.runs[r];
+        bp.map = s.chk_map + (bp.map - s.map);
+        bp.n_hl = bp.n_all;
+    }
+    ci.h->n_hl_max = ci.h->n_all_max;
+    ci.h->n_hl_min = ci.h->n_all_max;
+    ci.h->nseg = 0;  // no checker work
+    cudaStream_t st = s.st;
+    CK(cudaMemcpyAsync(s.chk_desc_dev, s.chk_desc_host, ctx->layout.bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s.chk_count, 0, 4, st));
+    gbh::launch_tile(s.chk_dd, ctx->gi, ctx->cfg.tile_log2, ctx->grids, st);
+    gbh::launch_large(s.chk_dd, ctx->grids, st);
+    gbh::launch_map_compare(s.dd, s.chk_dd, s.chk_count, ctx->grids, st);
+    ctx->launches += 3;
+    ctx->selfchecks += 1;
+    return GBC_OK;
+}
+
+static int enqueue_planned(gbc_ctx *ctx, Slot &s)
+{
+    const DescImage &img = s.img;
+    uint64_t need0, need1;
+    mtab_need(ctx, img.runs, img.h->nrun, need0, need1);
+    const bool hl = need0 <= need1;
+    if (hl) {
+        if (int r = ensure_mtab(ctx, need0, need1)) return r;
+        for (uint32_t r = 0; r < img.h->nrun; ++r) {
+            img.runs[r].mtab = ctx->mtab;
+            img.runs[r].m0 = ctx->mtab_m0;
+            img.runs[r].m1 = ctx->mtab_m1;
+        }
+    }
+    cudaStream_t st = s.st;
+    CK(cudaEventRecord(s.ev[0], st));
+    if (ctx->cfg.launch_mode == 2) {
+        if (int r = issue_pipeline(ctx, s, false)) return r;
+    } else {
+        if (!s.exec)
+            if (int r = capture_slot(ctx, s)) return r;
+        CK(cudaGraphLaunch(s.exec, st));
+        ctx->graph_replays += 1;
+    }
+    ctx->launches += kPipelineKernels;
+    s.did_selfcheck = false;
+    if (hl) {
+        ctx->hl_batches += 1;
+        const uint32_t every = ctx->cfg.selfcheck_every;
+        if (every && ctx->hl_batches % every == 0) {
+            if (int r = issue_selfcheck(ctx, s)) return r;
+            s.did_selfcheck = true;
+        }
+    }
+    CK(cudaEventRecord(s.ev[5], st));
+    CK(cudaGetLastError());
+    s.nseg = int(img.h->nseg);
+    s.nrun = int(img.h->nrun);
+    s.pending = true;
+    ctx->batches += 1;
+    return GBC_OK;
+}
+
+extern "C" int gbc_enqueue_segments(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags,
+                                    const uint64_t *seg_limits, int nseg)
+{
+    if (bad_slot(ctx, slot) || !seg_bounds || !seg_limits)
+        return fail(ctx, GBC_E_ARG, "bad context, slot, bounds or limits");
+    Slot &s = ctx->slot[slot];
+    if (s.pending) return fail(ctx, GBC_E_STATE, "slot already holds an uncollected batch");
+    if (int r = plan_batch(ctx, s, seg_bounds, seg_flags, seg_limits, nseg)) return r;
+    return enqueue_planned(ctx, s);
+}
+
 extern "C" int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags,
                                  int nseg, uint64_t limit)
 {
-    if (!ctx || slot < 0 || slot > 1 || !seg_bounds) return fail(ctx, GBC_E_ARG, "bad context, slot or bounds");
+    if (bad_slot(ctx, slot) || !seg_bounds) return fail(ctx, GBC_E_ARG, "bad context, slot or bounds");
+    if (nseg < 1 || uint32_t(nseg) > ctx->cfg.max_batch) return fail(ctx, GBC_E_ARG, "nseg outside [1, max_batch]");
+    for (int i = 1; i < nseg; ++i)
+        if (seg_bounds[2 * i] != seg_bounds[2 * i - 1] + 2) return fail(ctx, GBC_E_ARG, "segments must be consecutive");
+    std::vector<uint64_t> lim(size_t(nseg), limit);
+    return gbc_enqueue_segments(ctx, slot, seg_bounds, seg_flags, lim.data(), nseg);
+}
+
+extern "C" int gbc_poll(gbc_ctx *ctx, int slot)
+{
+    if (bad_slot(ctx, slot)) return fail(ctx, GBC_E_ARG, "bad context or slot");
     Slot &s = ctx->slot[slot];
-    if (s.pending) return fail(ctx, GBC_E_STATE, "slot already holds an uncollected batch");
-    gbk::BatchParams bp{};
-    if (int r = gbh_plan_batch(ctx, s, seg_bounds, seg_flags, nseg, limit, bp)) return r;
-    if (bp.n_hl < bp.n_all) {
-        // multipliers of the batch's q range for its hit-listed primes
-        const uint64_t q1 = bp.base + 30ull * bp.nblk - 1;
-        const uint64_t need0 = bp.base / ctx->primes[bp.n_all - 1];
-        const uint64_t need1 = q1 / ctx->primes[bp.n_hl];
-        if (int r = ensure_mtab(ctx, need0, need1)) return r;
-        bp.mtab = ctx->mtab;
-        bp.m0 = ctx->mtab_m0;
-        bp.m1 = ctx->mtab_m1;
-    }
-    s.bp = bp;
-    s.nseg = nseg;
-    cudaStream_t st = s.st;
-    CK(cudaMemsetAsync(s.err, 0, 4, st));
-    CK(cudaMemsetAsync(s.res, 0, size_t(nseg) * sizeof(gbc_segment_result), st));
-    for (int i = 0; i < nseg; ++i) {
-        CK(cudaMemsetAsync(s.res[i].first, 0xFF, sizeof(s.res[i].first), st));
-        CK(cudaMemsetAsync(&s.res[i].first_prime, 0xFF, sizeof(uint64_t), st));
-    }
-    CK(cudaEventRecord(s.ev[0], st));
-    gbh::launch_xfirst(bp, st);
-    gbh::launch_tile(bp, ctx->gi, st);
-    ctx->launches += 2;
-    CK(cudaEventRecord(s.ev[1], st));
-    ctx->launches += gbh::launch_large(bp, ctx->cfg.large_pass_mb, st);
-    ctx->launches += gbh::launch_hitlist(bp, ctx->cfg.hl_pass_mb, st);
-    CK(cudaEventRecord(s.ev[2], st));
-    for (int i = 0; i < nseg; ++i) {
-        if (s.segs[i].sampled) {
-            gbh::launch_check(bp, s.segs[i], ctx->ct, ctx->sm_count, st);
-            ctx->launches += 1;
-        } else {
-            gbh::launch_verify(bp, s.segs[i], ctx->vt, ctx->sm_count, st);
-            ctx->launches += 2;
-        }
-        gbh::launch_retry(s.segs[i], ctx->cfg.ridge_min, st);
-        ctx->launches += 1;
-    }
-    CK(cudaEventRecord(s.ev[3], st));
-    for (int i = 0; i < nseg; ++i) {
-        gbh::launch_count(bp, s.segs[i], st);
-        ctx->launches += 1;
-    }
-    CK(cudaEventRecord(s.ev[4], st));
-    CK(cudaGetLastError());
-    s.pending = true;
-    return GBC_OK;
+    if (!s.pending) return 0;
+    const cudaError_t q = cudaEventQuery(s.ev[5]);
+    if (q == cudaSuccess) return 1;
+    if (q == cudaErrorNotReady) return 0;
+    return fail(ctx, GBC_E_CUDA, std::string("batch: ") + cudaGetErrorString(q));
 }
 
 extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int nseg, gbc_batch_times *times,
                            int timeout_ms)
 {
-    if (!ctx || slot < 0 || slot > 1 || !out) return fail(ctx, GBC_E_ARG, "bad context, slot or output");
+    if (bad_slot(ctx, slot) || !out) return fail(ctx, GBC_E_ARG, "bad context, slot or output");
     Slot &s = ctx->slot[slot];
     if (!s.pending) return fail(ctx, GBC_E_STATE, "collect without an enqueued batch");
     if (nseg != s.nseg) return fail(ctx, GBC_E_ARG, "nseg differs from the enqueued batch");
     const auto t0 = std::chrono::steady_clock::now();
     for (;;) {
-        const cudaError_t q = cudaEventQuery(s.ev[4]);
+        const cudaError_t q = cudaEventQuery(s.ev[5]);
         if (q == cudaSuccess) break;
         if (q != cudaErrorNotReady) return fail(ctx, GBC_E_CUDA, std::string("batch: ") + cudaGetErrorString(q));
         if (timeout_ms >= 0 &&
@@ -623,30 +964,37 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
         std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     CK(cudaMemcpy(out, s.res, size_t(nseg) * sizeof(gbc_segment_result), cudaMemcpyDeviceToHost));
-    uint32_t berr = 0;
+    uint32_t berr = 0, bad_words = 0;
     CK(cudaMemcpy(&berr, s.err, 4, cudaMemcpyDeviceToHost));
+    if (s.did_selfcheck) CK(cudaMemcpy(&bad_words, s.chk_count, 4, cudaMemcpyDeviceToHost));
     s.pending = false;
     if (berr) {
-        char m[96];
-        std::snprintf(m, sizeof m, "device error flags 0x%x in the batch's sieve", berr);
+        char m[128];
+        if (berr & gbk::kErrSelfCheck)
+            std::snprintf(m, sizeof m, "map self-check: %u class-map words differ from the rebuild without hit lists",
+                          bad_words);
+        else std::snprintf(m, sizeof m, "device error flags 0x%x in the batch's sieve", berr);
         return fail(ctx, GBC_E_DEVICE, m);
     }
     if (times) {
-        float a = 0, b = 0, c = 0, d = 0;
+        float a = 0, b = 0, c = 0, d = 0, e = 0;
         cudaEventElapsedTime(&a, s.ev[0], s.ev[1]);
         cudaEventElapsedTime(&b, s.ev[1], s.ev[2]);
         cudaEventElapsedTime(&c, s.ev[2], s.ev[3]);
         cudaEventElapsedTime(&d, s.ev[3], s.ev[4]);
+        if (s.did_selfcheck) cudaEventElapsedTime(&e, s.ev[4], s.ev[5]);
         times->ms_setup = 0;
         times->ms_tile = a;
         times->ms_large = b;
         times->ms_check = c;
         times->ms_count = d;
-        times->ms_total = a + b + c + d;
+        times->ms_selfcheck = e;
+        times->ms_total = a + b + c + d + e;
+        times->runs = uint32_t(s.nrun);
     }
     for (int i = 0; i < nseg; ++i) {
         gbc_segment_result &r = out[i];
-        const gbk::SegParams &sp = s.segs[i];
+        const gbk::SegParams &sp = s.img.segs[i];
         r.seg_start = sp.seg_start;
         r.seg_end = sp.seg_end;
         r.evens = (sp.seg_end - sp.seg_start) / 2 + 1;
@@ -670,37 +1018,45 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
 
 extern "C" int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint64_t evens)
 {
-    if (!ctx || slot < 0 || slot > 1 || !out) return fail(ctx, GBC_E_ARG, "bad arguments");
+    if (bad_slot(ctx, slot) || !out) return fail(ctx, GBC_E_ARG, "bad arguments");
     Slot &s = ctx->slot[slot];
     if (!s.pn) return fail(ctx, GBC_E_STATE, "context made without want_pn");
     if (seg < 0 || seg >= s.nseg) return fail(ctx, GBC_E_ARG, "segment index");
-    const gbk::SegParams &sp = s.segs[seg];
+    const gbk::SegParams &sp = s.img.segs[seg];
     if (evens != (sp.seg_end - sp.seg_start) / 2 + 1) return fail(ctx, GBC_E_ARG, "evens differs from the segment");
     CK(cudaMemcpyAsync(out, s.pn + size_t(seg) * s.pn_stride, evens * 2, cudaMemcpyDeviceToHost, s.st));
     CK(cudaStreamSynchronize(s.st));
     return GBC_OK;
 }
 
-extern "C" int gbc_map_info(gbc_ctx *ctx, int slot, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
-                            uint64_t out_words)
+extern "C" int gbc_map_run(gbc_ctx *ctx, int slot, int run, uint64_t *base, uint32_t *nblk, uint32_t *wpc,
+                           uint32_t *out, uint64_t out_words)
 {
-    if (!ctx || slot < 0 || slot > 1) return fail(ctx, GBC_E_ARG, "bad context or slot");
+    if (bad_slot(ctx, slot)) return fail(ctx, GBC_E_ARG, "bad context or slot");
     Slot &s = ctx->slot[slot];
     if (s.pending) return fail(ctx, GBC_E_STATE, "the slot's batch is not collected yet");
     if (!s.nseg) return fail(ctx, GBC_E_STATE, "no batch on this slot yet");
-    if (base) *base = s.bp.base;
-    if (nblk) *nblk = s.bp.nblk;
-    if (wpc) *wpc = s.bp.wpc;
+    if (run < 0 || run >= s.nrun) return fail(ctx, GBC_E_ARG, "run index");
+    const gbk::BatchParams &bp = s.img.runs[run];
+    if (base) *base = bp.base;
+    if (nblk) *nblk = bp.nblk;
+    if (wpc) *wpc = bp.wpc;
     if (out) {
-        if (out_words < uint64_t(8) * s.bp.wpc) return fail(ctx, GBC_E_ARG, "output smaller than 8 * wpc words");
-        CK(cudaMemcpy(out, s.map, size_t(8) * s.bp.wpc * 4, cudaMemcpyDeviceToHost));
+        if (out_words < uint64_t(8) * bp.wpc) return fail(ctx, GBC_E_ARG, "output smaller than 8 * wpc words");
+        CK(cudaMemcpy(out, bp.map, size_t(8) * bp.wpc * 4, cudaMemcpyDeviceToHost));
     }
     return GBC_OK;
 }
 
+extern "C" int gbc_map_info(gbc_ctx *ctx, int slot, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
+                            uint64_t out_words)
+{
+    return gbc_map_run(ctx, slot, 0, base, nblk, wpc, out, out_words);
+}
+
 extern "C" const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg)
 {
-    if (!ctx || slot < 0 || slot > 1) return nullptr;
+    if (bad_slot(ctx, slot)) return nullptr;
     Slot &s = ctx->slot[slot];
     if (!s.pn || seg < 0 || uint32_t(seg) >= ctx->cfg.max_batch) return nullptr;
     return s.pn + size_t(seg) * s.pn_stride;

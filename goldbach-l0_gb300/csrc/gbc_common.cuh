@@ -1,13 +1,16 @@
 // gbc_common.cuh -- types and device helpers shared by the sieve, checker
 // and count kernels of the dense Goldbach verify path.
 //
-// Layout of a batch's class map (HBM-resident, one per slot):
+// Layout of a run's class map (HBM-resident; a run is a maximal set of
+// consecutive segments of a batch, and each run has its own map in the
+// slot's map buffer):
 //   8 class arrays, one per residue u_k in {1, 7, 11, 13, 17, 19, 23, 29}
 //   (mod 30); bit t of array k <-> q = base + 30 t + u_k, base a multiple
-//   of 30. Array k holds words [k * wpc, (k + 1) * wpc) of u32; bit t is
-//   bit (t & 31) of word t >> 5. A set bit means q is prime. The layout
-//   keeps the reference's mod-30 class map (include/host_math.hpp:63-78)
-//   with the class phases fixed to 0 by aligning base to 30.
+//   of 30. Array k holds words [k * wpc, (k + 1) * wpc) of u32 from the
+//   run's map pointer; bit t is bit (t & 31) of word t >> 5. A set bit means
+//   q is prime. The layout keeps the reference's mod-30 class map
+//   (include/host_math.hpp:63-78) with the class phases fixed to 0 by
+//   aligning base to 30.
 #pragma once
 #include <cstdint>
 
@@ -81,6 +84,7 @@ struct BatchParams {
     uint32_t n_hl;            // first hit-listed prime (n_all: none)
     const uint32_t *mtab;     // bit k of byte i <-> m = m0 + 30 i + u_k is prime
     uint64_t m0, m1;          // the table covers m in [m0, m1]
+    uint32_t bm1, bm2;        // base mod 1001 and mod 7429
 };
 
 struct GroupInfo {
@@ -88,6 +92,16 @@ struct GroupInfo {
     uint32_t off[kNumGroups];     // word offset of the group's pattern
     uint32_t inv30[kNumGroups];   // 30^-1 mod P
     uint32_t words;               // total pattern words
+};
+
+// Bit and word ranges of one segment for the count kernel (per class k:
+// bits [lo, hi] of the ranges).
+struct CountRanges {
+    uint32_t hash_t[8][2];  // hashed q range
+    uint32_t cnt_t[8][2];   // counted primes
+    uint32_t twin_t[8][2];  // counted lower twin primes
+    uint32_t w_lo, w_hi;    // words covering the hashed range
+    uint32_t in_lo, in_hi;  // words inside all three ranges for every class (in_hi < in_lo: none)
 };
 
 // One segment of a batch, as the checker and count kernels see it.
@@ -103,7 +117,66 @@ struct SegParams {
     uint32_t sampled;             // 1: exact p(n) of every even; 0: funnel verify + exact tail
     uint2 *pend;                  // phase-A misses: (class r / 2 << 27 | word, unresolved bits)
     uint32_t pend_cap;
+    uint32_t run;                 // the segment's run (class map) in the batch
+    uint32_t vbx;                 // checker CTAs per class of the segment
+    uint32_t pad;
+    CountRanges cr;
 };
+
+// A batch as the persistent kernels see it: a header of counts and the
+// per-run and per-segment parameter arrays, all in device memory and
+// rewritten for every batch by one host-to-device copy. The pointers are
+// fixed for a slot, so one CUDA graph of the whole pipeline, captured once,
+// replays every batch.
+struct BatchHeader {
+    uint32_t nrun, nseg;
+    uint32_t tile_items;           // (run, class, tile) items of the tile kernel
+    uint32_t n_mid_max;            // first bits: primes [i0, n_mid_max)
+    uint32_t n_mid_min, n_hl_max;  // large primes: [n_mid_min, n_hl_max)
+    uint32_t n_hl_min, n_all_max;  // hit-listed primes: [n_hl_min, n_all_max)
+    uint32_t chk_vb, ver_vb, cnt_vb; // virtual CTAs of k_check, k_verify, k_count
+    uint32_t nlow;                 // segments that need the generic low checker
+    uint32_t pad[3];
+    // work counters of the persistent kernels (CTAs take their next item
+    // with an atomic add); zero in the host image, so every batch's
+    // descriptor copy resets them
+    uint32_t work[4];
+};
+
+constexpr int kWorkTile = 0, kWorkCheck = 1, kWorkVerify = 2, kWorkCount = 3;
+
+struct BatchDesc {
+    const BatchHeader *h;
+    uint32_t *work;               // h->work, writable
+    const BatchParams *runs;
+    const SegParams *segs;
+    const uint32_t *tile_pref;    // nrun + 1: tile items before run r
+    const uint32_t *chk_pref;     // nseg + 1: virtual CTAs of k_check before segment s
+    const uint32_t *ver_pref;     // nseg + 1: the same for k_verify
+    const uint32_t *cnt_pref;     // nseg + 1: the same for k_count
+};
+
+// The next item of a persistent kernel's work counter for the whole CTA
+// (every thread gets the same value; the caller's loop body must end with
+// a __syncthreads before the next call).
+__device__ __forceinline__ uint32_t next_item(uint32_t *counter, uint32_t *s_slot)
+{
+    if (threadIdx.x == 0) *s_slot = atomicAdd(counter, 1u);
+    __syncthreads();
+    return *s_slot;
+}
+
+// the last index i in [0, n) with pref[i] <= x (pref ascending, pref[0] = 0)
+__device__ __forceinline__ uint32_t find_prefix(const uint32_t *pref, uint32_t n, uint32_t x)
+{
+    uint32_t lo = 0, hi = n;  // pref[lo] <= x < pref[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(pref + mid) <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 // Candidate tables of the checker (uploaded once per context).
 struct CheckTables {
@@ -134,6 +207,7 @@ constexpr uint32_t kErrRetry = 1u << 4;
 constexpr uint32_t kErrTable = 1u << 5;   // a multiplier outside the prime-multiplier table
 constexpr uint32_t kErrPendOverflow = 1u << 6;
 constexpr uint32_t kErrRidgeOverflow = 1u << 7;
+constexpr uint32_t kErrSelfCheck = 1u << 8;  // the map self-check found differing words
 
 // ---------------------------------------------------------------------------
 // 64-bit Miller-Rabin in Montgomery form (the GPU retry of evens without a
@@ -201,17 +275,35 @@ __device__ inline bool is_prime_u64_dev(uint64_t n)
 
 }  // namespace gbk
 
-// Host-side launchers (defined in the kernel translation units).
+// Host-side launchers (defined in the kernel translation units). Grids are
+// fixed per context (persistent kernels looping over the batch's items), so
+// the same launches serve every batch and can be captured into a graph.
 namespace gbh {
-void launch_xfirst(const gbk::BatchParams &bp, cudaStream_t st);
-void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st);
-int launch_large(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st);
-int launch_hitlist(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st);
+struct Grids {
+    int sm = 1;                  // multiprocessors
+    int check = 1, verify = 1, count = 1;  // resident CTAs of those kernels
+    int max_seg = 1;             // segments a batch can hold
+};
+void launch_init(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
+                 cudaStream_t st);
+void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st);
+void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st);
+void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st);
+void launch_count(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_map_compare(const gbk::BatchDesc &a, const gbk::BatchDesc &b, uint32_t *count, const Grids &g,
+                        cudaStream_t st);
+void tile_attributes(uint32_t tile_log2, const gbk::GroupInfo &gi);
+void query_check_grids(Grids &g);
+void query_count_grids(Grids &g);
+uint32_t check_vbx(uint64_t evens, int sm);
+// single-run forms (the allocation-free entry point and the table build)
+void launch_xfirst1(const gbk::BatchParams &bp, cudaStream_t st);
+void launch_tile1(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st);
 void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st);
-void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
-                  cudaStream_t st);
-void launch_retry(const gbk::SegParams &sp, uint32_t ridge_min, cudaStream_t st);
-void launch_verify(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::VerifyTables &vt, int sm_count,
-                   cudaStream_t st);
-void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStream_t st);
+// host geometry of the count kernel: CountRanges of a segment on its run's map, and its CTAs
+uint32_t count_ranges(uint64_t base, const gbk::SegParams &sp, gbk::CountRanges &cr);
 }  // namespace gbh

@@ -13,7 +13,13 @@
 // histogram and the first occurrence; evens left without a witness <= 9781
 // go to a list that k_retry settles on the GPU (the reference's CPU
 // fallback cpu_min_goldbach_prime, src/primes.cpp:482-493, moved on device).
+//
+// Every kernel here is persistent: a fixed grid takes the "virtual CTAs"
+// of all segments of the batch (per segment: vbx CTAs per class) from a
+// work counter, each found through the batch descriptor's prefix arrays.
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "gbc_common.cuh"
 
@@ -58,15 +64,15 @@ __device__ __forceinline__ void write_pn(uint16_t *pn, uint32_t idx0, uint32_t j
     }
 }
 
-// One CTA per (chunk column, class r); each warp takes 64 consecutive words
-// (2048 evens) of class r at a time, stages the 8 class-array windows they
-// read (64 words + the candidates' span) in its own shared memory, and tests
-// the class's useful candidates in ascending order: lane l holds words l and
-// l + 32 of the chunk, so every shared-memory read of the warp is 32
-// consecutive words.
-__global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegParams sp, CheckTables ct)
+// Virtual CTA (chunk column bx of vbx, class r) of a sampled segment; each
+// warp takes 64 consecutive words (2048 evens) of class r at a time, stages
+// the 8 class-array windows they read (64 words + the candidates' span) in
+// its own shared memory, and tests the class's useful candidates in
+// ascending order: lane l holds words l and l + 32 of the chunk, so every
+// shared-memory read of the warp is 32 consecutive words.
+__global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTables ct)
 {
-    __shared__ uint32_t s_ent[GBC_NCAND];   // word offset | shift << 8 | class array << 13
+    __shared__ uint32_t s_ent[GBC_NCAND];   // word offset | shift << 16
     __shared__ uint16_t s_p[GBC_NCAND];
     __shared__ uint16_t s_ci[GBC_NCAND];
     __shared__ uint32_t s_hist[GBC_NCAND];
@@ -74,198 +80,227 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchParams bp, SegPara
     __shared__ uint32_t s_win[kCheckWarps][8 * kWin];
     __shared__ uint32_t s_dmin, s_dmax;
 
-    const uint32_t cr = blockIdx.y, r = 2 * cr;
-    const uint64_t seg_start = sp.seg_start;
-    const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;  // first even of class r
-    if (n0 > sp.seg_end) return;
-    const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
-    const uint32_t nwords = uint32_t((ecount + 31) / 32);
-    const uint32_t ncand = ct.cnt[cr];
+    __shared__ uint32_t s_vb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t total = d.h->chk_vb, nseg = d.h->nseg;
+    for (;;) {
+        const uint32_t vb = next_item(d.work + kWorkCheck, &s_vb);
+        if (vb >= total) break;
+        const uint32_t si = find_prefix(d.chk_pref, nseg, vb);
+        const SegParams &sp = d.segs[si];
+        const BatchParams &bp = d.runs[sp.run];
+        const uint32_t local = vb - __ldg(d.chk_pref + si);
+        const uint32_t cr = local % GBC_NCLASS, bx = local / GBC_NCLASS, gx = sp.vbx, r = 2 * cr;
+        const uint64_t seg_start = sp.seg_start, base = bp.base;
+        const uint32_t wpc = bp.wpc;
+        const uint32_t *map = bp.map;
+        gbc_segment_result *res = sp.res;
+        uint16_t *pn = sp.pn;
+        const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;  // first even of class r
+        if (n0 > sp.seg_end) {
+            __syncthreads();
+            continue;
+        }
+        const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
+        const uint32_t nwords = uint32_t((ecount + 31) / 32);
+        const uint32_t ncand = ct.cnt[cr];
 
-    if (tid == 0) {
-        s_dmin = kNone;
-        s_dmax = 0;
-    }
-    __syncthreads();
-    // q = n0 + 30 t - p = base + 30 (D + t) + u: D is the bit of the
-    // candidate's window at word 0 of class r
-    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
-        const uint32_t ci = ct.list[ct.off[cr] + c];
-        const uint32_t p = ct.cand[ci];
-        const uint32_t D = uint32_t((n0 - bp.base - p - (r + 30 - p % 30) % 30) / 30);
-        atomicMin(&s_dmin, D);
-        atomicMax(&s_dmax, D);
-    }
-    __syncthreads();
-    const uint32_t dlo = s_dmin & ~31u;                 // staged windows start at word dlo / 32 + J
-    const uint32_t nstage = (s_dmax - dlo) / 32 + 66;   // words per class array (<= kWin)
-    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
-        const uint32_t ci = ct.list[ct.off[cr] + c];
-        const uint32_t p = ct.cand[ci];
-        const uint32_t u = (r + 30 - p % 30) % 30;
-        const uint32_t d = uint32_t((n0 - bp.base - p - u) / 30) - dlo;
-        // word offset of the window in the warp's staging area | shift << 16
-        s_ent[c] = (class_of(u) * kWin + (d >> 5)) | ((d & 31) << 16);
-        s_p[c] = uint16_t(p);
-        s_ci[c] = uint16_t(ci);
-        s_hist[c] = 0;
-        s_first[c] = kNone;
-    }
-    __syncthreads();
+        if (tid == 0) {
+            s_dmin = kNone;
+            s_dmax = 0;
+        }
+        __syncthreads();
+        // q = n0 + 30 t - p = base + 30 (D + t) + u: D is the bit of the
+        // candidate's window at word 0 of class r
+        for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+            const uint32_t ci = ct.list[ct.off[cr] + c];
+            const uint32_t p = ct.cand[ci];
+            const uint32_t D = uint32_t((n0 - base - p - (r + 30 - p % 30) % 30) / 30);
+            atomicMin(&s_dmin, D);
+            atomicMax(&s_dmax, D);
+        }
+        __syncthreads();
+        const uint32_t dlo = s_dmin & ~31u;                 // staged windows start at word dlo / 32 + J
+        const uint32_t nstage = (s_dmax - dlo) / 32 + 66;   // words per class array (<= kWin)
+        for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+            const uint32_t ci = ct.list[ct.off[cr] + c];
+            const uint32_t p = ct.cand[ci];
+            const uint32_t u = (r + 30 - p % 30) % 30;
+            const uint32_t dd = uint32_t((n0 - base - p - u) / 30) - dlo;
+            // word offset of the window in the warp's staging area | shift << 16
+            s_ent[c] = (class_of(u) * kWin + (dd >> 5)) | ((dd & 31) << 16);
+            s_p[c] = uint16_t(p);
+            s_ci[c] = uint16_t(ci);
+            s_hist[c] = 0;
+            s_first[c] = kNone;
+        }
+        __syncthreads();
 
-    const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
-    uint32_t *win = s_win[warp];
-    for (uint32_t ch = blockIdx.x * kCheckWarps + warp; ch * 64 < nwords; ch += gridDim.x * kCheckWarps) {
-        const uint32_t J = ch * 64;
-        // stage the windows: class array k, words dlo / 32 + J + [0, nstage)
-        const uint32_t *src = bp.map + (dlo >> 5) + J;
+        const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
+        uint32_t *win = s_win[warp];
+        for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps) {
+            const uint32_t J = ch * 64;
+            // stage the windows: class array k, words dlo / 32 + J + [0, nstage)
+            const uint32_t *src = map + (dlo >> 5) + J;
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k)
-            for (uint32_t i = lane; i < nstage; i += 32) win[k * kWin + i] = __ldg(src + size_t(k) * bp.wpc + i);
-        __syncwarp();
-        const uint32_t jA = J + lane, jB = J + 32 + lane;
-        uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
-        const uint32_t chunk_min = idx0 + 15u * 32u * J;  // smallest even index of this chunk
-        const uint32_t *wl = win + lane;
-        // records the hits hA / hB of candidate c (uA / uB already updated)
-        auto record = [&](uint32_t c, uint32_t hA, uint32_t hB, uint32_t cnt) {
-            if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
-                const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
-                                         : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
-                const uint32_t mn = __reduce_min_sync(~0u, mine);
-                if (lane == 0) atomicMin(&s_first[c], mn);
+            for (uint32_t k = 0; k < 8; ++k)
+                for (uint32_t i = lane; i < nstage; i += 32) win[k * kWin + i] = __ldg(src + size_t(k) * wpc + i);
+            __syncwarp();
+            const uint32_t jA = J + lane, jB = J + 32 + lane;
+            uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+            const uint32_t chunk_min = idx0 + 15u * 32u * J;  // smallest even index of this chunk
+            const uint32_t *wl = win + lane;
+            // records the hits hA / hB of candidate c (uA / uB already updated)
+            auto record = [&](uint32_t c, uint32_t hA, uint32_t hB, uint32_t cnt) {
+                if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
+                    const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
+                                             : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
+                    const uint32_t mn = __reduce_min_sync(~0u, mine);
+                    if (lane == 0) atomicMin(&s_first[c], mn);
+                }
+                if (lane == 0) atomicAdd(&s_hist[c], cnt);
+                if (pn) {
+                    write_pn(pn, idx0, jA, hA, s_p[c]);
+                    write_pn(pn, idx0, jB, hB, s_p[c]);
+                }
+                if (s_p[c] >= ct.ridge_min) {
+                    for (uint32_t h = hA; h; h &= h - 1u)
+                        append_ridge(res, n0 + 30ull * (32ull * jA + __ffs(h) - 1u), s_p[c]);
+                    for (uint32_t h = hB; h; h &= h - 1u)
+                        append_ridge(res, n0 + 30ull * (32ull * jB + __ffs(h) - 1u), s_p[c]);
+                }
+            };
+            uint32_t c = 0;
+            // two candidates per trip: their window reads are independent; the
+            // second one only tests what the first one left
+            for (; c + 1 < ncand; c += 2) {
+                if (!__any_sync(~0u, uA | uB)) break;
+                const uint32_t e0 = s_ent[c], e1 = s_ent[c + 1];
+                const uint32_t *w0 = wl + (e0 & 0xFFFF), *w1 = wl + (e1 & 0xFFFF);
+                const uint32_t s0 = e0 >> 16, s1 = e1 >> 16;
+                const uint32_t a0 = __funnelshift_r(w0[0], w0[1], s0), b0 = __funnelshift_r(w0[32], w0[33], s0);
+                const uint32_t a1 = __funnelshift_r(w1[0], w1[1], s1), b1 = __funnelshift_r(w1[32], w1[33], s1);
+                const uint32_t hA0 = uA & a0, hB0 = uB & b0;
+                uA ^= hA0;
+                uB ^= hB0;
+                const uint32_t hA1 = uA & a1, hB1 = uB & b1;
+                uA ^= hA1;
+                uB ^= hB1;
+                const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
+                const uint32_t cnt1 = __reduce_add_sync(~0u, __popc(hA1) + __popc(hB1));
+                if (cnt0) record(c, hA0, hB0, cnt0);
+                if (cnt1) record(c + 1, hA1, hB1, cnt1);
             }
-            if (lane == 0) atomicAdd(&s_hist[c], cnt);
-            if (sp.pn) {
-                write_pn(sp.pn, idx0, jA, hA, s_p[c]);
-                write_pn(sp.pn, idx0, jB, hB, s_p[c]);
+            if (c < ncand && __any_sync(~0u, uA | uB)) {
+                const uint32_t e0 = s_ent[c];
+                const uint32_t *w0 = wl + (e0 & 0xFFFF);
+                const uint32_t s0 = e0 >> 16;
+                const uint32_t hA0 = uA & __funnelshift_r(w0[0], w0[1], s0);
+                const uint32_t hB0 = uB & __funnelshift_r(w0[32], w0[33], s0);
+                uA ^= hA0;
+                uB ^= hB0;
+                const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
+                if (cnt0) record(c, hA0, hB0, cnt0);
             }
-            if (s_p[c] >= ct.ridge_min) {
-                for (uint32_t h = hA; h; h &= h - 1u)
-                    append_ridge(sp.res, n0 + 30ull * (32ull * jA + __ffs(h) - 1u), s_p[c]);
-                for (uint32_t h = hB; h; h &= h - 1u)
-                    append_ridge(sp.res, n0 + 30ull * (32ull * jB + __ffs(h) - 1u), s_p[c]);
+            while (uA) {
+                const uint32_t b = __ffs(uA) - 1u;
+                append_leftover(res, n0 + 30ull * (32ull * jA + b));
+                uA &= uA - 1u;
             }
-        };
-        uint32_t c = 0;
-        // two candidates per trip: their window reads are independent; the
-        // second one only tests what the first one left
-        for (; c + 1 < ncand; c += 2) {
-            if (!__any_sync(~0u, uA | uB)) break;
-            const uint32_t e0 = s_ent[c], e1 = s_ent[c + 1];
-            const uint32_t *w0 = wl + (e0 & 0xFFFF), *w1 = wl + (e1 & 0xFFFF);
-            const uint32_t s0 = e0 >> 16, s1 = e1 >> 16;
-            const uint32_t a0 = __funnelshift_r(w0[0], w0[1], s0), b0 = __funnelshift_r(w0[32], w0[33], s0);
-            const uint32_t a1 = __funnelshift_r(w1[0], w1[1], s1), b1 = __funnelshift_r(w1[32], w1[33], s1);
-            const uint32_t hA0 = uA & a0, hB0 = uB & b0;
-            uA ^= hA0;
-            uB ^= hB0;
-            const uint32_t hA1 = uA & a1, hB1 = uB & b1;
-            uA ^= hA1;
-            uB ^= hB1;
-            const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
-            const uint32_t cnt1 = __reduce_add_sync(~0u, __popc(hA1) + __popc(hB1));
-            if (cnt0) record(c, hA0, hB0, cnt0);
-            if (cnt1) record(c + 1, hA1, hB1, cnt1);
+            while (uB) {
+                const uint32_t b = __ffs(uB) - 1u;
+                append_leftover(res, n0 + 30ull * (32ull * jB + b));
+                uB &= uB - 1u;
+            }
+            __syncwarp();
         }
-        if (c < ncand && __any_sync(~0u, uA | uB)) {
-            const uint32_t e0 = s_ent[c];
-            const uint32_t *w0 = wl + (e0 & 0xFFFF);
-            const uint32_t s0 = e0 >> 16;
-            const uint32_t hA0 = uA & __funnelshift_r(w0[0], w0[1], s0);
-            const uint32_t hB0 = uB & __funnelshift_r(w0[32], w0[33], s0);
-            uA ^= hA0;
-            uB ^= hB0;
-            const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
-            if (cnt0) record(c, hA0, hB0, cnt0);
+        __syncthreads();
+        for (uint32_t c = tid; c < ncand; c += blockDim.x) {
+            if (s_hist[c]) atomicAdd(&res->hist[cr][s_ci[c]], s_hist[c]);
+            if (s_first[c] != kNone) atomicMin(&res->first[s_ci[c]], s_first[c]);
         }
-        while (uA) {
-            const uint32_t b = __ffs(uA) - 1u;
-            append_leftover(sp.res, n0 + 30ull * (32ull * jA + b));
-            uA &= uA - 1u;
-        }
-        while (uB) {
-            const uint32_t b = __ffs(uB) - 1u;
-            append_leftover(sp.res, n0 + 30ull * (32ull * jB + b));
-            uB &= uB - 1u;
-        }
-        __syncwarp();
-    }
-    __syncthreads();
-    for (uint32_t c = tid; c < ncand; c += blockDim.x) {
-        if (s_hist[c]) atomicAdd(&sp.res->hist[cr][s_ci[c]], s_hist[c]);
-        if (s_first[c] != kNone) atomicMin(&sp.res->first[s_ci[c]], s_first[c]);
+        __syncthreads();
     }
 }
 
-// Generic checker for a segment that reaches q < 7 (seg_start < 9788): one
+// Generic checker for segments that reach q < 7 (seg_start < 9788): one
 // thread per even, every candidate ascending, q = 3 and q = 5 prime by
 // definition (they are not in the class map), q < 3 ends the search.
-__global__ void __launch_bounds__(256) k_check_low(BatchParams bp, SegParams sp, const uint16_t *cand,
-                                                   uint32_t ridge_min)
+__global__ void __launch_bounds__(256) k_check_low(BatchDesc d, const uint16_t *cand, uint32_t ridge_min)
 {
-    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
-    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < evens;
-         e += uint64_t(gridDim.x) * blockDim.x) {
-        const uint64_t n = sp.seg_start + 2 * e;
-        const uint32_t cr = uint32_t(n % 30) / 2;
-        int ci = -1;
-        for (int c = 0; c < GBC_NCAND; ++c) {
-            const uint64_t p = cand[c];
-            if (p + 3 > n) break;
-            const uint64_t q = n - p;
-            bool prime;
-            if (q == 3 || q == 5) prime = true;
-            else if (q % 3 == 0 || q % 5 == 0) prime = false;
-            else {
-                const uint64_t t = (q - bp.base) / 30;
-                const uint32_t k = class_of(uint32_t(q % 30));
-                prime = (bp.map[size_t(k) * bp.wpc + (t >> 5)] >> (t & 31)) & 1u;
+    if (!d.h->nlow) return;
+    const uint32_t nseg = d.h->nseg;
+    for (uint32_t si = 0; si < nseg; ++si) {
+        const SegParams &sp = d.segs[si];
+        if (!sp.low) continue;
+        const BatchParams &bp = d.runs[sp.run];
+        const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
+        gbc_segment_result *res = sp.res;
+        for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < evens;
+             e += uint64_t(gridDim.x) * blockDim.x) {
+            const uint64_t n = sp.seg_start + 2 * e;
+            const uint32_t cr = uint32_t(n % 30) / 2;
+            int ci = -1;
+            for (int c = 0; c < GBC_NCAND; ++c) {
+                const uint64_t p = cand[c];
+                if (p + 3 > n) break;
+                const uint64_t q = n - p;
+                bool prime;
+                if (q == 3 || q == 5) prime = true;
+                else if (q % 3 == 0 || q % 5 == 0) prime = false;
+                else {
+                    const uint64_t t = (q - bp.base) / 30;
+                    const uint32_t k = class_of(uint32_t(q % 30));
+                    prime = (bp.map[size_t(k) * bp.wpc + (t >> 5)] >> (t & 31)) & 1u;
+                }
+                if (prime) {
+                    ci = c;
+                    break;
+                }
             }
-            if (prime) {
-                ci = c;
-                break;
+            if (ci >= 0) {
+                atomicAdd(&res->hist[cr][ci], 1u);
+                atomicMin(&res->first[ci], uint32_t(e));
+                if (sp.pn) sp.pn[e] = cand[ci];
+                if (cand[ci] >= ridge_min) append_ridge(res, n, cand[ci]);
+            } else {
+                append_leftover(res, n);
             }
-        }
-        if (ci >= 0) {
-            atomicAdd(&sp.res->hist[cr][ci], 1u);
-            atomicMin(&sp.res->first[ci], uint32_t(e));
-            if (sp.pn) sp.pn[e] = cand[ci];
-            if (cand[ci] >= ridge_min) append_ridge(sp.res, n, cand[ci]);
-        } else {
-            append_leftover(sp.res, n);
         }
     }
 }
 
 // Evens without a witness <= 9781: ascending odd p > 9781 by Miller-Rabin on
 // both p and n - p (n = 4: p = 2). A bounded search: a wait that runs out
-// sets an error flag instead of looping.
-__global__ void __launch_bounds__(64) k_retry(SegParams sp, uint32_t ridge_min)
+// sets an error flag instead of looping. A CTA per segment.
+__global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
 {
-    gbc_segment_result *res = sp.res;
-    const uint32_t nl = res->nleft < GBC_LEFT_CAP ? res->nleft : GBC_LEFT_CAP;
-    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
-        const uint64_t n = res->left_n[i];
-        uint64_t found = 0;
-        if (n == 4) found = 2;
-        else {
-            uint32_t tries = 0;
-            for (uint64_t p = GBC_MAX_CAND + 2; p <= n / 2; p += 2) {
-                if (++tries > (1u << 22)) {
-                    atomicOr(&res->err, kErrRetry);
-                    break;
-                }
-                if (is_prime_u64_dev(p) && is_prime_u64_dev(n - p)) {
-                    found = p;
-                    break;
+    const uint32_t nseg = d.h->nseg;
+    for (uint32_t si = blockIdx.x; si < nseg; si += gridDim.x) {
+        const SegParams &sp = d.segs[si];
+        gbc_segment_result *res = sp.res;
+        const uint32_t nl = res->nleft < GBC_LEFT_CAP ? res->nleft : GBC_LEFT_CAP;
+        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+            const uint64_t n = res->left_n[i];
+            uint64_t found = 0;
+            if (n == 4) found = 2;
+            else {
+                uint32_t tries = 0;
+                for (uint64_t p = GBC_MAX_CAND + 2; p <= n / 2; p += 2) {
+                    if (++tries > (1u << 22)) {
+                        atomicOr(&res->err, kErrRetry);
+                        break;
+                    }
+                    if (is_prime_u64_dev(p) && is_prime_u64_dev(n - p)) {
+                        found = p;
+                        break;
+                    }
                 }
             }
+            res->left_p[i] = found;
+            if (sp.pn) sp.pn[(n - sp.seg_start) / 2] = found < 65536 ? uint16_t(found) : 0;
+            if (found && found >= ridge_min) append_ridge(res, n, uint32_t(found));
         }
-        res->left_p[i] = found;
-        if (sp.pn) sp.pn[(n - sp.seg_start) / 2] = found < 65536 ? uint16_t(found) : 0;
-        if (found && found >= ridge_min) append_ridge(res, n, uint32_t(found));
     }
 }
 
@@ -278,115 +313,133 @@ constexpr uint32_t kMaxFun = 256;  // funnels per class the verify kernel holds
 // shifted by 0..d bits, so one 96-bit read tests up to five candidates for
 // 32 evens. No statistics here: evens left without a plan witness go to a
 // pending list of (class, word, bits) for k_tail.
-__global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchParams bp, SegParams sp, VerifyTables vt)
+__global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchDesc d, VerifyTables vt)
 {
     __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | top member << 21 | mask << 24
     __shared__ uint32_t s_win[kCheckWarps][8 * kVWin];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
 
-    const uint32_t cr = blockIdx.y, r = 2 * cr;
-    const uint64_t seg_start = sp.seg_start;
-    const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
-    if (n0 > sp.seg_end) return;
-    const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
-    const uint32_t nwords = uint32_t((ecount + 31) / 32);
-    const uint32_t nfun = vt.fun_cnt[cr] < kMaxFun ? vt.fun_cnt[cr] : kMaxFun;
+    __shared__ uint32_t s_vb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    gbc_segment_result *res = sp.res;
+    const uint32_t total = d.h->ver_vb, nseg = d.h->nseg;
+    for (;;) {
+        const uint32_t vb = next_item(d.work + kWorkVerify, &s_vb);
+        if (vb >= total) break;
+        const uint32_t si = find_prefix(d.ver_pref, nseg, vb);
+        const SegParams &sp = d.segs[si];
+        const BatchParams &bp = d.runs[sp.run];
+        const uint32_t local = vb - __ldg(d.ver_pref + si);
+        const uint32_t cr = local % GBC_NCLASS, bx = local / GBC_NCLASS, gx = sp.vbx, r = 2 * cr;
+        const uint64_t seg_start = sp.seg_start, base = bp.base;
+        const uint32_t wpc = bp.wpc;
+        const uint32_t *map = bp.map;
+        const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
+        if (n0 > sp.seg_end) {
+            __syncthreads();
+            continue;
+        }
+        const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
+        const uint32_t nwords = uint32_t((ecount + 31) / 32);
+        const uint32_t nfun = vt.fun_cnt[cr] < kMaxFun ? vt.fun_cnt[cr] : kMaxFun;
+        gbc_segment_result *res = sp.res;
+        uint2 *pend_list = sp.pend;
+        const uint32_t pend_cap = sp.pend_cap;
 
-    if (tid == 0) {
-        s_dmin = kNone;
-        s_dmax = 0;
-        s_pend = 0;
-    }
-    __syncthreads();
-    // the lowest window bit of each funnel: its top member p + 30 d
-    for (uint32_t f = tid; f < nfun; f += blockDim.x) {
-        const uint32_t e = vt.fun[vt.fun_off[cr] + f];
-        const uint32_t p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(e >> 16);
-        const uint32_t u = (r + 30 - p0 % 30) % 30;
-        const uint32_t dlow = uint32_t((n0 - bp.base - p0 - u) / 30) - dm;
-        atomicMin(&s_dmin, dlow);
-        atomicMax(&s_dmax, dlow);
-    }
-    __syncthreads();
-    const uint32_t dlo = s_dmin & ~31u;
-    const uint32_t nstage = (s_dmax - dlo) / 32 + 68;  // <= kVWin
-    for (uint32_t f = tid; f < nfun; f += blockDim.x) {
-        const uint32_t e = vt.fun[vt.fun_off[cr] + f];
-        const uint32_t mask = e >> 16, p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(mask);
-        const uint32_t u = (r + 30 - p0 % 30) % 30;
-        const uint32_t d = uint32_t((n0 - bp.base - p0 - u) / 30) - dm - dlo;
-        s_fent[f] = (class_of(u) * kVWin + (d >> 5)) | ((d & 31) << 16) | (dm << 21) | (mask << 24);
-    }
-    __syncthreads();
+        if (tid == 0) {
+            s_dmin = kNone;
+            s_dmax = 0;
+            s_pend = 0;
+        }
+        __syncthreads();
+        // the lowest window bit of each funnel: its top member p + 30 d
+        for (uint32_t f = tid; f < nfun; f += blockDim.x) {
+            const uint32_t e = vt.fun[vt.fun_off[cr] + f];
+            const uint32_t p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(e >> 16);
+            const uint32_t u = (r + 30 - p0 % 30) % 30;
+            const uint32_t dlow = uint32_t((n0 - base - p0 - u) / 30) - dm;
+            atomicMin(&s_dmin, dlow);
+            atomicMax(&s_dmax, dlow);
+        }
+        __syncthreads();
+        const uint32_t dlo = s_dmin & ~31u;
+        const uint32_t nstage = (s_dmax - dlo) / 32 + 68;  // <= kVWin
+        for (uint32_t f = tid; f < nfun; f += blockDim.x) {
+            const uint32_t e = vt.fun[vt.fun_off[cr] + f];
+            const uint32_t mask = e >> 16, p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(mask);
+            const uint32_t u = (r + 30 - p0 % 30) % 30;
+            const uint32_t dd = uint32_t((n0 - base - p0 - u) / 30) - dm - dlo;
+            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (dm << 21) | (mask << 24);
+        }
+        __syncthreads();
 
-    uint32_t *win = s_win[warp];
-    unsigned long long pend = 0;
-    for (uint32_t ch = blockIdx.x * kCheckWarps + warp; ch * 64 < nwords; ch += gridDim.x * kCheckWarps) {
-        const uint32_t J = ch * 64;
-        const uint32_t *src = bp.map + (dlo >> 5) + J;
+        uint32_t *win = s_win[warp];
+        uint32_t pend = 0;
+        for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps) {
+            const uint32_t J = ch * 64;
+            const uint32_t *src = map + (dlo >> 5) + J;
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k)
-            for (uint32_t i = lane; i < nstage; i += 32) win[k * kVWin + i] = __ldg(src + size_t(k) * bp.wpc + i);
-        __syncwarp();
-        const uint32_t jA = J + lane, jB = J + 32 + lane;
-        uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
-        const uint32_t *wl = win + lane;
-        for (uint32_t f = 0; f < nfun; ++f) {
-            if (!__any_sync(~0u, uA | uB)) break;
-            const uint32_t e = s_fent[f];
-            const uint32_t *w = wl + (e & 0xFFFF);
-            const uint32_t sh = (e >> 16) & 31, dm = (e >> 21) & 7, mask = e >> 24;
-            const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
-            uint32_t wa = 0, wb = 0;
+            for (uint32_t k = 0; k < 8; ++k)
+                for (uint32_t i = lane; i < nstage; i += 32) win[k * kVWin + i] = __ldg(src + size_t(k) * wpc + i);
+            __syncwarp();
+            const uint32_t jA = J + lane, jB = J + 32 + lane;
+            uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+            const uint32_t *wl = win + lane;
+            for (uint32_t f = 0; f < nfun; ++f) {
+                if (!__any_sync(~0u, uA | uB)) break;
+                const uint32_t e = s_fent[f];
+                const uint32_t *w = wl + (e & 0xFFFF);
+                const uint32_t sh = (e >> 16) & 31, dm = (e >> 21) & 7, mask = e >> 24;
+                const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
+                uint32_t wa = 0, wb = 0;
 #pragma unroll
-            for (uint32_t d = 0; d <= 4; ++d) {
-                if (!((mask >> d) & 1u)) continue;
-                const uint32_t a = sh + dm - d;  // member d's window starts a bits into the read
-                if (a < 32) {
-                    wa |= __funnelshift_r(x0, x1, a);
-                    wb |= __funnelshift_r(y0, y1, a);
-                } else {
-                    wa |= __funnelshift_r(x1, x2, a - 32);
-                    wb |= __funnelshift_r(y1, y2, a - 32);
+                for (uint32_t dd = 0; dd <= 4; ++dd) {
+                    if (!((mask >> dd) & 1u)) continue;
+                    const uint32_t a = sh + dm - dd;  // member dd's window starts a bits into the read
+                    if (a < 32) {
+                        wa |= __funnelshift_r(x0, x1, a);
+                        wb |= __funnelshift_r(y0, y1, a);
+                    } else {
+                        wa |= __funnelshift_r(x1, x2, a - 32);
+                        wb |= __funnelshift_r(y1, y2, a - 32);
+                    }
+                }
+                uA &= ~wa;
+                uB &= ~wb;
+            }
+            // pending words: one reservation per warp
+            const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
+            uint32_t pre = has;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t n = __shfl_up_sync(~0u, pre, o);
+                if (lane >= uint32_t(o)) pre += n;
+            }
+            const uint32_t tot = __shfl_sync(~0u, pre, 31);
+            if (tot) {
+                uint32_t at0 = 0;
+                if (lane == 31) at0 = atomicAdd(&res->npend, tot);
+                at0 = __shfl_sync(~0u, at0, 31);
+                uint32_t at = at0 + pre - has;
+                if (uA) {
+                    if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jA, uA);
+                    else atomicOr(&res->err, kErrPendOverflow);
+                    ++at;
+                }
+                if (uB) {
+                    if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jB, uB);
+                    else atomicOr(&res->err, kErrPendOverflow);
                 }
             }
-            uA &= ~wa;
-            uB &= ~wb;
+            pend += __popc(uA) + __popc(uB);
+            __syncwarp();
         }
-        // pending words: one reservation per warp
-        const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
-        uint32_t pre = has;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(~0u, pre, o);
-            if (lane >= uint32_t(o)) pre += n;
-        }
-        const uint32_t total = __shfl_sync(~0u, pre, 31);
-        if (total) {
-            uint32_t base = 0;
-            if (lane == 31) base = atomicAdd(&res->npend, total);
-            base = __shfl_sync(~0u, base, 31);
-            uint32_t at = base + pre - has;
-            if (uA) {
-                if (at < sp.pend_cap) sp.pend[at] = make_uint2((cr << 27) | jA, uA);
-                else atomicOr(&res->err, kErrPendOverflow);
-                ++at;
-            }
-            if (uB) {
-                if (at < sp.pend_cap) sp.pend[at] = make_uint2((cr << 27) | jB, uB);
-                else atomicOr(&res->err, kErrPendOverflow);
-            }
-        }
-        pend += __popc(uA) + __popc(uB);
-        __syncwarp();
+        pend = __reduce_add_sync(~0u, pend);
+        if (lane == 0 && pend) atomicAdd(&s_pend, (unsigned long long)pend);
+        __syncthreads();
+        if (tid == 0 && s_pend) atomicAdd((unsigned long long *)&res->pending, s_pend);
+        __syncthreads();
     }
-    pend = __reduce_add_sync(~0u, uint32_t(pend));
-    if (lane == 0 && pend) atomicAdd(&s_pend, pend);
-    __syncthreads();
-    if (tid == 0 && s_pend) atomicAdd((unsigned long long *)&res->pending, s_pend);
 }
 
 // Phase B (the reference's check30_b, kernels/goldbach.cl:2210-2306): the
@@ -394,33 +447,57 @@ __global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchParams bp, Seg
 // ascending order (every plan member already failed for it), one thread per
 // pending word. The histogram and first occurrences of these evens hold
 // every even with p(n) >= the plan bound; ridges above the floor are listed.
-__global__ void __launch_bounds__(128) k_tail(BatchParams bp, SegParams sp, VerifyTables vt)
+__global__ void __launch_bounds__(128) k_tail(BatchDesc d, VerifyTables vt)
 {
-    gbc_segment_result *res = sp.res;
-    const uint32_t np = res->npend < sp.pend_cap ? res->npend : sp.pend_cap;
-    const uint64_t seg_start = sp.seg_start;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
-        const uint2 e = sp.pend[i];
-        const uint32_t cr = e.x >> 27, j = e.x & ((1u << 27) - 1), r = 2 * cr;
-        uint32_t mask = e.y;
-        const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
-        const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);
-        const uint32_t off = vt.rest_off[cr], cnt = vt.rest_cnt[cr];
-        for (uint32_t c = 0; c < cnt && mask; ++c) {
-            const uint32_t ci = vt.rest[off + c];
-            const uint32_t p = vt.cand[ci];
-            const uint32_t u = (r + 30 - p % 30) % 30;
-            const uint32_t pos = uint32_t((n0 - bp.base - p - u) / 30) + 32 * j;
-            const uint32_t *wk = bp.map + size_t(class_of(u)) * bp.wpc + (pos >> 5);
-            const uint32_t hit = mask & __funnelshift_r(__ldg(wk), __ldg(wk + 1), pos & 31);
-            if (!hit) continue;
-            atomicAdd(&res->hist[cr][ci], uint32_t(__popc(hit)));
-            atomicMin(&res->first[ci], idx0 + 15u * (32u * j + __ffs(hit) - 1u));
-            if (p >= vt.ridge_min)
-                for (uint32_t h = hit; h; h &= h - 1u) append_ridge(res, n0 + 30ull * (32ull * j + __ffs(h) - 1u), p);
-            mask &= ~hit;
+    const uint32_t nseg = d.h->nseg;
+    for (uint32_t si = 0; si < nseg; ++si) {
+        const SegParams &sp = d.segs[si];
+        if (sp.sampled) continue;
+        const BatchParams &bp = d.runs[sp.run];
+        gbc_segment_result *res = sp.res;
+        const uint32_t np = res->npend < sp.pend_cap ? res->npend : sp.pend_cap;
+        const uint64_t seg_start = sp.seg_start, base = bp.base;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+            const uint2 e = sp.pend[i];
+            const uint32_t cr = e.x >> 27, j = e.x & ((1u << 27) - 1), r = 2 * cr;
+            uint32_t mask = e.y;
+            const uint64_t n0 = seg_start + (r + 30 - uint32_t(seg_start % 30)) % 30;
+            const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);
+            const uint32_t off = vt.rest_off[cr], cnt = vt.rest_cnt[cr];
+            for (uint32_t c = 0; c < cnt && mask; ++c) {
+                const uint32_t ci = vt.rest[off + c];
+                const uint32_t p = vt.cand[ci];
+                const uint32_t u = (r + 30 - p % 30) % 30;
+                const uint32_t pos = uint32_t((n0 - base - p - u) / 30) + 32 * j;
+                const uint32_t *wk = bp.map + size_t(class_of(u)) * bp.wpc + (pos >> 5);
+                const uint32_t hit = mask & __funnelshift_r(__ldg(wk), __ldg(wk + 1), pos & 31);
+                if (!hit) continue;
+                atomicAdd(&res->hist[cr][ci], uint32_t(__popc(hit)));
+                atomicMin(&res->first[ci], idx0 + 15u * (32u * j + __ffs(hit) - 1u));
+                if (p >= vt.ridge_min)
+                    for (uint32_t h = hit; h; h &= h - 1u)
+                        append_ridge(res, n0 + 30ull * (32ull * j + __ffs(h) - 1u), p);
+                mask &= ~hit;
+            }
+            for (; mask; mask &= mask - 1u) append_leftover(res, n0 + 30ull * (32ull * j + __ffs(mask) - 1u));
         }
-        for (; mask; mask &= mask - 1u) append_leftover(res, n0 + 30ull * (32ull * j + __ffs(mask) - 1u));
+    }
+}
+
+// Result areas of the batch's segments: zero, except the first-occurrence
+// indices and the first prime (all ones: none yet); the slot's error word.
+__global__ void __launch_bounds__(256) k_init(BatchDesc d)
+{
+    constexpr uint32_t kWords = sizeof(gbc_segment_result) / 4;
+    constexpr uint32_t kF0 = offsetof(gbc_segment_result, first) / 4, kF1 = kF0 + GBC_NCAND;
+    constexpr uint32_t kP0 = offsetof(gbc_segment_result, first_prime) / 4;
+    const uint32_t nseg = d.h->nseg;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0 && d.h->nrun) *d.runs[0].err = 0;
+    for (uint32_t si = 0; si < nseg; ++si) {
+        uint32_t *w = reinterpret_cast<uint32_t *>(d.segs[si].res);
+        for (uint32_t i = tid; i < kWords; i += gridDim.x * blockDim.x)
+            w[i] = ((i >= kF0 && i < kF1) || i == kP0 || i == kP0 + 1) ? ~0u : 0u;
     }
 }
 
@@ -428,43 +505,50 @@ __global__ void __launch_bounds__(128) k_tail(BatchParams bp, SegParams sp, Veri
 
 namespace gbh {
 
-void launch_check(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::CheckTables &ct, int sm_count,
-                  cudaStream_t st)
+void launch_init(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 {
-    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
-    if (sp.low) {
-        uint64_t blocks = (evens + 255) / 256;
-        if (blocks > uint64_t(sm_count) * 16) blocks = uint64_t(sm_count) * 16;
-        gbk::k_check_low<<<uint32_t(blocks), 256, 0, st>>>(bp, sp, ct.cand, ct.ridge_min);
-        return;
-    }
-    // words per class ~ evens / 15 / 32; 8 warps per CTA, chunks of 64 words
-    const uint64_t words = (evens / 15 + 32) / 32 + 1;
-    uint64_t bx = (words + gbk::kCheckWarps * 64 - 1) / (gbk::kCheckWarps * 64);
-    const uint64_t cap = uint64_t(sm_count) * 2;  // per class: the 15 classes share the GPU
-    if (bx > cap) bx = cap;
-    if (bx < 1) bx = 1;
-    dim3 grid(uint32_t(bx), GBC_NCLASS);
-    gbk::k_check<<<grid, gbk::kCheckThreads, 0, st>>>(bp, sp, ct);
+    gbk::k_init<<<g.sm * 2, 256, 0, st>>>(d);
 }
 
-void launch_retry(const gbk::SegParams &sp, uint32_t ridge_min, cudaStream_t st)
+// checker CTAs per class of a segment with the given evens (a virtual grid
+// column count: each warp about six 64-word chunks, to spread the CTA's
+// table setup; at most two per SM)
+uint32_t check_vbx(uint64_t evens, int sm)
 {
-    gbk::k_retry<<<1, 64, 0, st>>>(sp, ridge_min);
-}
-
-void launch_verify(const gbk::BatchParams &bp, const gbk::SegParams &sp, const gbk::VerifyTables &vt, int sm_count,
-                   cudaStream_t st)
-{
-    const uint64_t evens = (sp.seg_end - sp.seg_start) / 2 + 1;
     const uint64_t words = (evens / 15 + 32) / 32 + 1;
-    uint64_t bx = (words + gbk::kCheckWarps * 64 - 1) / (gbk::kCheckWarps * 64);
-    const uint64_t cap = uint64_t(sm_count) * 2;
+    constexpr uint64_t kPerVb = gbk::kCheckWarps * 64 * 6;
+    uint64_t bx = (words + kPerVb - 1) / kPerVb;
+    const uint64_t cap = uint64_t(sm) * 2;
     if (bx > cap) bx = cap;
     if (bx < 1) bx = 1;
-    dim3 grid(uint32_t(bx), GBC_NCLASS);
-    gbk::k_verify<<<grid, gbk::kCheckThreads, 0, st>>>(bp, sp, vt);
-    gbk::k_tail<<<uint32_t(sm_count) * 2, 128, 0, st>>>(bp, sp, vt);
+    return uint32_t(bx);
+}
+
+void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st)
+{
+    gbk::k_check_low<<<g.sm * 16, 256, 0, st>>>(d, ct.cand, ct.ridge_min);
+    gbk::k_check<<<g.sm * g.check, gbk::kCheckThreads, 0, st>>>(d, ct);
+}
+
+void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st)
+{
+    gbk::k_verify<<<g.sm * g.verify, gbk::kCheckThreads, 0, st>>>(d, vt);
+    gbk::k_tail<<<g.sm * 2, 128, 0, st>>>(d, vt);
+}
+
+void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st)
+{
+    gbk::k_retry<<<g.max_seg < 1024 ? g.max_seg : 1024, 64, 0, st>>>(d, ridge_min);
+}
+
+void query_check_grids(Grids &g)
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_check, gbk::kCheckThreads, 0);
+    g.check = n > 0 ? n : 1;
+    n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_verify, gbk::kCheckThreads, 0);
+    g.verify = n > 0 ? n : 1;
 }
 
 }  // namespace gbh

@@ -69,18 +69,13 @@ __device__ __forceinline__ int32_t rel_clamp(uint64_t x, uint64_t q0)
 // residue of class k (0..7) by one byte permute
 __device__ __forceinline__ uint32_t unit_of(uint32_t k) { return __byte_perm(0x0D0B0701u, 0x1D171311u, k) & 0xFF; }
 
-struct CountRanges {
-    uint32_t hash_t[8][2];  // per class: bits of the hashed q range (inclusive)
-    uint32_t cnt_t[8][2];   // bits of the counted primes
-    uint32_t twin_t[8][2];  // bits of the counted lower twin primes
-    uint32_t w_lo, w_hi;    // words covering the hashed range
-    uint32_t in_lo, in_hi;  // words inside all three ranges for every class (in_hi < in_lo: none)
-};
-
 constexpr int kCountThreads = 256;
 constexpr int32_t kNoPos = INT32_MIN;
 
-__global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegParams sp, CountRanges cr)
+// Persistent: a fixed grid takes the virtual CTAs of every segment of the
+// batch (per segment: one per 256 words of its hashed range) from a work
+// counter.
+__global__ void __launch_bounds__(kCountThreads) k_count(BatchDesc d)
 {
     __shared__ uint32_t s_ghist[GBC_GBINS];
     __shared__ int32_t s_wlast[kCountThreads / 32];
@@ -90,171 +85,183 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchParams bp, SegPara
     __shared__ int32_t s_first, s_last;
     __shared__ unsigned long long s_hash;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x) s_ghist[i] = 0;
-    if (tid < 12) s_cnt[tid] = 0;
-    const uint32_t wc0 = cr.w_lo + blockIdx.x * blockDim.x;  // first word of the CTA
-    const uint64_t q0 = bp.base + 30ull * 32ull * wc0;         // q of relative position 0
-    if (tid == 0) {
-        s_key = 0;
-        s_first = INT32_MAX;
-        s_last = kNoPos;
-        s_hash = 0;
-        // last hashed prime before the CTA's first word (negative position)
-        int32_t pv = kNoPos;
-        for (int64_t ww = int64_t(wc0) - 1; ww >= int64_t(cr.w_lo) && pv == kNoPos; --ww) {
-            for (uint32_t k = 0; k < 8; ++k) {
-                const uint32_t v = bp.map[size_t(k) * bp.wpc + ww] &
-                                   range_mask(uint32_t(ww), cr.hash_t[k][0], cr.hash_t[k][1]);
-                if (v) {
-                    const int32_t pos =
-                        int32_t(30 * (32 * (ww - int64_t(wc0)) + 31 - __clz(v))) + int32_t(unit_of(k));
-                    if (pos > pv) pv = pos;
-                }
-            }
-        }
-        s_prev0 = pv;
-    }
-    // the counted range as positions relative to q0 (the CTA's positions
-    // stay within +-2^20, so clamping at +-2^30 changes nothing)
-    const int32_t clo = rel_clamp(sp.cnt_lo, q0), chi = rel_clamp(sp.cnt_hi, q0);
-
-    const uint32_t w = wc0 + tid;
-    const bool valid = w <= cr.w_hi;
-    const bool inner = w >= cr.in_lo && w <= cr.in_hi;
-    uint32_t h[8], c[8], raw[8];
-#pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) {
-        raw[k] = valid ? bp.map[size_t(k) * bp.wpc + w] : 0u;
-        h[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
-        c[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]);
-    }
-    // twins (11, 13), (17, 19) inside a block; (29, 31) into the next block
-    const uint32_t next0 = valid ? bp.map[w + 1] : 0u;  // class 0, word w + 1
-    const uint32_t up29 = (raw[0] >> 1) | (next0 << 31);
-    const uint32_t tw0 = __popc(raw[2] & raw[3] & (inner ? ~0u : range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1])));
-    const uint32_t tw1 = __popc(raw[4] & raw[5] & (inner ? ~0u : range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1])));
-    const uint32_t tw2 = __popc(raw[7] & up29 & (inner ? ~0u : range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1])));
-
-    // one byte per block, natural order: word i of T holds blocks 4 i .. 4 i + 3
-    uint32_t T[8];
-#pragma unroll
-    for (uint32_t g = 0; g < 4; ++g) {
-        const uint32_t sel = g | ((g + 4) << 4);
-        const uint32_t lo = __byte_perm(__byte_perm(h[0], h[1], sel), __byte_perm(h[2], h[3], sel), 0x5410);
-        const uint32_t hi = __byte_perm(__byte_perm(h[4], h[5], sel), __byte_perm(h[6], h[7], sel), 0x5410);
-        const uint64_t t = transpose8((uint64_t(hi) << 32) | lo);
-        T[2 * g] = uint32_t(t);
-        T[2 * g + 1] = uint32_t(t >> 32);
-    }
-    const int32_t cbase = int32_t(960 * tid);  // position of this thread's first block
-    int32_t mylast = kNoPos;
-    uint32_t nh = 0;
-#pragma unroll
-    for (int i = 7; i >= 0; --i)
-        if (T[i] && mylast == kNoPos) {
-            const uint32_t b = 31 - __clz(T[i]);
-            mylast = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
-        }
-    // exclusive max-scan of mylast over the CTA
-    int32_t v = mylast;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int32_t n = __shfl_up_sync(~0u, v, o);
-        if (lane >= uint32_t(o) && n > v) v = n;
-    }
-    int32_t excl = __shfl_up_sync(~0u, v, 1);
-    if (lane == 0) excl = kNoPos;
-    if (lane == 31) s_wlast[warp] = v;
-    __syncthreads();
-    int32_t prev = s_prev0;
-    if (excl > prev) prev = excl;
-    for (uint32_t i = 0; i < warp; ++i)
-        if (s_wlast[i] > prev) prev = s_wlast[i];
-
-    // the primes in natural order: gaps of the counted ones, the hash of all
-    const bool hash = !(sp.flags & GBC_SEG_NOHASH);
-    uint64_t hsum = 0;
-    uint32_t key = 0, err = 0;
-    int32_t cfirst = INT32_MAX, clast = kNoPos;
-#pragma unroll
-    for (uint32_t i = 0; i < 8; ++i) {
-        uint32_t x = T[i];
-        nh += __popc(x);
-        while (x) {
-            const uint32_t b = __ffs(x) - 1u;
-            x &= x - 1u;
-            const int32_t pos = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
-            if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
-            if (pos >= clo && pos <= chi) {
-                if (pos < cfirst) cfirst = pos;
-                clast = pos;
-                if (prev != kNoPos) {
-                    const uint32_t g = uint32_t(pos - prev);
-                    if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
-                    else atomicAdd(&s_ghist[g / 2], 1u);
-                    // largest gap, the smallest lower prime on ties: g << 21 | ~(lower + 2^20)
-                    const uint32_t k2 = (g << 21) | (0x1FFFFFu - uint32_t(prev + (1 << 20)));
-                    if (k2 > key) key = k2;
-                    if (g >= GBC_GTAIL) {
-                        const uint32_t slot = atomicAdd(&sp.res->ntail, 1u);
-                        if (slot < GBC_TAIL_CAP) {
-                            sp.res->tail_g[slot] = g;
-                            sp.res->tail_lo[slot] = q0 + uint64_t(int64_t(prev));
-                        } else err |= kErrTailOverflow;
+    __shared__ uint32_t s_vb;
+    const uint32_t total = d.h->cnt_vb, nseg = d.h->nseg;
+    for (;;) {
+        const uint32_t vb = next_item(d.work + kWorkCount, &s_vb);
+        if (vb >= total) break;
+        const uint32_t si = find_prefix(d.cnt_pref, nseg, vb);
+        const SegParams &sp = d.segs[si];
+        const BatchParams &bp = d.runs[sp.run];
+        const CountRanges &cr = sp.cr;
+        const uint32_t vbx = vb - __ldg(d.cnt_pref + si);
+        for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x) s_ghist[i] = 0;
+        if (tid < 12) s_cnt[tid] = 0;
+        const uint32_t wc0 = cr.w_lo + vbx * blockDim.x;  // first word of the CTA
+        const uint64_t q0 = bp.base + 30ull * 32ull * wc0;         // q of relative position 0
+        if (tid == 0) {
+            s_key = 0;
+            s_first = INT32_MAX;
+            s_last = kNoPos;
+            s_hash = 0;
+            // last hashed prime before the CTA's first word (negative position)
+            int32_t pv = kNoPos;
+            for (int64_t ww = int64_t(wc0) - 1; ww >= int64_t(cr.w_lo) && pv == kNoPos; --ww) {
+                for (uint32_t k = 0; k < 8; ++k) {
+                    const uint32_t v = bp.map[size_t(k) * bp.wpc + ww] &
+                                       range_mask(uint32_t(ww), cr.hash_t[k][0], cr.hash_t[k][1]);
+                    if (v) {
+                        const int32_t pos =
+                            int32_t(30 * (32 * (ww - int64_t(wc0)) + 31 - __clz(v))) + int32_t(unit_of(k));
+                        if (pos > pv) pv = pos;
                     }
-                } else if (q0 + uint64_t(int64_t(pos)) > 7) {
-                    err |= kErrNoPred;
                 }
             }
-            prev = pos;
+            s_prev0 = pv;
         }
-    }
-    if (err) atomicOr(&sp.res->err, err);
+        // the counted range as positions relative to q0 (the CTA's positions
+        // stay within +-2^20, so clamping at +-2^30 changes nothing)
+        const int32_t clo = rel_clamp(sp.cnt_lo, q0), chi = rel_clamp(sp.cnt_hi, q0);
 
-    // warp reductions, then one shared atomic per warp
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) hsum += __shfl_xor_sync(~0u, hsum, o);
-    key = __reduce_max_sync(~0u, key);
-    cfirst = __reduce_min_sync(~0u, cfirst);
-    clast = __reduce_max_sync(~0u, clast);
-    uint32_t r8[12];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) r8[k] = __reduce_add_sync(~0u, __popc(c[k]));
-    r8[8] = __reduce_add_sync(~0u, tw0);
-    r8[9] = __reduce_add_sync(~0u, tw1);
-    r8[10] = __reduce_add_sync(~0u, tw2);
-    r8[11] = __reduce_add_sync(~0u, nh);
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < 12; ++k) atomicAdd(&s_cnt[k], r8[k]);
-        atomicAdd(&s_hash, (unsigned long long)hsum);
-        atomicMax(&s_key, key);
-        atomicMin(&s_first, cfirst);
-        atomicMax(&s_last, clast);
-    }
-    __syncthreads();
-    gbc_segment_result *res = sp.res;
-    for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x)
-        if (s_ghist[i]) atomicAdd(&res->ghist[i], s_ghist[i]);
-    if (tid < 8) {
-        if (s_cnt[tid]) atomicAdd((unsigned long long *)&res->primes30[tid], (unsigned long long)s_cnt[tid]);
-    } else if (tid < 11) {
-        if (s_cnt[tid]) atomicAdd((unsigned long long *)&res->twins[tid - 8], (unsigned long long)s_cnt[tid]);
-    } else if (tid == 11) {
-        if (hash) atomicAdd((unsigned long long *)&res->map_hash, s_hash);
-        atomicAdd((unsigned long long *)&res->map_primes, (unsigned long long)s_cnt[11]);
-    } else if (tid == 12) {
-        if (s_key) {
-            const uint64_t g = s_key >> 21;
-            const uint64_t lower = q0 + uint64_t(int64_t(int32_t(0x1FFFFFu - (s_key & 0x1FFFFFu)) - (1 << 20)));
-            const unsigned long long k64 = (g << 32) | (0xFFFFFFFFull - uint32_t(lower - sp.hash_lo));
-            atomicMax((unsigned long long *)&res->gmax_key, k64);
+        const uint32_t w = wc0 + tid;
+        const bool valid = w <= cr.w_hi;
+        const bool inner = w >= cr.in_lo && w <= cr.in_hi;
+        uint32_t h[8], c[8], raw[8];
+    #pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            raw[k] = valid ? bp.map[size_t(k) * bp.wpc + w] : 0u;
+            h[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
+            c[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]);
         }
-    } else if (tid == 13) {
-        if (s_first != INT32_MAX)
-            atomicMin((unsigned long long *)&res->first_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_first))));
-        if (s_last != kNoPos)
-            atomicMax((unsigned long long *)&res->last_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_last))));
+        // twins (11, 13), (17, 19) inside a block; (29, 31) into the next block
+        const uint32_t next0 = valid ? bp.map[w + 1] : 0u;  // class 0, word w + 1
+        const uint32_t up29 = (raw[0] >> 1) | (next0 << 31);
+        const uint32_t tw0 = __popc(raw[2] & raw[3] & (inner ? ~0u : range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1])));
+        const uint32_t tw1 = __popc(raw[4] & raw[5] & (inner ? ~0u : range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1])));
+        const uint32_t tw2 = __popc(raw[7] & up29 & (inner ? ~0u : range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1])));
+
+        // one byte per block, natural order: word i of T holds blocks 4 i .. 4 i + 3
+        uint32_t T[8];
+    #pragma unroll
+        for (uint32_t g = 0; g < 4; ++g) {
+            const uint32_t sel = g | ((g + 4) << 4);
+            const uint32_t lo = __byte_perm(__byte_perm(h[0], h[1], sel), __byte_perm(h[2], h[3], sel), 0x5410);
+            const uint32_t hi = __byte_perm(__byte_perm(h[4], h[5], sel), __byte_perm(h[6], h[7], sel), 0x5410);
+            const uint64_t t = transpose8((uint64_t(hi) << 32) | lo);
+            T[2 * g] = uint32_t(t);
+            T[2 * g + 1] = uint32_t(t >> 32);
+        }
+        const int32_t cbase = int32_t(960 * tid);  // position of this thread's first block
+        int32_t mylast = kNoPos;
+        uint32_t nh = 0;
+    #pragma unroll
+        for (int i = 7; i >= 0; --i)
+            if (T[i] && mylast == kNoPos) {
+                const uint32_t b = 31 - __clz(T[i]);
+                mylast = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+            }
+        // exclusive max-scan of mylast over the CTA
+        int32_t v = mylast;
+    #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t n = __shfl_up_sync(~0u, v, o);
+            if (lane >= uint32_t(o) && n > v) v = n;
+        }
+        int32_t excl = __shfl_up_sync(~0u, v, 1);
+        if (lane == 0) excl = kNoPos;
+        if (lane == 31) s_wlast[warp] = v;
+        __syncthreads();
+        int32_t prev = s_prev0;
+        if (excl > prev) prev = excl;
+        for (uint32_t i = 0; i < warp; ++i)
+            if (s_wlast[i] > prev) prev = s_wlast[i];
+
+        // the primes in natural order: gaps of the counted ones, the hash of all
+        const bool hash = !(sp.flags & GBC_SEG_NOHASH);
+        uint64_t hsum = 0;
+        uint32_t key = 0, err = 0;
+        int32_t cfirst = INT32_MAX, clast = kNoPos;
+    #pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+            uint32_t x = T[i];
+            nh += __popc(x);
+            while (x) {
+                const uint32_t b = __ffs(x) - 1u;
+                x &= x - 1u;
+                const int32_t pos = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+                if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
+                if (pos >= clo && pos <= chi) {
+                    if (pos < cfirst) cfirst = pos;
+                    clast = pos;
+                    if (prev != kNoPos) {
+                        const uint32_t g = uint32_t(pos - prev);
+                        if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
+                        else atomicAdd(&s_ghist[g / 2], 1u);
+                        // largest gap, the smallest lower prime on ties: g << 21 | ~(lower + 2^20)
+                        const uint32_t k2 = (g << 21) | (0x1FFFFFu - uint32_t(prev + (1 << 20)));
+                        if (k2 > key) key = k2;
+                        if (g >= GBC_GTAIL) {
+                            const uint32_t slot = atomicAdd(&sp.res->ntail, 1u);
+                            if (slot < GBC_TAIL_CAP) {
+                                sp.res->tail_g[slot] = g;
+                                sp.res->tail_lo[slot] = q0 + uint64_t(int64_t(prev));
+                            } else err |= kErrTailOverflow;
+                        }
+                    } else if (q0 + uint64_t(int64_t(pos)) > 7) {
+                        err |= kErrNoPred;
+                    }
+                }
+                prev = pos;
+            }
+        }
+        if (err) atomicOr(&sp.res->err, err);
+
+        // warp reductions, then one shared atomic per warp
+    #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) hsum += __shfl_xor_sync(~0u, hsum, o);
+        key = __reduce_max_sync(~0u, key);
+        cfirst = __reduce_min_sync(~0u, cfirst);
+        clast = __reduce_max_sync(~0u, clast);
+        uint32_t r8[12];
+    #pragma unroll
+        for (int k = 0; k < 8; ++k) r8[k] = __reduce_add_sync(~0u, __popc(c[k]));
+        r8[8] = __reduce_add_sync(~0u, tw0);
+        r8[9] = __reduce_add_sync(~0u, tw1);
+        r8[10] = __reduce_add_sync(~0u, tw2);
+        r8[11] = __reduce_add_sync(~0u, nh);
+        if (lane == 0) {
+    #pragma unroll
+            for (int k = 0; k < 12; ++k) atomicAdd(&s_cnt[k], r8[k]);
+            atomicAdd(&s_hash, (unsigned long long)hsum);
+            atomicMax(&s_key, key);
+            atomicMin(&s_first, cfirst);
+            atomicMax(&s_last, clast);
+        }
+        __syncthreads();
+        gbc_segment_result *res = sp.res;
+        for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x)
+            if (s_ghist[i]) atomicAdd(&res->ghist[i], s_ghist[i]);
+        if (tid < 8) {
+            if (s_cnt[tid]) atomicAdd((unsigned long long *)&res->primes30[tid], (unsigned long long)s_cnt[tid]);
+        } else if (tid < 11) {
+            if (s_cnt[tid]) atomicAdd((unsigned long long *)&res->twins[tid - 8], (unsigned long long)s_cnt[tid]);
+        } else if (tid == 11) {
+            if (hash) atomicAdd((unsigned long long *)&res->map_hash, s_hash);
+            atomicAdd((unsigned long long *)&res->map_primes, (unsigned long long)s_cnt[11]);
+        } else if (tid == 12) {
+            if (s_key) {
+                const uint64_t g = s_key >> 21;
+                const uint64_t lower = q0 + uint64_t(int64_t(int32_t(0x1FFFFFu - (s_key & 0x1FFFFFu)) - (1 << 20)));
+                const unsigned long long k64 = (g << 32) | (0xFFFFFFFFull - uint32_t(lower - sp.hash_lo));
+                atomicMax((unsigned long long *)&res->gmax_key, k64);
+            }
+        } else if (tid == 13) {
+            if (s_first != INT32_MAX)
+                atomicMin((unsigned long long *)&res->first_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_first))));
+            if (s_last != kNoPos)
+                atomicMax((unsigned long long *)&res->last_prime, (unsigned long long)(q0 + uint64_t(int64_t(s_last))));
+        }
+        __syncthreads();
     }
 }
 
@@ -308,19 +315,24 @@ static void inner_words(const uint32_t t[8][2], uint32_t &lo, uint32_t &hi)
     hi = uint32_t(h);
 }
 
-void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStream_t st)
+uint32_t count_ranges(uint64_t base, const gbk::SegParams &sp, gbk::CountRanges &cr)
 {
-    gbk::CountRanges cr;
-    class_range(bp.base, sp.hash_lo, sp.hash_hi, cr.hash_t);
-    class_range(bp.base, sp.cnt_lo, sp.cnt_hi, cr.cnt_t);
-    class_range(bp.base, sp.cnt_lo, sp.twin_hi, cr.twin_t);
+    class_range(base, sp.hash_lo, sp.hash_hi, cr.hash_t);
+    class_range(base, sp.cnt_lo, sp.cnt_hi, cr.cnt_t);
+    class_range(base, sp.cnt_lo, sp.twin_hi, cr.twin_t);
     uint32_t tlo = 0xFFFFFFFFu, thi = 0;
     for (int k = 0; k < 8; ++k)
         if (cr.hash_t[k][1] >= cr.hash_t[k][0]) {
             if (cr.hash_t[k][0] < tlo) tlo = cr.hash_t[k][0];
             if (cr.hash_t[k][1] > thi) thi = cr.hash_t[k][1];
         }
-    if (tlo > thi) return;
+    if (tlo > thi) {
+        cr.w_lo = 1;
+        cr.w_hi = 0;
+        cr.in_lo = 1;
+        cr.in_hi = 0;
+        return 0;
+    }
     cr.w_lo = tlo / 32;
     cr.w_hi = thi / 32;
     uint32_t a0, a1, b0, b1, c0, c1;
@@ -330,8 +342,19 @@ void launch_count(const gbk::BatchParams &bp, const gbk::SegParams &sp, cudaStre
     cr.in_lo = std::max({a0, b0, c0});
     cr.in_hi = std::min({a1, b1, c1});
     const uint32_t nw = cr.w_hi - cr.w_lo + 1;
-    const uint32_t blocks = (nw + gbk::kCountThreads - 1) / gbk::kCountThreads;
-    gbk::k_count<<<blocks, gbk::kCountThreads, 0, st>>>(bp, sp, cr);
+    return (nw + gbk::kCountThreads - 1) / gbk::kCountThreads;
+}
+
+void launch_count(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_count<<<g.sm * g.count, gbk::kCountThreads, 0, st>>>(d);
+}
+
+void query_count_grids(Grids &g)
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_count, gbk::kCountThreads, 0);
+    g.count = n > 0 ? n : 1;
 }
 
 }  // namespace gbh

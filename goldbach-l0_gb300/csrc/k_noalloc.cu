@@ -153,8 +153,8 @@ extern "C" int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_
     // every scratch word a kernel reads is written earlier in this call:
     // nothing needs clearing
     k_noalloc_magic<<<64, 256, 0, st>>>(d_primes, nprimes, scratch + kPatWords);
-    gbh::launch_xfirst(bp, st);
-    gbh::launch_tile(bp, g_groups, st);
+    gbh::launch_xfirst1(bp, st);
+    gbh::launch_tile1(bp, g_groups, st);  // 2^16-bit tiles: under the default shared-memory limit
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(err, err_cap, GBC_E_CUDA, cudaGetErrorString(e));
     return GBC_OK;

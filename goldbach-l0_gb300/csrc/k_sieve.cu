@@ -1,22 +1,26 @@
-// k_sieve.cu -- builds a batch's mod-30 class map on the GPU.
+// k_sieve.cu -- builds the mod-30 class maps of a batch on the GPU.
 //
 // Stages (the reference's make_prime_map, mid_setup/mid_window and
 // sieve_large_packed, kernels/goldbach.cl:1092-1608, 3528-3701, 1738-1849,
-// re-designed for one HBM-resident map per batch of segments):
-//   k_xfirst  per tile-sieve prime and class: the first class bit of the
-//             batch that is a multiple of p and >= p^2 (mid_setup's job,
+// re-designed for HBM-resident maps, one per run of consecutive segments,
+// and persistent kernels that take every run of the batch in one launch):
+//   k_xfirst  per tile-sieve prime, class and run: the first class bit of
+//             the run that is a multiple of p and >= p^2 (mid_setup's job,
 //             goldbach.cl:3528-3563; host_math.cpp:80-113).
-//   k_tile    one CTA per (tile, class): 2^tile_log2 bits in shared memory;
-//             the primes 7..67 by whole-word AND patterns of seven prime
-//             groups, then every prime 71..p_mid by shared-memory atomics
-//             (small primes warp-cooperatively, the rest one per thread);
-//             one coalesced store of the finished tile.
-//   k_large   primes above p_mid, one thread per prime, marking every
-//             multiple p m (m coprime to 30) of the batch with a global
-//             atomic AND after a read (read-before-mark, goldbach.cl:
+//   k_tile    one CTA per (run, class, tile) item: up to 2^tile_log2 bits in
+//             shared memory; the primes 7..67 by whole-word AND patterns of
+//             seven prime groups, then every prime 71..p_mid by shared-memory
+//             atomics (small primes warp-cooperatively, the rest one per
+//             thread); one coalesced store of the finished tile.
+//   k_large   primes above p_mid, one thread per prime and every run it
+//             reaches, marking every multiple p m (m coprime to 30) with a
+//             global atomic AND after a read (read-before-mark, goldbach.cl:
 //             328-336), skipping multipliers divisible by 7..23 whose
 //             multiples the pattern stage already cleared (the 30030 wheel
 //             and the 17..29 skip of goldbach.cl:638-748).
+//   k_hitlist the primes above p_hl through the prime-multiplier table.
+// A thread reads its prime once and applies it to every run of the batch,
+// so a batch of many short windows streams the sieving primes once.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,22 +29,61 @@
 
 namespace gbk {
 
-// First class bit, for each class k, of a multiple of p in the batch with
-// q >= p^2; kNone when the first one is at or past nblk. p > 29.
+// x mod p, exactly, for x < p * 2^32 and 3 <= p < 2^32, without a
+// division: a float estimate of the quotient (error below 2^11 for these
+// bounds), an exact 64-bit remainder r (negative when the estimate was
+// high), a second float estimate of the now small quotient r / p (error
+// below 1), and a final +-p correction. rp = 1/p rounded to nearest.
+__device__ __forceinline__ uint32_t mod_below(uint64_t x, uint32_t p, float rp)
+{
+    // float(x) from its two 32-bit halves (32-bit conversions only: 64-bit
+    // integer <-> float conversions are multi-instruction sequences)
+    const float xf = fmaf(__uint2float_rz(uint32_t(x >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(x)));
+    const uint32_t qe = __float2uint_rz(xf * rp);
+    int64_t r = int64_t(x - uint64_t(qe) * p);
+    // |r| < 2^43: float(|r|) from its halves as above, then the sign (the
+    // halves of a negative r would lose up to 2^8 in the low word's
+    // conversion, too much for p below 2^9)
+    const uint64_t m = r < 0 ? uint64_t(-r) : uint64_t(r);
+    const float mf = fmaf(__uint2float_rz(uint32_t(m >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(m)));
+    const float rf = r < 0 ? -mf : mf;
+    const int32_t q2 = __float2int_rn(rf * rp);
+    r -= int64_t(q2) * p;
+    if (r < 0) r += p;
+    if (r >= int64_t(p)) r -= p;
+    return uint32_t(r);
+}
+
+// x mod p for any 64-bit x (two base-2^32 digits)
+__device__ __forceinline__ uint32_t mod_u64(uint64_t x, uint32_t p, float rp)
+{
+    const uint32_t r = mod_below(uint32_t(x >> 32), p, rp);
+    return mod_below((uint64_t(r) << 32) | uint32_t(x), p, rp);
+}
+
+// a + d mod p for a, d < p without overflow
+__device__ __forceinline__ uint32_t addmod(uint32_t a, uint32_t d, uint32_t p)
+{
+    return a >= p - d ? a - (p - d) : a + d;
+}
+
+// First class bit, for each class k, of a multiple of p in the run with
+// q >= p^2; kNone when the first one is at or past nblk. 29 < p < 2^31.
 __device__ __forceinline__ void first_bits8(uint64_t base, uint32_t nblk, uint32_t p, uint32_t *out)
 {
-    const uint32_t r = uint32_t(base % p);
+    const float rp = __frcp_rn(float(p));
+    const uint32_t r = mod_u64(base, p, rp);
     const uint32_t iv = inv30_mod(p);
     const uint64_t pp = uint64_t(p) * p;
 #pragma unroll
     for (uint32_t k = 0; k < 8; ++k) {
         const uint32_t u = unit30(k);
-        uint32_t a = r + u;                 // (base + u) mod p
+        uint32_t a = r + u;                                  // (base + u) mod p
         if (a >= p) a -= p;
-        a = a ? p - a : 0;                  // -(base + u) mod p
-        uint64_t t = uint64_t(a) * iv % p;  // base + 30 t + u = 0 (mod p)
+        a = a ? p - a : 0;                                   // -(base + u) mod p
+        uint64_t t = mod_below(uint64_t(a) * iv, p, rp);     // base + 30 t + u = 0 (mod p)
         const uint64_t q = base + 30 * t + u;
-        if (q < pp) {                       // p itself and smaller multiples stay unmarked
+        if (q < pp) {                                        // p itself and smaller multiples stay unmarked
             const uint64_t tmin = (pp - base - u + 29) / 30;
             if (tmin > t) t += (tmin - t + p - 1) / p * p;
         }
@@ -48,7 +91,28 @@ __device__ __forceinline__ void first_bits8(uint64_t base, uint32_t nblk, uint32
     }
 }
 
-__global__ void __launch_bounds__(256) k_xfirst(BatchParams bp)
+// every run's first bits of the tile-sieve primes
+__global__ void __launch_bounds__(256) k_xfirst(BatchDesc d)
+{
+    const uint32_t nrun = d.h->nrun, nmax = d.h->n_mid_max;
+    if (!nrun) return;
+    const uint32_t *primes = d.runs[0].primes;
+    for (uint32_t i = d.runs[0].i0 + blockIdx.x * blockDim.x + threadIdx.x; i < nmax; i += gridDim.x * blockDim.x) {
+        const uint32_t p = primes[i];
+        for (uint32_t r = 0; r < nrun; ++r) {
+            const BatchParams &bp = d.runs[r];
+            const uint32_t n = bp.n_mid;
+            if (i >= n) continue;
+            uint32_t x[8];
+            first_bits8(bp.base, bp.nblk, p, x);
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) bp.xfirst[size_t(k) * n + i] = x[k];
+        }
+    }
+}
+
+// the same for one run passed by value
+__global__ void __launch_bounds__(256) k_xfirst1(BatchParams bp)
 {
     const uint32_t n = bp.n_mid;
     for (uint32_t i = bp.i0 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -59,7 +123,7 @@ __global__ void __launch_bounds__(256) k_xfirst(BatchParams bp)
     }
 }
 
-// Tile-local first mark of a prime from its batch-level first bit x.
+// Tile-local first mark of a prime from its run-level first bit x.
 __device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_t p, uint32_t magic, uint32_t tb)
 {
     if (x == kNone) return kNone;
@@ -74,17 +138,15 @@ __device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_
     return rem ? p - rem : 0;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
+// Sieves bits [t0, t0 + tl) of class array k of a run in shared memory s
+// (the group patterns already in pat) and stores them. tl is a multiple of
+// 128 bits. Ends with the CTA synchronized, s free for the next tile.
+__device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo &gi, const uint32_t *pat,
+                                          uint32_t *s, uint32_t k, uint32_t t0, uint32_t tl)
 {
-    extern __shared__ uint32_t sm[];
-    const uint32_t tb = 1u << bp.tile_log2, tw = tb >> 5;
-    uint32_t *s = sm;
-    uint32_t *pat = sm + tw;
-    const uint32_t k = blockIdx.y, tid = threadIdx.x, bs = blockDim.x;
-    const uint32_t t0 = blockIdx.x << bp.tile_log2;
+    const uint32_t tid = threadIdx.x, bs = blockDim.x;
+    const uint32_t tw = tl >> 5;
     const uint64_t q0 = bp.base + 30ull * t0 + unit30(k);
-
-    for (uint32_t i = tid; i < gi.words; i += bs) pat[i] = bp.pat[i];
 
     // phase of this thread's first word in each group's canonical pattern:
     // local bit x is cleared by the group iff (x + c) mod P has a factor in
@@ -99,7 +161,6 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
         ph[g] = uint32_t((32ull * tid + c) % P);
         stp[g] = uint32_t((32ull * bs) % P);
     }
-    __syncthreads();
     for (uint32_t w = tid; w < tw; w += bs) {
         uint32_t v = ~0u;
 #pragma unroll
@@ -121,7 +182,7 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
             const uint32_t p = small[i];
             if (p % 30 == unit30(k) && p >= q0) {
                 const uint32_t b = uint32_t((p - q0) / 30);
-                if (b < tb) s[b >> 5] |= 1u << (b & 31);
+                if (b < tl) s[b >> 5] |= 1u << (b & 31);
             }
         }
         if (q0 == 1) s[0] &= ~1u;
@@ -133,61 +194,71 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchParams bp, GroupInfo gi)
     // small primes: a warp per prime, lanes take every 32nd multiple
     for (uint32_t i = bp.i0 + warp; i < bp.i_warp; i += nw) {
         const uint32_t p = bp.primes[i];
-        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tb);
-        if (l >= tb) continue;
-        for (uint32_t b = l + lane * p; b < tb; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tl);
+        if (l >= tl) continue;
+        for (uint32_t b = l + lane * p; b < tl; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
     }
     // the rest: a thread per prime
     for (uint32_t i = bp.i_warp + tid; i < bp.n_mid; i += bs) {
         const uint32_t p = bp.primes[i];
-        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tb);
-        for (uint32_t b = l; b < tb; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tl);
+        for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
     }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(bp.map + size_t(k) * bp.wpc + (t0 >> 5));
     const uint4 *src = reinterpret_cast<const uint4 *>(s);
     for (uint32_t i = tid; i < tw / 4; i += bs) dst[i] = src[i];
+    __syncthreads();
 }
 
-// x mod p, exactly, for x < p * 2^32 and 2^7 <= p < 2^32, without a
-// division: a float estimate of the quotient (error below 2^10 for these
-// bounds), an exact 64-bit remainder, a second float estimate of the now
-// small quotient (error below 1), and a final +-p correction. rp = 1/p
-// rounded to nearest.
-__device__ __forceinline__ uint32_t mod_below(uint64_t x, uint32_t p, float rp)
+// Persistent tile kernel: CTAs take the batch's (run, class, tile) items
+// from a work counter; a run's last tile of a class ends at its class
+// array's end.
+__global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tile_log2)
 {
-    // float(x) from its two 32-bit halves (32-bit conversions only: 64-bit
-    // integer <-> float conversions are multi-instruction sequences)
-    const float xf = fmaf(__uint2float_rz(uint32_t(x >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(x)));
-    const uint32_t qe = __float2uint_rz(xf * rp);
-    int64_t r = int64_t(x - uint64_t(qe) * p);
-    // |r| < 2^42: float(r) from its halves, exactly as above
-    const float rf = fmaf(float(int32_t(r >> 32)), 4294967296.0f, __uint2float_rz(uint32_t(r)));
-    const int32_t q2 = __float2int_rn(rf * rp);
-    r -= int64_t(q2) * p;
-    if (r < 0) r += p;
-    if (r >= int64_t(p)) r -= p;
-    return uint32_t(r);
+    extern __shared__ uint32_t sm[];
+    const uint32_t tb = 1u << tile_log2;
+    uint32_t *s = sm;
+    uint32_t *pat = sm + (tb >> 5);
+    const uint32_t nrun = d.h->nrun, items = d.h->tile_items;
+    if (!nrun) return;
+    __shared__ uint32_t s_j;
+    for (uint32_t i = threadIdx.x; i < gi.words; i += blockDim.x) pat[i] = d.runs[0].pat[i];
+    for (;;) {
+        const uint32_t j = next_item(d.work + kWorkTile, &s_j);
+        if (j >= items) break;
+        const uint32_t r = find_prefix(d.tile_pref, nrun, j);
+        const BatchParams &bp = d.runs[r];
+        const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
+        const uint32_t k = local / tpc, t0 = (local - k * tpc) << tile_log2;
+        const uint32_t tl = min(tb, bp.wpc * 32 - t0);
+        tile_body(bp, gi, pat, s, k, t0, tl);
+    }
 }
 
-// a + d mod p for a, d < p without overflow
-__device__ __forceinline__ uint32_t addmod(uint32_t a, uint32_t d, uint32_t p)
+// one run by value: grid (tiles_pc, 8), full tiles (wpc = tiles_pc tiles)
+__global__ void __launch_bounds__(1024, 1) k_tile1(BatchParams bp, GroupInfo gi)
 {
-    return a >= p - d ? a - (p - d) : a + d;
+    extern __shared__ uint32_t sm[];
+    const uint32_t tb = 1u << bp.tile_log2;
+    uint32_t *pat = sm + (tb >> 5);
+    for (uint32_t i = threadIdx.x; i < gi.words; i += blockDim.x) pat[i] = bp.pat[i];
+    __syncthreads();
+    tile_body(bp, gi, pat, sm, blockIdx.y, blockIdx.x << bp.tile_log2, tb);
 }
 
-// Marks class k's multiples p m of the pass, m coprime to 30 and to 7..23,
+// Marks class k's multiples p m of the run, m coprime to 30 and to 7..23,
 // from class bit t on: read the word, clear with an atomic AND only if the
 // bit is still set.
 template <uint32_t K>
-__device__ __forceinline__ void large_walk(const BatchParams &bp, uint32_t t, uint32_t p, uint32_t pi1, uint32_t pi2,
-                                           uint32_t bm1, uint32_t bm2, const uint32_t *s_skip)
+__device__ __forceinline__ void large_walk(uint32_t *map, uint32_t wpc, uint32_t nblk, uint32_t t, uint32_t p,
+                                           uint32_t pi1, uint32_t pi2, uint32_t bm1, uint32_t bm2,
+                                           const uint32_t *s_skip)
 {
     constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
     constexpr uint32_t u = (0x1D1713110D0B0701ull >> (8 * K)) & 0xFF;
-    const uint32_t nblk = bp.nblk;
     if (t >= nblk) return;
-    uint32_t *wk = bp.map + size_t(K) * bp.wpc;
+    uint32_t *wk = map + size_t(K) * wpc;
     // multiplier m = q / p modulo 1001 and 7429: m = q p^-1, q = base + 30 t + u
     uint32_t m1 = (bm1 + (30 * (t % kSkip1) + u) % kSkip1) % kSkip1 * pi1 % kSkip1;
     uint32_t m2 = (bm2 + (30 * (t % kSkip2) + u) % kSkip2) % kSkip2 * pi2 % kSkip2;
@@ -207,63 +278,69 @@ __device__ __forceinline__ void large_walk(const BatchParams &bp, uint32_t t, ui
     }
 }
 
-// One pass of the large primes over class bits [0, nblk) of the map at
-// bp.map (bp.base already moved to the pass's first block).
-__global__ void __launch_bounds__(256) k_large(BatchParams bp)
+// The large primes [n_mid, n_hl) of every run: a thread per prime, the
+// runs in turn.
+__global__ void __launch_bounds__(256) k_large(BatchDesc d)
 {
     __shared__ uint32_t s_skip[(kSkip1 + 31) / 32 + (kSkip2 + 31) / 32];
     __shared__ uint16_t s_inv[kSkip1 + kSkip2];
     constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
-    for (uint32_t i = threadIdx.x; i < kW1 + (kSkip2 + 31) / 32; i += blockDim.x) s_skip[i] = bp.skip_tab[i];
-    for (uint32_t i = threadIdx.x; i < kSkip1 + kSkip2; i += blockDim.x) s_inv[i] = bp.inv_tab[i];
+    const uint32_t nrun = d.h->nrun;
+    if (!nrun) return;
+    const BatchParams &b0 = d.runs[0];
+    for (uint32_t i = threadIdx.x; i < kW1 + (kSkip2 + 31) / 32; i += blockDim.x) s_skip[i] = b0.skip_tab[i];
+    for (uint32_t i = threadIdx.x; i < kSkip1 + kSkip2; i += blockDim.x) s_inv[i] = b0.inv_tab[i];
     __syncthreads();
-    const uint64_t base = bp.base;
-    const uint32_t bm1 = uint32_t(base % kSkip1), bm2 = uint32_t(base % kSkip2);
-    const uint32_t bhi = uint32_t(base >> 32), blo = uint32_t(base);
-    for (uint32_t i = bp.n_mid + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_hl;
+    const uint32_t *primes = b0.primes;
+    const uint32_t nhi = d.h->n_hl_max;
+    for (uint32_t i = d.h->n_mid_min + blockIdx.x * blockDim.x + threadIdx.x; i < nhi;
          i += gridDim.x * blockDim.x) {
-        const uint32_t p = bp.primes[i];
+        const uint32_t p = primes[i];
         const float rp = __frcp_rn(float(p));
-        // r = base mod p by two base-2^32 digits
-        uint32_t r = mod_below(bhi, p, rp);
-        r = mod_below((uint64_t(r) << 32) | blo, p, rp);
         const uint32_t iv = inv30_mod(p);
-        // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
-        const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
         const uint32_t d2 = addmod(iv, iv, p), d4 = addmod(d2, d2, p), d6 = addmod(d4, d2, p);
         const uint32_t pi1 = s_inv[p % kSkip1], pi2 = s_inv[kSkip1 + p % kSkip2];
-        const bool need_pp = uint64_t(p) * p > base;  // only near the bottom of the range
-        uint32_t c = iv;
-        uint32_t t[8];
-#pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
-            uint32_t x = tb - c;
-            if (tb < c) x += p;
-            t[k] = x;
-            const uint32_t d = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
-            c = addmod(c, d, p);
-        }
-        if (need_pp) {
-            const uint64_t pp = uint64_t(p) * p;
+        for (uint32_t ri = 0; ri < nrun; ++ri) {
+            const BatchParams &bp = d.runs[ri];
+            if (i < bp.n_mid || i >= bp.n_hl) continue;
+            const uint64_t base = bp.base;
+            const uint32_t nblk = bp.nblk, wpc = bp.wpc, bm1 = bp.bm1, bm2 = bp.bm2;
+            uint32_t *map = bp.map;
+            const uint32_t r = mod_u64(base, p, rp);
+            // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
+            const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
+            uint32_t c = iv;
+            uint32_t t[8];
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
-                const uint64_t u = unit30(k);
-                const uint64_t q = base + 30ull * t[k] + u;
-                if (q < pp) {
-                    const uint64_t tmin = (pp - base - u + 29) / 30;
-                    const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
-                    t[k] = tt < bp.nblk ? uint32_t(tt) : kNone;
+                uint32_t x = tb - c;
+                if (tb < c) x += p;
+                t[k] = x;
+                const uint32_t dd = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
+                c = addmod(c, dd, p);
+            }
+            if (uint64_t(p) * p > base) {  // only near the bottom of the range
+                const uint64_t pp = uint64_t(p) * p;
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) {
+                    const uint64_t u = unit30(k);
+                    const uint64_t q = base + 30ull * t[k] + u;
+                    if (q < pp) {
+                        const uint64_t tmin = (pp - base - u + 29) / 30;
+                        const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
+                        t[k] = tt < nblk ? uint32_t(tt) : kNone;
+                    }
                 }
             }
+            large_walk<0>(map, wpc, nblk, t[0], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<1>(map, wpc, nblk, t[1], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<2>(map, wpc, nblk, t[2], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<3>(map, wpc, nblk, t[3], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<4>(map, wpc, nblk, t[4], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<5>(map, wpc, nblk, t[5], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<6>(map, wpc, nblk, t[6], p, pi1, pi2, bm1, bm2, s_skip);
+            large_walk<7>(map, wpc, nblk, t[7], p, pi1, pi2, bm1, bm2, s_skip);
         }
-        large_walk<0>(bp, t[0], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<1>(bp, t[1], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<2>(bp, t[2], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<3>(bp, t[3], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<4>(bp, t[4], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<5>(bp, t[5], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<6>(bp, t[6], p, pi1, pi2, bm1, bm2, s_skip);
-        large_walk<7>(bp, t[7], p, pi1, pi2, bm1, bm2, s_skip);
     }
 }
 
@@ -295,11 +372,12 @@ __device__ __forceinline__ uint32_t inv_mod_2_32(uint32_t p)
 // hl_harvest_mt / hl_apply, kernels/goldbach.cl:3181-3471): for a prime
 // p >= cbrt(q), a composite multiplier m of q = p m has a prime factor below
 // p, which marks q already, so only prime m matter. One thread per prime
-// p: the primes m in [ceil(Q0 / p), floor(Q1 / p)] are one contiguous run of
-// bytes of the table; each gives q = p m, whose class bit is cleared with an
-// atomic AND. Every such q is a semiprime whose factors are both above the
-// sieving bound of the other stages, so the bit is set and no read is needed.
-__global__ void __launch_bounds__(256) k_hitlist(BatchParams bp)
+// p and run: the primes m in [ceil(Q0 / p), floor(Q1 / p)] are one
+// contiguous run of bytes of the table; each gives q = p m, whose class bit
+// is cleared with an atomic AND. Every such q is a semiprime whose factors
+// are both above the sieving bound of the other stages, so the bit is set
+// and no read is needed.
+__global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
 {
     // class array of q = p m from the classes of p and of m
     __shared__ uint8_t s_cls[8][8];
@@ -308,34 +386,45 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchParams bp)
         s_cls[a][b] = uint8_t(class_of(unit30(a) * unit30(b) % 30));
     }
     __syncthreads();
-    const uint64_t q0 = bp.base, q1 = bp.base + 30ull * bp.nblk - 1;
-    const uint64_t m0 = bp.m0;
-    for (uint32_t i = bp.n_hl + blockIdx.x * blockDim.x + threadIdx.x; i < bp.n_all;
+    const uint32_t nrun = d.h->nrun;
+    if (!nrun) return;
+    const uint32_t *primes = d.runs[0].primes;
+    const uint32_t nhi = d.h->n_all_max;
+    for (uint32_t i = d.h->n_hl_min + blockIdx.x * blockDim.x + threadIdx.x; i < nhi;
          i += gridDim.x * blockDim.x) {
-        const uint32_t p = bp.primes[i];
+        const uint32_t p = primes[i];
         const float rp = __frcp_rn(float(p));
         const uint32_t pinv = inv_mod_2_32(p);
-        uint32_t r0, r1;
-        uint64_t mlo = divmod_u64(q0, p, rp, pinv, r0);
-        mlo += r0 ? 1 : 0;
-        const uint64_t mhi = divmod_u64(q1, p, rp, pinv, r1);
-        if (mhi < mlo) continue;
-        if (mlo < m0 || mhi > bp.m1) {
-            atomicOr(bp.err, kErrTable);
-            continue;
-        }
         const uint32_t kp = class_of(p % 30);
-        const uint64_t b0 = (mlo - m0) / 30, b1 = (mhi - m0) / 30;
-        for (uint64_t w = b0 >> 2; w <= (b1 >> 2); ++w) {
-            uint32_t v = bp.mtab[w];
-            while (v) {
-                const uint32_t j = __ffs(v) - 1u;
-                v &= v - 1u;
-                const uint32_t k = j & 7;
-                const uint64_t m = m0 + 30 * (4 * w + (j >> 3)) + unit30(k);
-                if (m < mlo || m > mhi) continue;
-                const uint64_t t = (uint64_t(p) * m - bp.base) / 30;
-                atomicAnd(bp.map + size_t(s_cls[kp][k]) * bp.wpc + (t >> 5), ~(1u << (t & 31)));
+        for (uint32_t ri = 0; ri < nrun; ++ri) {
+            const BatchParams &bp = d.runs[ri];
+            if (i < bp.n_hl || i >= bp.n_all) continue;
+            const uint64_t base = bp.base, q1 = base + 30ull * bp.nblk - 1;
+            uint32_t r0, r1;
+            uint64_t mlo = divmod_u64(base, p, rp, pinv, r0);
+            mlo += r0 ? 1 : 0;
+            const uint64_t mhi = divmod_u64(q1, p, rp, pinv, r1);
+            if (mhi < mlo) continue;
+            const uint64_t m0 = bp.m0;
+            if (mlo < m0 || mhi > bp.m1) {
+                atomicOr(bp.err, kErrTable);
+                continue;
+            }
+            uint32_t *map = bp.map;
+            const uint32_t wpc = bp.wpc;
+            const uint32_t *mtab = bp.mtab;
+            const uint64_t b0 = (mlo - m0) / 30, b1 = (mhi - m0) / 30;
+            for (uint64_t w = b0 >> 2; w <= (b1 >> 2); ++w) {
+                uint32_t v = mtab[w];
+                while (v) {
+                    const uint32_t j = __ffs(v) - 1u;
+                    v &= v - 1u;
+                    const uint32_t k = j & 7;
+                    const uint64_t m = m0 + 30 * (4 * w + (j >> 3)) + unit30(k);
+                    if (m < mlo || m > mhi) continue;
+                    const uint64_t t = (uint64_t(p) * m - base) / 30;
+                    atomicAnd(map + size_t(s_cls[kp][k]) * wpc + (t >> 5), ~(1u << (t & 31)));
+                }
             }
         }
     }
@@ -368,33 +457,83 @@ __global__ void __launch_bounds__(256) k_wheel_bytes(BatchParams bp, uint32_t *o
     }
 }
 
+// Map self-check: every word of every run's class arrays in two batch
+// descriptors of the same geometry (the maps built with and without hit
+// lists); differing words are counted and flag the batch.
+__global__ void __launch_bounds__(256) k_map_compare(BatchDesc a, BatchDesc b, uint32_t *count)
+{
+    const uint32_t nrun = a.h->nrun;
+    for (uint32_t r = 0; r < nrun; ++r) {
+        const BatchParams &ra = a.runs[r];
+        const uint32_t *mb = b.runs[r].map;
+        const size_t words = size_t(8) * ra.wpc;
+        uint32_t bad = 0;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < words; i += size_t(gridDim.x) * blockDim.x)
+            bad += ra.map[i] != mb[i];
+        bad = __reduce_add_sync(~0u, bad);
+        if ((threadIdx.x & 31) == 0 && bad) {
+            atomicAdd(count, bad);
+            atomicOr(ra.err, kErrSelfCheck);
+        }
+    }
+}
+
 }  // namespace gbk
 
 namespace gbh {
 
-static int sm_count_cached();
-
-int launch_hitlist(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st)
+void launch_map_compare(const gbk::BatchDesc &a, const gbk::BatchDesc &b, uint32_t *count, const Grids &g,
+                        cudaStream_t st)
 {
-    if (bp.n_all <= bp.n_hl) return 0;
-    const uint32_t n = bp.n_all - bp.n_hl;
-    uint32_t blocks = uint32_t(sm_count_cached()) * 8;
-    const uint32_t need = (n + 255) / 256;
-    if (blocks > need) blocks = need;
-    // passes over pass_mb megabytes of map: each prime redoes its two
-    // divisions per pass, and the pass's atomic marks stay in L2
-    uint64_t pass_bits = (uint64_t(pass_mb ? pass_mb : 48) << 20) & ~uint64_t(31);
-    if (pass_bits < 32) pass_bits = 32;
-    int launches = 0;
-    for (uint64_t lo = 0; lo < bp.nblk; lo += pass_bits) {
-        gbk::BatchParams q = bp;
-        q.base = bp.base + 30 * lo;
-        q.nblk = uint32_t(std::min<uint64_t>(bp.nblk - lo, pass_bits));
-        q.map = bp.map + (lo >> 5);
-        gbk::k_hitlist<<<blocks, 256, 0, st>>>(q);
-        ++launches;
-    }
-    return launches;
+    gbk::k_map_compare<<<g.sm * 8, 256, 0, st>>>(a, b, count);
+}
+
+static size_t tile_smem(uint32_t tile_log2, const gbk::GroupInfo &gi)
+{
+    return size_t(((1u << tile_log2) >> 5) + gi.words) * 4;
+}
+
+void tile_attributes(uint32_t tile_log2, const gbk::GroupInfo &gi)
+{
+    const int smem = int(tile_smem(tile_log2, gi));
+    cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_xfirst<<<g.sm * 8, 256, 0, st>>>(d);
+}
+
+void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
+                 cudaStream_t st)
+{
+    gbk::k_tile<<<g.sm, 1024, tile_smem(tile_log2, gi), st>>>(d, gi, tile_log2);
+}
+
+void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_large<<<g.sm * 8, 256, 0, st>>>(d);
+}
+
+void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_hitlist<<<g.sm * 8, 256, 0, st>>>(d);
+}
+
+void launch_xfirst1(const gbk::BatchParams &bp, cudaStream_t st)
+{
+    if (bp.n_mid <= bp.i0) return;
+    const uint32_t n = bp.n_mid - bp.i0;
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    gbk::k_xfirst1<<<blocks, 256, 0, st>>>(bp);
+}
+
+void launch_tile1(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st)
+{
+    dim3 grid(bp.tiles_pc, 8);
+    gbk::k_tile1<<<grid, 1024, tile_smem(bp.tile_log2, gi), st>>>(bp, gi);
 }
 
 void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st)
@@ -403,63 +542,6 @@ void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t 
     uint32_t blocks = (nw + 255) / 256;
     if (blocks > 65535) blocks = 65535;
     gbk::k_wheel_bytes<<<blocks, 256, 0, st>>>(bp, out);
-}
-
-static int sm_count_cached()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
-
-void launch_xfirst(const gbk::BatchParams &bp, cudaStream_t st)
-{
-    if (bp.n_mid <= bp.i0) return;
-    const uint32_t n = bp.n_mid - bp.i0;
-    uint32_t blocks = (n + 255) / 256;
-    if (blocks > 8192) blocks = 8192;
-    gbk::k_xfirst<<<blocks, 256, 0, st>>>(bp);
-}
-
-void launch_tile(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st)
-{
-    const uint32_t tw = (1u << bp.tile_log2) >> 5;
-    const size_t smem = size_t(tw + gi.words) * 4;
-    static size_t set_for = 0;
-    if (set_for != smem) {
-        cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        set_for = smem;
-    }
-    dim3 grid(bp.tiles_pc, 8);
-    gbk::k_tile<<<grid, 1024, smem, st>>>(bp, gi);
-}
-
-int launch_large(const gbk::BatchParams &bp, uint32_t pass_mb, cudaStream_t st)
-{
-    if (bp.n_all <= bp.n_mid) return 0;
-    const uint32_t n = bp.n_all - bp.n_mid;
-    uint32_t blocks = uint32_t(sm_count_cached()) * 8;
-    const uint32_t need = (n + 255) / 256;
-    if (blocks > need) blocks = need;
-    // passes of pass_mb megabytes of map (8 class slices of pass bits / 8
-    // bytes each), so the random marks of a pass stay in L2
-    uint64_t pass_bits = (uint64_t(pass_mb ? pass_mb : 48) << 20) & ~uint64_t(31);
-    if (pass_bits < 32) pass_bits = 32;
-    int launches = 0;
-    for (uint64_t lo = 0; lo < bp.nblk; lo += pass_bits) {
-        gbk::BatchParams q = bp;
-        q.base = bp.base + 30 * lo;
-        q.nblk = uint32_t(std::min<uint64_t>(bp.nblk - lo, pass_bits));
-        q.map = bp.map + (lo >> 5);
-        gbk::k_large<<<blocks, 256, 0, st>>>(q);
-        ++launches;
-    }
-    return launches;
 }
 
 }  // namespace gbh

@@ -3,9 +3,9 @@
 The product path is libgbc.so next to this file; importing this module does
 not load it. `load()` loads it and raises if it is missing (there is no CPU
 fallback). `Context` wraps one gbc_ctx: the per-segment contract
-(enqueue_batch / collect, the reference's enqueue/collect_slot,
-src/verifier.cpp:1741-2444) and the whole-range call verify_range
-(gb::run_gpu, include/verifier.hpp:71-110).
+(enqueue_batch / enqueue_segments / collect, the reference's
+enqueue/collect_slot, src/verifier.cpp:1741-2444) and the whole-range call
+verify_range (gb::run_gpu, include/verifier.hpp:71-110).
 """
 import ctypes as C
 import os
@@ -24,6 +24,7 @@ DEFAULT_SEGMENT = 467_500_000
 MAX_LIMIT = 18446742974197923840
 SEG_NOHASH = 2
 SEG_VERIFY = 4
+MAX_SLOTS = 8
 
 ERRORS = {0: "ok", -1: "argument", -2: "cuda", -3: "device flag", -4: "timeout", -5: "state", -6: "overflow"}
 
@@ -31,9 +32,10 @@ ERRORS = {0: "ok", -1: "argument", -2: "cuda", -3: "device flag", -4: "timeout",
 class Config(C.Structure):
     _fields_ = [("limit", C.c_uint64), ("segment_even", C.c_uint64), ("max_batch", C.c_uint32),
                 ("tile_log2", C.c_uint32), ("p_mid", C.c_uint32), ("want_pn", C.c_uint32),
-                ("device", C.c_int32), ("large_pass_mb", C.c_uint32), ("hl_mode", C.c_uint32),
-                ("mtab_max_gb", C.c_uint32), ("hl_pass_mb", C.c_uint32), ("sample_every", C.c_uint32),
-                ("plan_funnels", C.c_uint32), ("ridge_min", C.c_uint32)]
+                ("device", C.c_int32), ("max_runs", C.c_uint32), ("hl_mode", C.c_uint32),
+                ("mtab_max_gb", C.c_uint32), ("nslots", C.c_uint32), ("sample_every", C.c_uint32),
+                ("plan_funnels", C.c_uint32), ("ridge_min", C.c_uint32), ("launch_mode", C.c_uint32),
+                ("selfcheck_every", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class SegmentResult(C.Structure):
@@ -55,7 +57,14 @@ class SegmentResult(C.Structure):
 
 class BatchTimes(C.Structure):
     _fields_ = [("ms_setup", C.c_float), ("ms_tile", C.c_float), ("ms_large", C.c_float),
-                ("ms_check", C.c_float), ("ms_count", C.c_float), ("ms_total", C.c_float)]
+                ("ms_check", C.c_float), ("ms_count", C.c_float), ("ms_total", C.c_float),
+                ("ms_selfcheck", C.c_float), ("runs", C.c_uint32)]
+
+
+class CtxStats(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("batches", C.c_uint64), ("graph_replays", C.c_uint64),
+                ("selfchecks", C.c_uint64), ("mtab_builds", C.c_uint64), ("mtab_bytes", C.c_uint64),
+                ("mtab_build_ms", C.c_double), ("device_bytes", C.c_uint64)]
 
 
 class RunResult(C.Structure):
@@ -63,6 +72,18 @@ class RunResult(C.Structure):
                 ("batches", C.c_uint64), ("leftovers", C.c_uint64), ("pmax", C.c_uint64),
                 ("primes", C.c_uint64), ("twins", C.c_uint64), ("gpu_seconds", C.c_double),
                 ("wall_seconds", C.c_double)]
+
+
+class WindowsSummary(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("segments", C.c_uint64), ("runs", C.c_uint64),
+                ("gpu_seconds", C.c_double), ("wall_seconds", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
+                ("segments", C.c_uint64), ("runs", C.c_uint64), ("max_in_flight", C.c_uint32),
+                ("pad", C.c_uint32), ("gpu_seconds", C.c_double), ("wall_seconds", C.c_double),
+                ("device_bytes", C.c_uint64), ("hbm_budget", C.c_uint64)]
 
 
 # every entry point of include/gbc.h: name -> (restype, argtypes)
@@ -74,6 +95,13 @@ SIGNATURES = {
     "gbc_candidates": (C.c_int, [C.POINTER(C.c_uint16), C.c_int]),
     "gbc_enqueue_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.c_int,
                                     C.c_uint64]),
+    "gbc_enqueue_segments": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                       C.POINTER(C.c_uint64), C.c_int]),
+    "gbc_poll": (C.c_int, [C.c_void_p, C.c_int]),
+    "gbc_prepare": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
+    "gbc_get_stats": (C.c_int, [C.c_void_p, C.POINTER(CtxStats)]),
+    "gbc_map_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                              C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint64]),
     "gbc_collect": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(SegmentResult), C.c_int, C.POINTER(BatchTimes),
                               C.c_int]),
     "gbc_copy_pn": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_uint16), C.c_uint64]),
@@ -84,6 +112,15 @@ SIGNATURES = {
     "gbc_launch_count": (C.c_uint64, [C.c_void_p]),
     "gbc_verify_range": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(RunResult), C.c_char_p,
                                    C.c_uint64, C.POINTER(C.c_uint16)]),
+    "gbc_verify_windows": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int, C.POINTER(RunResult),
+                                     C.c_char_p, C.c_uint64, C.POINTER(WindowsSummary)]),
+    "gbc_server_start": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "gbc_server_submit": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gbc_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int, C.POINTER(RunResult), C.c_char_p, C.c_uint64,
+                                  C.POINTER(C.c_double)]),
+    "gbc_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "gbc_server_error": (C.c_char_p, [C.c_void_p]),
+    "gbc_server_stop": (C.c_int, [C.c_void_p]),
     "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
@@ -123,17 +160,18 @@ def candidates():
 
 
 class Context:
-    """One gbc_ctx: sieving primes for `limit`, two slots of `max_batch`
-    segments of `segment_even` integers."""
+    """One gbc_ctx: sieving primes for `limit`, `nslots` slots of `max_batch`
+    segments of `segment_even` integers in at most `max_runs` runs."""
 
     def __init__(self, limit, segment_even=DEFAULT_SEGMENT, max_batch=8, tile_log2=0, p_mid=0, want_pn=False,
-                 device=0, large_pass_mb=0, hl_mode=0, mtab_max_gb=0, hl_pass_mb=0, sample_every=0,
-                 plan_funnels=0, ridge_min=0):
+                 device=0, max_runs=0, hl_mode=0, mtab_max_gb=0, nslots=0, sample_every=0,
+                 plan_funnels=0, ridge_min=0, launch_mode=0, selfcheck_every=0):
         self.lib = load()
         cfg = Config(limit=limit, segment_even=segment_even, max_batch=max_batch, tile_log2=tile_log2,
-                     p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, large_pass_mb=large_pass_mb,
-                     hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, hl_pass_mb=hl_pass_mb,
-                     sample_every=sample_every, plan_funnels=plan_funnels, ridge_min=ridge_min)
+                     p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, max_runs=max_runs,
+                     hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, nslots=nslots,
+                     sample_every=sample_every, plan_funnels=plan_funnels, ridge_min=ridge_min,
+                     launch_mode=launch_mode, selfcheck_every=selfcheck_every)
         h = C.c_void_p()
         rc = self.lib.gbc_create(C.byref(cfg), C.byref(h))
         self.h = h
@@ -165,6 +203,29 @@ class Context:
         f = (C.c_uint32 * n)(*flags) if flags else None
         self._check(self.lib.gbc_enqueue_batch(self.h, slot, b, f, n, limit))
 
+    def enqueue_segments(self, slot, segments, limits, flags=None):
+        """segments: [(seg_start, seg_end)] of any windows; limits: the last
+        even of each segment's window."""
+        n = len(segments)
+        b = (C.c_uint64 * (2 * n))(*[x for s in segments for x in s])
+        lim = (C.c_uint64 * n)(*limits)
+        f = (C.c_uint32 * n)(*flags) if flags else None
+        self._check(self.lib.gbc_enqueue_segments(self.h, slot, b, f, lim, n))
+
+    def poll(self, slot):
+        rc = self.lib.gbc_poll(self.h, slot)
+        if rc < 0:
+            self._check(rc)
+        return rc == 1
+
+    def prepare(self, lo, hi):
+        self._check(self.lib.gbc_prepare(self.h, lo, hi))
+
+    def stats(self):
+        st = CtxStats()
+        self._check(self.lib.gbc_get_stats(self.h, C.byref(st)))
+        return st
+
     def collect(self, slot, nseg, timeout_ms=600000):
         out = (SegmentResult * nseg)()
         t = BatchTimes()
@@ -176,13 +237,13 @@ class Context:
         self._check(self.lib.gbc_copy_pn(self.h, slot, seg, buf, evens))
         return buf
 
-    def map(self, slot):
-        """(base, nblk, wpc, words) of the slot's last collected class map;
-        words is a u32 array of 8 * wpc entries."""
+    def map(self, slot, run=0):
+        """(base, nblk, wpc, words) of a run's class map in the slot's last
+        collected batch; words is a u32 array of 8 * wpc entries."""
         base, nblk, wpc = C.c_uint64(), C.c_uint32(), C.c_uint32()
-        self._check(self.lib.gbc_map_info(self.h, slot, C.byref(base), C.byref(nblk), C.byref(wpc), None, 0))
+        self._check(self.lib.gbc_map_run(self.h, slot, run, C.byref(base), C.byref(nblk), C.byref(wpc), None, 0))
         words = (C.c_uint32 * (8 * wpc.value))()
-        self._check(self.lib.gbc_map_info(self.h, slot, None, None, None, words, len(words)))
+        self._check(self.lib.gbc_map_run(self.h, slot, run, None, None, None, words, len(words)))
         return base.value, nblk.value, wpc.value, words
 
     def stream(self, slot):
@@ -190,6 +251,22 @@ class Context:
 
     def launches(self):
         return self.lib.gbc_launch_count(self.h)
+
+    def verify_windows(self, windows, line_cap=1 << 16):
+        """[(RunResult, line)] of every window [(start, limit)], packed into
+        shared batches; also returns the WindowsSummary."""
+        n = len(windows)
+        b = (C.c_uint64 * (2 * n))(*[x for w in windows for x in w])
+        res = (RunResult * n)()
+        lines = C.create_string_buffer(n * line_cap)
+        summ = WindowsSummary()
+        self._check(self.lib.gbc_verify_windows(self.h, b, n, res, lines, line_cap, C.byref(summ)))
+        raw = lines.raw
+        out = []
+        for i in range(n):
+            chunk = raw[i * line_cap:(i + 1) * line_cap]
+            out.append((res[i], chunk[:chunk.index(b"\0")].decode()))
+        return out, summ
 
     def verify_range(self, start, limit, want_pn=False):
         """Returns (RunResult, stats_ref line, p(n) array or None)."""
@@ -200,6 +277,52 @@ class Context:
             pn = (C.c_uint16 * ((limit - start) // 2 + 1))()
         self._check(self.lib.gbc_verify_range(self.h, start, limit, C.byref(res), line, len(line), pn))
         return res, line.value.decode(), pn
+
+
+class Server:
+    """The serving loop (gbc_server_*) over a Context; the context must not
+    be used otherwise until stop()."""
+
+    def __init__(self, ctx, hbm_budget=0, lo=0, hi=0):
+        self.ctx, self.lib = ctx, ctx.lib
+        h = C.c_void_p()
+        ctx._check(self.lib.gbc_server_start(ctx.h, hbm_budget, lo, hi, C.byref(h)))
+        self.h = h
+
+    def _check(self, rc):
+        if rc:
+            raise GbcError(rc, self.lib.gbc_server_error(self.h).decode() if self.h else "no server")
+
+    def submit(self, start, limit):
+        i = C.c_uint64()
+        self._check(self.lib.gbc_server_submit(self.h, start, limit, C.byref(i)))
+        return i.value
+
+    def wait(self, ticket, timeout_ms=600000):
+        """(RunResult, line, latency in ms) of a submitted window."""
+        res = RunResult()
+        line = C.create_string_buffer(1 << 16)
+        lat = C.c_double()
+        self._check(self.lib.gbc_server_wait(self.h, ticket, timeout_ms, C.byref(res), line, len(line),
+                                             C.byref(lat)))
+        return res, line.value.decode(), lat.value
+
+    def stats(self):
+        st = ServerStats()
+        self._check(self.lib.gbc_server_get_stats(self.h, C.byref(st)))
+        return st
+
+    def stop(self):
+        if self.h:
+            rc = self.lib.gbc_server_stop(self.h)
+            self.h = None
+            self.ctx._check(rc)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()
 
 
 def segments_of(start, limit, segment_even):

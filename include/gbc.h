@@ -13,10 +13,12 @@
  * Terms: an "even" is an even n to verify; p(n) is the smallest odd prime p
  * with n - p prime (2 for n = 4). A "segment" is a run of consecutive evens
  * [seg_start, seg_end] (inclusive) whose statistics are reported together;
- * a "batch" is up to max_batch consecutive segments sieved in one pass over
- * one HBM-resident mod-30 class map. A "slot" is one of two independent sets
- * of device buffers, so batch k + 1 can be enqueued while batch k is being
- * collected.
+ * a "batch" is up to max_batch segments sieved and checked by one pass of
+ * the pipeline; its segments form "runs" (maximal sets of consecutive
+ * segments), each with its own HBM-resident mod-30 class map, so one batch
+ * can hold many windows of different widths and heights. A "slot" is one of
+ * nslots independent sets of device buffers with its own stream, so batch
+ * k + 1 can be enqueued while batch k is on the GPU or being collected.
  */
 #ifndef GBC_H
 #define GBC_H
@@ -58,21 +60,19 @@ extern "C" {
 typedef struct gbc_config {
     uint64_t limit;          /* largest even any batch will reach: sizes the sieving primes */
     uint64_t segment_even;   /* integer span of a full segment (default 467.5M) */
-    uint32_t max_batch;      /* segments per batch the slots are sized for (default 8) */
-    uint32_t tile_log2;      /* log2 of shared-memory tile bits per class (16..20, default 20) */
+    uint32_t max_batch;      /* segments per batch the slots are sized for (default 8, at most 256) */
+    uint32_t tile_log2;      /* log2 of shared-memory tile bits per class (14..20, default 20) */
     uint32_t p_mid;          /* primes <= p_mid: shared-memory tiles; above: large-prime kernel (default 2^22) */
     uint32_t want_pn;        /* 1: slots also hold a per-even u16 p(n) buffer */
     int32_t device;          /* CUDA device ordinal (default 0) */
-    uint32_t large_pass_mb;  /* class-map megabytes one pass of the large-prime kernel covers (default
-                                4096: one pass per batch; smaller passes keep the marks in L2 but repeat
-                                the per-prime setup) */
+    uint32_t max_runs;       /* runs per batch the slots are sized for (a run: consecutive segments
+                                with one class map; windows that do not touch are separate runs);
+                                default max_batch, at most max_batch */
     uint32_t hl_mode;        /* prime-multiplier hit lists: 0 auto (on when a batch spans >= 1e9
                                 integers), 1 on, 2 off */
     uint32_t mtab_max_gb;    /* HBM budget of the prime-multiplier table (default 48 GB); primes below
                                 limit / (30 * budget) keep the read-before-mark kernel */
-    uint32_t hl_pass_mb;     /* class-map megabytes one hit-list pass covers (default 4096: one pass;
-                                smaller passes keep the atomic marks in L2 but redo the per-prime
-                                divisions) */
+    uint32_t nslots;         /* independent slots (default 2, 2..GBC_MAX_SLOTS) */
     uint32_t sample_every;   /* run driver: every sample_every-th segment of a run (segment 0 always)
                                 gets p(n) of every even, the others the funnel verify + exact tail
                                 (GB_STATS_SAMPLE, include/gstats.hpp:62); 0 or 1: every segment
@@ -80,7 +80,16 @@ typedef struct gbc_config {
     uint32_t plan_funnels;   /* funnels per class of the verify plan (default 40) */
     uint32_t ridge_min;      /* evens with p(n) >= ridge_min are listed (default 3000,
                                 include/config.hpp:104 RIDGE_MIN_DEFAULT) */
+    uint32_t launch_mode;    /* 0 or 1: a batch is one replay of the slot's CUDA graph of the whole
+                                pipeline (captured at the slot's first batch); 2: the same kernels
+                                launched one by one */
+    uint32_t selfcheck_every;/* every selfcheck_every-th batch that uses hit lists rebuilds its maps
+                                without them and compares every word (src/verifier.cpp:2057-2112);
+                                a mismatch fails the batch closed. 0: never (default) */
+    uint32_t reserved[4];
 } gbc_config;
+
+#define GBC_MAX_SLOTS 8
 
 typedef struct gbc_ctx gbc_ctx;
 
@@ -130,6 +139,8 @@ typedef struct gbc_segment_result {
 /* Stage times of one batch (device events on the slot's stream). */
 typedef struct gbc_batch_times {
     float ms_setup, ms_tile, ms_large, ms_check, ms_count, ms_total;
+    float ms_selfcheck;      /* map self-check of this batch (0 when it had none) */
+    uint32_t runs;           /* class maps (runs) of the batch */
 } gbc_batch_times;
 
 /* Creates a context on cfg->device: the sieving primes up to
@@ -166,6 +177,21 @@ int gbc_candidates(uint16_t *out, int cap);
 int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags, int nseg,
                       uint64_t limit);
 
+/* Enqueues one batch of nseg segments of any windows on a slot, the batched
+ * form of gbc_enqueue_batch (the reference enqueues one segment per slot,
+ * src/verifier.cpp:1741-2146; here every stage is one persistent launch over
+ * all segments and runs of the batch). Segment i is [seg_bounds[2i],
+ * seg_bounds[2i+1]] with the same rules as above, and seg_limits[i] is the
+ * last even of the window it belongs to (its counts stop at seg_limits[i] -
+ * 1 when seg_end = seg_limits[i]). Segments that follow each other
+ * (seg_start[i] = seg_end[i-1] + 2) share one class map (a run); any other
+ * step starts a new run, so windows may overlap, repeat or come in any
+ * order. At most max_runs runs, and their maps must fit the slot's map
+ * buffer (max_batch full segments plus a small margin per run);
+ * GBC_E_ARG otherwise, with nothing enqueued. */
+int gbc_enqueue_segments(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const uint32_t *seg_flags,
+                         const uint64_t *seg_limits, int nseg);
+
 /* Waits (at most timeout_ms; < 0 waits without a limit) for the slot's
  * batch and copies its nseg results to host memory (collect_slot,
  * src/verifier.cpp:2402-2444). Fails closed with GBC_E_DEVICE on any device
@@ -173,6 +199,30 @@ int gbc_enqueue_batch(gbc_ctx *ctx, int slot, const uint64_t *seg_bounds, const 
  * times may be NULL. */
 int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int nseg, gbc_batch_times *times,
                 int timeout_ms);
+
+/* 1 when the slot's enqueued batch has finished on the GPU (gbc_collect
+ * will not wait), 0 while it runs or when the slot holds no batch, or a
+ * negative error (the reference polls its check event the same way,
+ * src/verifier.cpp:1847-1858). */
+int gbc_poll(gbc_ctx *ctx, int slot);
+
+/* Builds the prime-multiplier table for every batch whose evens lie in
+ * [lo, hi] now, so no later batch in that range rebuilds it (the reference
+ * builds its mtab once at start-up, src/verifier.cpp:1444-1508). Waits for
+ * every slot first. A no-op when hit lists are off or the table already
+ * covers the range. */
+int gbc_prepare(gbc_ctx *ctx, uint64_t lo, uint64_t hi);
+
+/* Counters of the context: launches of its kernels, batches, graph
+ * replays, map self-checks, prime-multiplier table builds and their time,
+ * and the device bytes the context holds. */
+typedef struct gbc_ctx_stats {
+    uint64_t launches, batches, graph_replays, selfchecks;
+    uint64_t mtab_builds, mtab_bytes;
+    double mtab_build_ms;
+    uint64_t device_bytes;
+} gbc_ctx_stats;
+int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out);
 
 /* Copies segment i's per-even p(n) of the last collected batch of the slot
  * (u16, index (n - seg_start) / 2; 2 for n = 4; 0 only for a counterexample)
@@ -183,15 +233,21 @@ int gbc_copy_pn(gbc_ctx *ctx, int slot, int seg, uint16_t *out, uint64_t evens);
  * without want_pn), for callers that keep results on the device. */
 const uint16_t *gbc_pn_device_ptr(gbc_ctx *ctx, int slot, int seg);
 
-/* The class map of the slot's last collected batch, for bit-exact
- * validation against an independent primality test (the reference's
- * debug_map validator, docs/PROJECT-REFERENCE.md:615-620): *base (q of
- * class-array bit 0 minus its residue, a multiple of 30), *nblk (bits per
- * class array in use) and *wpc (words per class array); when out is not
- * NULL, 8 * wpc words are copied to it (class k at out + k * wpc, bit t of
- * class k <-> q = base + 30 t + u_k, u = 1, 7, 11, 13, 17, 19, 23, 29). */
+/* The class map of the first run of the slot's last collected batch, for
+ * bit-exact validation against an independent primality test (the
+ * reference's debug_map validator, docs/PROJECT-REFERENCE.md:615-620):
+ * *base (q of class-array bit 0 minus its residue, a multiple of 30), *nblk
+ * (bits per class array in use) and *wpc (words per class array); when out
+ * is not NULL, 8 * wpc words are copied to it (class k at out + k * wpc,
+ * bit t of class k <-> q = base + 30 t + u_k, u = 1, 7, 11, 13, 17, 19, 23,
+ * 29). */
 int gbc_map_info(gbc_ctx *ctx, int slot, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
                  uint64_t out_words);
+
+/* The same for run `run` of the batch (runs numbered in segment order);
+ * GBC_E_ARG past the batch's last run. */
+int gbc_map_run(gbc_ctx *ctx, int slot, int run, uint64_t *base, uint32_t *nblk, uint32_t *wpc, uint32_t *out,
+                uint64_t out_words);
 
 /* The CUDA stream of a slot (a cudaStream_t), for callers that time or
  * order their own work against it. */
@@ -219,6 +275,72 @@ typedef struct gbc_run_result {
  * in flight, fail closed on any error. */
 int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gbc_run_result *res, char *line,
                      uint64_t line_cap, uint16_t *pn);
+
+/* ---- batched windows and the serving loop ---------------------------------
+ * Both pack the segments of many windows into shared batches (continuous
+ * batching over the context's slots): a window's segments go out in order,
+ * windows in arrival order, up to max_batch segments in up to max_runs runs
+ * per batch, up to nslots batches on the GPU at once. Each window's
+ * statistics are exactly those of a run of that window alone. */
+
+/* Totals of one gbc_verify_windows call. */
+typedef struct gbc_windows_summary {
+    uint64_t batches, segments, runs;
+    double gpu_seconds, wall_seconds;
+} gbc_windows_summary;
+
+/* Verifies nwin windows [bounds[2i], bounds[2i+1]] (each with the rules of
+ * gbc_verify_range, limit <= the context's limit) in shared batches. res
+ * (nwin entries or NULL) gets each window's counts (wall_seconds: from the
+ * call to the window's completion); lines (nwin * line_stride bytes or
+ * NULL) gets each window's line as gbc_verify_range writes it, window i at
+ * lines + i * line_stride; sum (or NULL) the call's totals. The reference
+ * has no such call: it runs windows one after another (run_gpu,
+ * src/verifier.cpp:2487-2569). */
+int gbc_verify_windows(gbc_ctx *ctx, const uint64_t *bounds, int nwin, gbc_run_result *res, char *lines,
+                       uint64_t line_stride, gbc_windows_summary *sum);
+
+/* A serving loop over one context: a worker thread owns the context (no
+ * other call may use it until gbc_server_stop), admits submitted windows
+ * in arrival order into batches as slots free up, and keeps the sieving
+ * primes and the prime-multiplier table resident. No counterpart in the
+ * reference (its service mode runs one range at a time). */
+typedef struct gbc_server gbc_server;
+
+typedef struct gbc_server_stats {
+    uint64_t submitted, completed, batches, segments, runs;
+    uint32_t max_in_flight;        /* most batches on the GPU at once */
+    uint32_t pad;
+    double gpu_seconds, wall_seconds;
+    uint64_t device_bytes;         /* device memory the context holds */
+    uint64_t hbm_budget;
+} gbc_server_stats;
+
+/* Starts the loop. The context's whole device footprint (slots, tables,
+ * and the prime-multiplier table built now for every window in [lo, hi];
+ * hi = 0: none) must fit hbm_budget bytes (0: no budget), else GBC_E_ARG.
+ * *out receives the server. */
+int gbc_server_start(gbc_ctx *ctx, uint64_t hbm_budget, uint64_t lo, uint64_t hi, gbc_server **out);
+
+/* Queues the window [start, limit] (rules of gbc_verify_range); *id
+ * receives its ticket. Any thread. */
+int gbc_server_submit(gbc_server *srv, uint64_t start, uint64_t limit, uint64_t *id);
+
+/* Waits at most timeout_ms (< 0: no limit) for window id, then writes its
+ * counts, its line (as gbc_verify_range) and the time from its submission
+ * to its completion; a ticket can be waited for once. Fails with the
+ * worker's error if the loop stopped on one (fail closed). */
+int gbc_server_wait(gbc_server *srv, uint64_t id, int timeout_ms, gbc_run_result *res, char *line,
+                    uint64_t line_cap, double *latency_ms);
+
+int gbc_server_get_stats(gbc_server *srv, gbc_server_stats *out);
+
+/* The worker's error text (empty when none). */
+const char *gbc_server_error(gbc_server *srv);
+
+/* Drains every queued window, stops the worker and frees the server; the
+ * context is the caller's again. Returns the worker's error, if any. */
+int gbc_server_stop(gbc_server *srv);
 
 /* ---- allocation-free class map ---------------------------------------------
  * This entry point has no counterpart in the reference.

@@ -1,0 +1,155 @@
+"""The batched forms on the GPU: many windows of different widths and
+heights in shared batches (one persistent launch per stage over all their
+runs and segments), the pipeline replayed as a CUDA graph against the same
+kernels launched one by one, the map self-check, and the serving loop with
+each result the same alone and in the mix.
+
+Everything is compared bit-exact: with the oracle's exact sieve (the
+stats_ref line of tests/stats_ref.cpp), with Miller-Rabin for every map bit,
+and with runs of each window alone through the plain per-range call.
+"""
+import random
+import threading
+
+import pytest
+
+import gbc
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+U30 = [1, 7, 11, 13, 17, 19, 23, 29]
+
+# windows at very different heights; two overlap, one is tiny, one starts at 6
+WINDOWS = [
+    (10**12, 10**12 + 2_400_000),
+    (4 * 10**18 + 123_456, 4 * 10**18 + 1_123_456),
+    (9223372036853775808, 9223372036853775808 + 600_000),
+    (10**15 + 2, 10**15 + 2_999_998),
+    (6, 150_000),
+    (10**12 + 1_000_000, 10**12 + 3_000_000),
+    (10**10, 10**10 + 10),
+    (gbc.MAX_LIMIT - 1_000_000, gbc.MAX_LIMIT),
+]
+
+
+@pytest.fixture(scope="module")
+def wctx():
+    with gbc.Context(limit=gbc.MAX_LIMIT, segment_even=1_000_000, max_batch=8, max_runs=8, nslots=3) as c:
+        yield c
+
+
+def test_windows_in_shared_batches_match_oracle(wctx):
+    """Every window's statistics from shared batches equal the oracle's."""
+    out, summ = wctx.verify_windows(WINDOWS)
+    assert summ.segments == sum(len(gbc.segments_of(a, b, 1_000_000)) for a, b in WINDOWS)
+    assert summ.batches < summ.segments  # segments of different windows shared batches
+    for (a, b), (res, line) in zip(WINDOWS, out):
+        assert line == oracle.stats_line(a, b, oracle.SIEVE), (a, b)
+
+
+def test_windows_equal_alone(wctx):
+    """The same window alone (the plain per-range call) gives the same line."""
+    out, _ = wctx.verify_windows(WINDOWS[::-1])
+    for (a, b), (_, line) in zip(WINDOWS[::-1], out):
+        assert line == wctx.verify_range(a, b)[1], (a, b)
+
+
+def test_runs_class_maps_bit_exact():
+    """Three runs at three heights in one batch: every bit of every run's
+    class map against Miller-Rabin."""
+    segs = [(10**12, 10**12 + 299_998), (10**12 + 300_000, 10**12 + 599_998),
+            (4 * 10**18, 4 * 10**18 + 299_998), (2**63 + 10**6, 2**63 + 10**6 + 299_998)]
+    limits = [10**12 + 599_998, 10**12 + 599_998, 4 * 10**18 + 299_998, 2**63 + 10**6 + 299_998]
+    with gbc.Context(limit=gbc.MAX_LIMIT, segment_even=300_000, max_batch=4, max_runs=4, hl_mode=1,
+                     mtab_max_gb=8, p_mid=1 << 18) as c:
+        c.enqueue_segments(0, segs, limits)
+        res, t = c.collect(0, len(segs))
+        assert t.runs == 3
+        for run in range(3):
+            base, nblk, wpc, w = c.map(0, run)
+            bad = [base + 30 * t + U30[k] for k in range(8) for t in range(nblk)
+                   if ((w[k * wpc + (t >> 5)] >> (t & 31)) & 1) != oracle.is_prime(base + 30 * t + U30[k])]
+            assert not bad, (run, bad[:8])
+        with pytest.raises(gbc.GbcError):
+            c.map(0, 3)
+
+
+def test_graph_replay_equals_direct_launches():
+    """launch_mode 1 (graph per slot) and 2 (kernels one by one) agree, and
+    the graph path really replays."""
+    a, b = 4 * 10**18, 4 * 10**18 + 8_000_000
+    lines = []
+    for mode in (1, 2):
+        with gbc.Context(limit=b, segment_even=1_000_000, max_batch=4, hl_mode=1, mtab_max_gb=8,
+                         launch_mode=mode) as c:
+            lines.append(c.verify_range(a, b)[1])
+            st = c.stats()
+            assert st.batches == 3
+            assert st.graph_replays == (3 if mode == 1 else 0)
+    assert lines[0] == lines[1] == oracle.stats_line(a, b, oracle.SIEVE)
+
+
+def test_map_selfcheck_runs_and_passes():
+    """Every batch rebuilt without hit lists and compared word for word."""
+    a, b = 9 * 10**18, 9 * 10**18 + 6_000_000
+    with gbc.Context(limit=b, segment_even=1_000_000, max_batch=2, hl_mode=1, mtab_max_gb=8,
+                     selfcheck_every=1) as c:
+        line = c.verify_range(a, b)[1]
+        st = c.stats()
+    assert st.selfchecks == st.batches == 4
+    assert line == oracle.stats_line(a, b, oracle.SIEVE)
+
+
+def test_prepare_builds_the_table_once():
+    with gbc.Context(limit=5 * 10**18, segment_even=1_000_000, max_batch=4, hl_mode=1, mtab_max_gb=16) as c:
+        c.prepare(10**16, 5 * 10**18)
+        assert c.stats().mtab_builds == 1
+        for a in (10**16, 10**17 + 8, 3 * 10**18, 5 * 10**18 - 4_000_000):
+            c.verify_range(a, a + 3_000_000)
+        assert c.stats().mtab_builds == 1
+
+
+def serving_windows(n, seed):
+    rnd = random.Random(seed)
+    out = []
+    for _ in range(n):
+        a = int(10 ** rnd.uniform(10, 18.6)) // 2 * 2
+        w = int(10 ** rnd.uniform(4, 6.5)) // 2 * 2
+        out.append((a, a + w))
+    return out
+
+
+@pytest.mark.parametrize("sample_every", [1, 2])
+def test_server_results_same_alone_and_in_the_mix(sample_every):
+    """Windows submitted from several threads while others are on the GPU:
+    each window's line equals its line alone (bit-exact, no tolerance), and
+    several batches were in flight at once."""
+    wins = serving_windows(40, 11 + sample_every)
+    with gbc.Context(limit=gbc.MAX_LIMIT, segment_even=1_000_000, max_batch=8, nslots=4,
+                     sample_every=sample_every) as c:
+        got = {}
+        with gbc.Server(c, hbm_budget=150 * 10**9) as srv:
+            tickets = {}
+
+            def submit(part):
+                for w in part:
+                    tickets[w] = srv.submit(*w)
+
+            th = [threading.Thread(target=submit, args=(wins[i::4],)) for i in range(4)]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            for w, tk in tickets.items():
+                got[w] = srv.wait(tk)
+            st = srv.stats()
+        assert st.completed == len(wins)
+        assert st.segments >= len(wins)
+        for w in wins:
+            res, line, lat = got[w]
+            assert lat > 0
+            assert line == c.verify_range(*w)[1], w
+        for w in wins[:4]:
+            if sample_every == 1:
+                assert got[w][1] == oracle.stats_line(w[0], w[1], oracle.SIEVE)
