@@ -1,11 +1,12 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 dense Goldbach verify path.
 
-Workload: production segments of 467.5M integers at 4e18 + k * 467.5e6, k
-drawn from seed 1 in [0, 1e5) (the reference's production segment shape).
-A step is one batch of --batch consecutive segments (default 16: one sieve
-pass over one HBM-resident class map of 250 MB, then per segment the
-checker, prime / twin / gap statistics and the class-map hash). Successive
+Headline workload: production segments of 467.5M integers at 4e18 + k *
+467.5e6, k drawn from seed 1 in [0, 1e5) (the reference's production
+segment shape). A step is one batch of --batch consecutive segments
+(default 16: one sieve pass over one HBM-resident class map of 250 MB,
+then per segment the checker, prime / twin / gap statistics and the
+class-map hash), replayed as the slot's captured CUDA graph. Successive
 steps take successive batches, so no step repeats work, and a step's map
 and sieving primes (393 MB) exceed L2.
 
@@ -22,6 +23,19 @@ value  = evens verified per second over the timed steps, device time from
 e2e    = the same metric through the C ABI as a caller uses it: two slots in
          flight, gbc_enqueue_batch + gbc_collect, per-segment results copied
          to host memory inside the timed region, wall clock.
+plain  = the plain per-segment form on the same GPU: one segment per batch,
+         two slots in flight, kernels launched one by one; batched_over_plain
+         is value / plain.value.
+windows = 256 windows of log-uniform widths in [1e6, 1e10] at uniform starts
+         in [1e15, 5e18] (seed 7) verified in shared batches, against the same
+         windows run one at a time; every window's statistics compared.
+serving = Poisson arrivals at 50 windows/s for 60 s (seed 11), widths
+         log-uniform in [1e4, 1e9], starts log-uniform in [1e10, 5e18], served
+         by the continuous-batching loop under a 150 GB HBM budget: p50 / p99
+         latency from submission to completion, sustained evens/s, and a
+         sample of windows compared with their runs alone.
+--slice runs the full 5e13-wide slice at 4e18 batched and plain, and checks
+3 seeded segments against the CPU oracle.
 --impl reference times the reference's CPU algorithm (the oracle's
 restatement of tests/stats_ref.cpp: Miller-Rabin p(n) of every even, run on
 every host core) on a bounded sample of the same workload.
@@ -42,7 +56,7 @@ sys.path.insert(0, os.path.join(ROOT, "goldbach-l0_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 SEG = 467_500_000
-METRIC = "G evens/s at 4e18, bit-exact stats"
+METRIC = "G evens/s at 4e18, bit-exact stats: batched vs plain on 1 GB300; p99 latency"
 NPRIMES_4E18 = 98_222_287   # odd primes <= 2.0e9 = sqrt of the workload's end
 
 
@@ -189,6 +203,179 @@ def device_run(ctx, bs, limit, sample_every, gbc):
     return total, stage
 
 
+def plain_leg(gbc, start, nseg, first_seg, knobs=None):
+    """The plain per-segment form: batches of one segment, kernels launched
+    one by one (no graph), the prime-multiplier table built once before
+    timing. value: device time of nseg segments back to back on one slot
+    (CUDA events, as the batched value); e2e: wall time of the next nseg
+    segments with two slots in flight, the reference's double-buffered
+    loop."""
+    segs = [(start + i * SEG, start + i * SEG + SEG - 2) for i in range(first_seg, first_seg + 2 * nseg + 1)]
+    limit = segs[-1][1]
+    k = {n: v for n, v in (knobs or {}).items() if n in ("p_mid", "mtab_max_gb", "tile_log2", "plan_funnels")}
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=1, launch_mode=2, hl_mode=1, **k) as ctx:
+        for sl in (0, 1):                                     # warm-up: tables, both slots
+            ctx.enqueue_batch(sl, [segs[0]], limit, [gbc.SEG_VERIFY])
+            ctx.collect(sl, 1)
+        dev_ms = 0.0
+        for s in segs[1:1 + nseg]:
+            ctx.enqueue_batch(0, [s], limit, [gbc.SEG_VERIFY])
+            _, t = ctx.collect(0, 1)
+            dev_ms += t.ms_total
+        todo = segs[1 + nseg:]
+        t0 = time.perf_counter()
+        for i in range(min(2, nseg)):
+            ctx.enqueue_batch(i, [todo[i]], limit, [gbc.SEG_VERIFY])
+        for i in range(nseg):
+            ctx.collect(i & 1, 1)
+            if i + 2 < nseg:
+                ctx.enqueue_batch(i & 1, [todo[i + 2]], limit, [gbc.SEG_VERIFY])
+        wall = time.perf_counter() - t0
+    evens = nseg * (SEG // 2)
+    return {"value": evens / (dev_ms / 1e3) / 1e9, "unit": "G evens/s",
+            "e2e": {"value": evens / wall / 1e9, "unit": "G evens/s"}, "segments": nseg,
+            "config": "one production segment per batch, kernels launched one by one, funnel verify + exact tail, "
+                      "hit lists on (table built before timing), the batched form's other knobs; value: one slot, "
+                      "device events; e2e: two slots in flight, wall clock"}
+
+
+def log_uniform(rnd, lo, hi):
+    import math
+    return math.exp(rnd.uniform(math.log(lo), math.log(hi)))
+
+
+def windows_leg(gbc, n=256, seed=7):
+    """Batched uneven windows against the same windows one at a time."""
+    rnd = random.Random(seed)
+    wins = []
+    for _ in range(n):
+        w = int(log_uniform(rnd, 1e6, 1e10)) // 2 * 2
+        a = int(rnd.uniform(1e15, 5e18)) // 2 * 2
+        wins.append((a, a + w))
+    limit = max(b for _, b in wins)
+    evens = sum((b - a) // 2 + 1 for a, b in wins)
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3) as ctx:
+        ctx.prepare(min(a for a, _ in wins), limit)
+        ctx.verify_windows(wins[:4])                               # warm-up: graphs
+        t0 = time.perf_counter()
+        out, summ = ctx.verify_windows(wins)
+        wall = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        alone = [ctx.verify_range(a, b)[1] for a, b in wins]
+        wall_alone = time.perf_counter() - t0
+        same = sum(1 for (_, line), al in zip(out, alone) if line == al)
+        st = ctx.stats()
+    return {"value": evens / wall / 1e9, "unit": "G evens/s", "windows": n, "evens": evens,
+            "batches": summ.batches, "segments": summ.segments, "runs": summ.runs, "wall_s": wall,
+            "alone": {"value": evens / wall_alone / 1e9, "wall_s": wall_alone},
+            "batched_over_alone": wall_alone / wall, "bit_exact_vs_alone": f"{same}/{n}",
+            "mtab_gb": st.mtab_bytes / 1e9,
+            "config": f"{n} windows, widths log-uniform [1e6, 1e10], starts uniform [1e15, 5e18], seed {seed}, "
+                      f"p(n) of every even, 16 segments / 16 runs per batch, 3 slots"}
+
+
+def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64):
+    """Poisson arrivals into the serving loop; latency = submission to
+    completion of each window."""
+    rnd = random.Random(seed)
+    reqs, t = [], 0.0
+    while True:
+        t += rnd.expovariate(rate)
+        if t > seconds:
+            break
+        w = int(log_uniform(rnd, 1e4, 1e9)) // 2 * 2
+        a = int(log_uniform(rnd, 1e10, 5e18)) // 2 * 2
+        reqs.append((t, a, a + max(w, 2)))
+    limit = max(b for _, _, b in reqs)
+    evens = sum((b - a) // 2 + 1 for _, a, b in reqs)
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=4) as ctx:
+        with gbc.Server(ctx, hbm_budget=150 * 10**9, lo=10**10, hi=limit) as srv:
+            warm = [srv.submit(a, b) for _, a, b in reqs[:16]]      # warm-up: graphs of every slot
+            for tk in warm:
+                srv.wait(tk)
+            tickets = [None] * len(reqs)
+
+            def feeder():
+                t0 = time.perf_counter()
+                for i, (ta, a, b) in enumerate(reqs):
+                    d = ta - (time.perf_counter() - t0)
+                    if d > 0:
+                        time.sleep(d)
+                    tickets[i] = srv.submit(a, b)
+
+            th = threading.Thread(target=feeder)
+            t0 = time.perf_counter()
+            th.start()
+            lat, lines = [], []
+            for i in range(len(reqs)):
+                while tickets[i] is None:
+                    time.sleep(0.0005)
+                _, line, ms = srv.wait(tickets[i])
+                lat.append(ms)
+                lines.append(line)
+            wall = time.perf_counter() - t0
+            th.join()
+            st = srv.stats()
+        pick = random.Random(seed + 1).sample(range(len(reqs)), min(check, len(reqs)))
+        same = sum(1 for i in pick if ctx.verify_range(reqs[i][1], reqs[i][2])[1] == lines[i])
+    lat.sort()
+
+    def q(x):
+        return lat[min(len(lat) - 1, int(x * len(lat)))]
+    return {"p50_ms": q(0.50), "p99_ms": q(0.99), "max_ms": lat[-1], "mean_ms": sum(lat) / len(lat),
+            "requests": len(reqs), "rate_per_s": rate, "seconds": seconds, "evens": evens,
+            "sustained": {"value": evens / wall / 1e9, "unit": "G evens/s"},
+            "batches": st.batches, "segments": st.segments, "runs": st.runs,
+            "max_batches_in_flight": st.max_in_flight, "gpu_busy_s": st.gpu_seconds,
+            "device_gb": st.device_bytes / 1e9, "hbm_budget_gb": st.hbm_budget / 1e9,
+            "bit_exact_vs_alone": f"{same}/{len(pick)}",
+            "config": f"Poisson {rate}/s for {seconds} s (seed {seed}), widths log-uniform [1e4, 1e9], starts "
+                      f"log-uniform [1e10, 5e18], p(n) of every even, 4 slots, 16 segments / 16 runs per batch, "
+                      f"latency from submission to the window's merged statistics"}
+
+
+def slice_mode(args):
+    """The full 5e13 slice at 4e18, batched and plain, 3 seeded segments
+    against the CPU oracle."""
+    import gbc
+    import oracle
+    a = 4 * 10**18
+    b = a + 5 * 10**13
+    segs = gbc.segments_of(a, b, SEG)
+    evens = (b - a) // 2 + 1
+    import autotune
+    knobs = autotune.load(args.tuning or autotune.DEFAULT_RECORD) if args.tuning != "none" else None
+    knobs = knobs or {"max_batch": args.batch}
+    args.batch = knobs["max_batch"]
+    with gbc.Context(limit=b, segment_even=SEG, sample_every=args.sample_every, **knobs) as ctx:
+        ctx.prepare(a, b)
+        res, line, _ = ctx.verify_range(a, b)
+        st = ctx.stats()
+    plain = plain_leg(gbc, a, args.plain_segments, 0, knobs)
+    pick = sorted(random.Random(3).sample(range(len(segs)), 3))
+    checks = []
+    with gbc.Context(limit=b, segment_even=SEG, max_batch=1) as ctx:
+        for i in pick:
+            s, e = segs[i]
+            t0 = time.perf_counter()
+            got = ctx.verify_range(s, e)[1]
+            t1 = time.perf_counter()
+            want = oracle.stats_line(s, e, oracle.SIEVE)
+            checks.append({"segment": i, "start": s, "end": e, "bit_exact": got == want,
+                           "oracle_s": time.perf_counter() - t1, "gpu_wall_s": t1 - t0})
+    # the run keeps two batches in flight, so its value is wall-clock
+    # throughput through gbc_verify_range, against the plain form's e2e
+    out = {"metric": METRIC + " (full 5e13 slice)", "value": evens / res.wall_seconds / 1e9, "unit": "G evens/s",
+           "segments": len(segs), "batches": res.batches, "wall_s": res.wall_seconds,
+           "mtab_build_ms": st.mtab_build_ms, "plain": plain,
+           "batched_over_plain": (evens / res.wall_seconds / 1e9) / plain["e2e"]["value"],
+           "oracle_segments": checks, "gbstats": line,
+           "config": {"workload": f"[{a}, {b}]", "segments_per_batch": args.batch,
+                      "sample_every": args.sample_every}}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -206,9 +393,17 @@ def main():
     ap.add_argument("--cpu-evens", type=int, default=4_000_000)
     ap.add_argument("--exact-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-segments", type=int, default=48)
+    ap.add_argument("--windows", type=int, default=256)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--slice", action="store_true")
+    ap.add_argument("--tuning", default="", help="autotuner record (default: the committed one); 'none': defaults")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.slice:
+        return slice_mode(args)
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
         print(json.dumps({"error": "one GPU per process: run N independent replicas for N > 1"}))
         return 2
@@ -216,12 +411,22 @@ def main():
 
     start = workload_start()
     nb = args.warmup + 2 * args.steps + 2 + args.exact_steps
+    # knobs: the autotuner's record when there is one (goldbach-l0_gb300/autotune.py),
+    # command-line values otherwise
+    knobs = {"max_batch": args.batch, "tile_log2": args.tile_log2, "p_mid": args.p_mid,
+             "plan_funnels": args.plan_funnels}
+    tuned = None
+    if args.tuning != "none":
+        import autotune
+        tuned = autotune.load(args.tuning or autotune.DEFAULT_RECORD)
+        if tuned:
+            knobs.update(tuned)
+    args.batch = knobs["max_batch"]
     allb = batches(start, 0, nb, args.batch)
     limit = allb[-1][-1][2]
     evens_per_step = sum((e - s) // 2 + 1 for _, s, e in allb[0])
-    with gbc.Context(limit=limit, segment_even=SEG, max_batch=args.batch, tile_log2=args.tile_log2,
-                     p_mid=args.p_mid, hl_mode=args.hl_mode, launch_mode=args.launch_mode,
-                     plan_funnels=args.plan_funnels) as ctx:
+    with gbc.Context(limit=limit, segment_even=SEG, hl_mode=args.hl_mode, launch_mode=args.launch_mode,
+                     **knobs) as ctx:
         device_run(ctx, allb[:args.warmup], limit, args.sample_every, gbc)   # warm-up (builds the tables)
         launches0 = ctx.launches()
         timed = allb[args.warmup:args.warmup + args.steps]
@@ -282,7 +487,10 @@ def main():
                             f"+ exact p(n) >= plan bound; primes, twins, gap walk, map hash on every segment",
                    "l2": "inputs larger than L2: 250 MB class map + 393 MB sieving primes per step",
                    "tile_log2": cfg.tile_log2, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
-                   "plan_funnels": cfg.plan_funnels},
+                   "mtab_max_gb": cfg.mtab_max_gb, "plan_funnels": cfg.plan_funnels,
+                   "launch": "graph replay" if cfg.launch_mode != 2 else "direct launches",
+                   "tuning": ("autotuner record " + os.path.relpath(args.tuning or autotune.DEFAULT_RECORD, ROOT))
+                   if tuned else "defaults"},
         "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
         "wall_ms_per_step": wall * 1e3 / args.steps,
         "exact_all": {"value": exact_all, "unit": "G evens/s",
@@ -296,6 +504,14 @@ def main():
                      "ms_per_launch": stage_bw[dom]["ms_per_launch"], "stages": stage_bw},
         "clocks": clk.summary(),
     }
+    if args.plain_segments:
+        out["plain"] = plain_leg(gbc, start, args.plain_segments, nb * args.batch, knobs)
+        out["batched_over_plain"] = {"device": value / out["plain"]["value"],
+                                     "e2e": e2e / out["plain"]["e2e"]["value"]}
+    if args.windows:
+        out["windows"] = windows_leg(gbc, args.windows)
+    if args.serve_seconds > 0:
+        out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.cpu_evens, start)
     print(json.dumps(out))

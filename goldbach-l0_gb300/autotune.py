@@ -1,0 +1,135 @@
+"""Autotuner of the batched form (the knobs the reference fixes by hand in
+include/config.hpp: SMEM tile size, the tile / large-prime split, the
+hit-list split through the prime-multiplier table's budget, segments per
+batch, and the verify plan's funnel count).
+
+Coordinate descent on calibration batches of the workload: from the
+defaults, each knob in turn takes the value with the highest throughput
+while the others stay fixed, for two rounds. Every trial verifies the same
+consecutive production segments (192 of them, whole batches for every
+batch size tried), timed on the device with the pipeline's own CUDA events, one
+slot, after a warm-up batch that builds the tables. The record holds every
+trial and the choice; callers (bench.py, the serving setup) load it with
+`load()`.
+
+    python goldbach-l0_gb300/autotune.py --start 4000008233142500000 \\
+        --out goldbach-l0_gb300/tuning/gb300_production_4e18.json
+"""
+import argparse
+import datetime
+import json
+import os
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import gbc  # noqa: E402
+
+SEG = 467_500_000
+KNOBS = {
+    "p_mid": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
+    "mtab_max_gb": [48, 96, 160],
+    "tile_log2": [19, 20],
+    "max_batch": [16, 32, 48, 64],
+    "plan_funnels": [24, 32, 40],
+}
+DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 40}
+DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")
+
+
+def measure(knobs, start, nseg=192, sample_every=256):
+    """Device throughput (G evens/s) of nseg production segments from start
+    under the given knobs; segment i gets p(n) of every even when i is a
+    multiple of sample_every, else the funnel verify + exact tail."""
+    mb = knobs["max_batch"]
+    segs = [(start + i * SEG, start + i * SEG + SEG - 2) for i in range(nseg + mb)]
+    limit = segs[-1][1]
+    flags = [0 if i % sample_every == 0 else gbc.SEG_VERIFY for i in range(len(segs))]
+    with gbc.Context(limit=limit, segment_even=SEG, **knobs) as ctx:
+        ctx.enqueue_batch(0, segs[:mb], limit, flags[:mb])        # warm-up: tables and the slot's graph
+        ctx.collect(0, mb)
+        ms = 0.0
+        for b in range(mb, mb + nseg, mb):
+            ctx.enqueue_batch(0, segs[b:b + mb], limit, flags[b:b + mb])
+            _, t = ctx.collect(0, mb)
+            ms += t.ms_total
+    return nseg * (SEG // 2) / (ms / 1e3) / 1e9
+
+
+def gpu_name():
+    try:
+        return subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                              capture_output=True, text=True, timeout=20).stdout.strip()
+    except Exception:
+        return "unknown"
+
+
+def tune(start, rounds=2, nseg=192, log=print):
+    best = dict(DEFAULTS)
+    trials = []
+    cache = {}
+
+    def run(k):
+        key = tuple(sorted(k.items()))
+        if key not in cache:
+            t0 = time.perf_counter()
+            v = measure(k, start, nseg)
+            cache[key] = v
+            trials.append({"knobs": dict(k), "g_evens_s": v, "seconds": time.perf_counter() - t0})
+            log(f"  {k} -> {v:.2f} G evens/s")
+        return cache[key]
+
+    base = run(best)
+    for r in range(rounds):
+        changed = False
+        for name, values in KNOBS.items():
+            scores = {}
+            for v in values:
+                k = dict(best)
+                k[name] = v
+                scores[v] = run(k)
+            pick = max(scores, key=scores.get)
+            if pick != best[name]:
+                best[name] = pick
+                changed = True
+        if not changed:
+            break
+    return {"gpu": gpu_name(), "date": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
+            "workload": {"start": start, "segment": SEG, "segments": nseg, "sample_every": 256,
+                         "what": "consecutive production segments, funnel verify + exact tail, every 256th "
+                                 "segment p(n) of every even"},
+            "method": "coordinate descent over the knobs, two rounds, device time of the pipeline's events",
+            "defaults": DEFAULTS, "default_g_evens_s": base,
+            "choice": best, "choice_g_evens_s": cache[tuple(sorted(best.items()))], "trials": trials}
+
+
+def load(path=DEFAULT_RECORD):
+    """The recorded choice (a dict of Context keyword arguments), or None."""
+    try:
+        with open(path) as f:
+            return dict(json.load(f)["choice"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--start", type=int, default=4000008233142500000)
+    ap.add_argument("--segments", type=int, default=192)
+    ap.add_argument("--rounds", type=int, default=2)
+    ap.add_argument("--out", default=DEFAULT_RECORD)
+    a = ap.parse_args()
+    rec = tune(a.start, a.rounds, a.segments)
+    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    with open(a.out, "w") as f:
+        json.dump(rec, f, indent=1)
+    print(json.dumps({"choice": rec["choice"], "g_evens_s": rec["choice_g_evens_s"],
+                      "default_g_evens_s": rec["default_g_evens_s"], "trials": len(rec["trials"])}))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -19,6 +19,8 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -153,6 +155,31 @@ std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n)
     out.reserve(tot);
     for (auto &p : parts) out.insert(out.end(), p.begin(), p.end());
     return out;
+}
+
+// The odd primes <= n, shared by the contexts of a process: the last list
+// sieved is kept and a smaller bound takes a prefix of it.
+static std::vector<uint32_t> cached_primes(uint64_t n)
+{
+    static std::mutex mu;
+    static std::shared_ptr<const std::vector<uint32_t>> last;
+    static uint64_t last_n = 0;
+    std::shared_ptr<const std::vector<uint32_t>> have;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (last && last_n >= n) have = last;
+    }
+    if (!have) {
+        auto fresh = std::make_shared<const std::vector<uint32_t>>(gbh_odd_primes_upto(n));
+        std::lock_guard<std::mutex> lk(mu);
+        if (!last || last_n < n) {
+            last = fresh;
+            last_n = n;
+        }
+        have = fresh;
+    }
+    const auto end = std::upper_bound(have->begin(), have->end(), n);
+    return std::vector<uint32_t>(have->begin(), end);
 }
 
 static int fail(gbc_ctx *c, int code, const std::string &msg)
@@ -295,7 +322,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     // (the reference's base_prime_bound, include/primes.hpp:222-225)
     const double rt = std::sqrt(double(cfg.limit + 3)) + 16.0;
     const uint64_t bound = rt >= 4294967295.0 ? 0xFFFFFFFFull : uint64_t(rt);
-    ctx->primes = gbh_odd_primes_upto(std::max<uint64_t>(bound, 127));
+    ctx->primes = cached_primes(std::max<uint64_t>(bound, 127));
     const auto &pr = ctx->primes;
     ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
     ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());

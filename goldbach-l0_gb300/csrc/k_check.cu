@@ -313,9 +313,9 @@ constexpr uint32_t kMaxFun = 256;  // funnels per class the verify kernel holds
 // shifted by 0..d bits, so one 96-bit read tests up to five candidates for
 // 32 evens. No statistics here: evens left without a plan witness go to a
 // pending list of (class, word, bits) for k_tail.
-__global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchDesc d, VerifyTables vt)
+__global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
 {
-    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | top member << 21 | mask << 24
+    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member shifts << 21
     __shared__ uint32_t s_win[kCheckWarps][8 * kVWin];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
@@ -369,7 +369,11 @@ __global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchDesc d, Verify
             const uint32_t mask = e >> 16, p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(mask);
             const uint32_t u = (r + 30 - p0 % 30) % 30;
             const uint32_t dd = uint32_t((n0 - base - p0 - u) / 30) - dm - dlo;
-            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (dm << 21) | (mask << 24);
+            // member d's window starts dm - d bits above the top member's
+            uint32_t sm = 0;
+            for (uint32_t d = 0; d <= dm; ++d)
+                if ((mask >> d) & 1u) sm |= 1u << (dm - d);
+            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (sm << 21);
         }
         __syncthreads();
 
@@ -386,24 +390,22 @@ __global__ void __launch_bounds__(kCheckThreads, 6) k_verify(BatchDesc d, Verify
             uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
             const uint32_t *wl = win + lane;
             for (uint32_t f = 0; f < nfun; ++f) {
-                if (!__any_sync(~0u, uA | uB)) break;
+                if ((f & 3) == 0 && !__any_sync(~0u, uA | uB)) break;
                 const uint32_t e = s_fent[f];
                 const uint32_t *w = wl + (e & 0xFFFF);
-                const uint32_t sh = (e >> 16) & 31, dm = (e >> 21) & 7, mask = e >> 24;
+                const uint32_t sh = (e >> 16) & 31, sm = e >> 21;
                 const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
-                uint32_t wa = 0, wb = 0;
+                // the top member's 64-bit window; every other member's is
+                // the same shifted down by 1..4 bits (bit s of sm)
+                const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
+                const uint32_t bl = __funnelshift_r(y0, y1, sh), bh = __funnelshift_r(y1, y2, sh);
+                uint32_t wa = al, wb = bl;
 #pragma unroll
-                for (uint32_t dd = 0; dd <= 4; ++dd) {
-                    if (!((mask >> dd) & 1u)) continue;
-                    const uint32_t a = sh + dm - dd;  // member dd's window starts a bits into the read
-                    if (a < 32) {
-                        wa |= __funnelshift_r(x0, x1, a);
-                        wb |= __funnelshift_r(y0, y1, a);
-                    } else {
-                        wa |= __funnelshift_r(x1, x2, a - 32);
-                        wb |= __funnelshift_r(y1, y2, a - 32);
+                for (uint32_t k = 1; k <= 4; ++k)
+                    if ((sm >> k) & 1u) {
+                        wa |= __funnelshift_r(al, ah, k);
+                        wb |= __funnelshift_r(bl, bh, k);
                     }
-                }
                 uA &= ~wa;
                 uB &= ~wb;
             }
