@@ -99,7 +99,8 @@ class Clocks:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,"
+                 "temperature.gpu",
                  "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -127,7 +128,10 @@ class Clocks:
         mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        mem = [float(r[8]) for r in self.rows if len(r) > 8 and r[8].replace(".", "").isdigit()]
+        temp = [float(r[9]) for r in self.rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "mem_mhz": statistics.median(mem) if mem else None, "temp_c": max(temp) if temp else None,
                 "reasons": reasons, "samples": len(self.rows)}
 
 
@@ -387,6 +391,7 @@ def main():
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--p-mid", type=int, default=0)
     ap.add_argument("--hl-mode", type=int, default=0)
+    ap.add_argument("--mtab-gb", type=int, default=0)
     ap.add_argument("--launch-mode", type=int, default=0)
     ap.add_argument("--plan-funnels", type=int, default=0)
     ap.add_argument("--ref-evens", type=int, default=1_000_000)
@@ -414,7 +419,7 @@ def main():
     # knobs: the autotuner's record when there is one (goldbach-l0_gb300/autotune.py),
     # command-line values otherwise
     knobs = {"max_batch": args.batch, "tile_log2": args.tile_log2, "p_mid": args.p_mid,
-             "plan_funnels": args.plan_funnels}
+             "plan_funnels": args.plan_funnels, "mtab_max_gb": args.mtab_gb}
     tuned = None
     if args.tuning != "none":
         import autotune
@@ -455,7 +460,7 @@ def main():
         # p(n) of every even on every segment
         exb = allb[off + args.steps + 2:off + args.steps + 2 + args.exact_steps]
         ex_ms, ex_stage = device_run(ctx, exb, limit, 1, gbc)
-        exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9
+        exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9 if exb else None
         cfg = ctx.cfg
     hbm, kind = peaks()
     # per stage: launches per step and algorithmic HBM bytes per launch
@@ -494,7 +499,7 @@ def main():
         "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
         "wall_ms_per_step": wall * 1e3 / args.steps,
         "exact_all": {"value": exact_all, "unit": "G evens/s",
-                      "stage_ms_per_step": {k: v / len(exb) for k, v in ex_stage.items()}},
+                      "stage_ms_per_step": {k: v / len(exb) for k, v in ex_stage.items()} if exb else None},
         "e2e": {"value": e2e, "unit": "G evens/s", "h2d_bytes_per_step": 16 * args.batch,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

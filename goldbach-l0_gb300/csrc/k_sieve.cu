@@ -379,15 +379,24 @@ __device__ __forceinline__ uint32_t inv_mod_2_32(uint32_t p)
 // and no read is needed.
 __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
 {
-    // class array of q = p m from the classes of p and of m
-    __shared__ uint8_t s_cls[8][8];
+    // per (class of p, class of m): the class kq of q = p m, its residue
+    // u_kq and u_m, as kq | u_kq << 8 | u_m << 16; the class of a residue
+    __shared__ uint32_t s_cls[8][8];
+    __shared__ uint8_t s_res[32];
     if (threadIdx.x < 64) {
         const uint32_t a = threadIdx.x >> 3, b = threadIdx.x & 7;
-        s_cls[a][b] = uint8_t(class_of(unit30(a) * unit30(b) % 30));
+        const uint32_t uq = unit30(a) * unit30(b) % 30;
+        s_cls[a][b] = class_of(uq) | (uq << 8) | (unit30(b) << 16);
+    } else if (threadIdx.x < 96) {
+        s_res[threadIdx.x - 64] = uint8_t(class_of(threadIdx.x - 64));
     }
     __syncthreads();
     const uint32_t nrun = d.h->nrun;
     if (!nrun) return;
+    // bit r set for the units r mod 30: the classes below a residue
+    constexpr uint32_t kUnits = (1u << 1) | (1u << 7) | (1u << 11) | (1u << 13) | (1u << 17) | (1u << 19) |
+                                (1u << 23) | (1u << 29);
+    constexpr uint32_t kInv15 = 0xEEEEEEEFu;  // 15^-1 mod 2^32
     const uint32_t *primes = d.runs[0].primes;
     const uint32_t nhi = d.h->n_all_max;
     for (uint32_t i = d.h->n_hl_min + blockIdx.x * blockDim.x + threadIdx.x; i < nhi;
@@ -395,15 +404,18 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
         const uint32_t p = primes[i];
         const float rp = __frcp_rn(float(p));
         const uint32_t pinv = inv_mod_2_32(p);
-        const uint32_t kp = class_of(p % 30);
+        const uint32_t kp = s_res[p % 30];
         for (uint32_t ri = 0; ri < nrun; ++ri) {
             const BatchParams &bp = d.runs[ri];
             if (i < bp.n_hl || i >= bp.n_all) continue;
-            const uint64_t base = bp.base, q1 = base + 30ull * bp.nblk - 1;
-            uint32_t r0, r1;
-            uint64_t mlo = divmod_u64(base, p, rp, pinv, r0);
-            mlo += r0 ? 1 : 0;
-            const uint64_t mhi = divmod_u64(q1, p, rp, pinv, r1);
+            const uint64_t base = bp.base;
+            // m in [ceil(base / p), floor(q1 / p)], q1 = base + span: the
+            // second quotient from the first and a division of r0 + span < 2^37
+            uint32_t r0;
+            const uint64_t qb = divmod_u64(base, p, rp, pinv, r0);
+            const uint64_t x = uint64_t(r0) + (30ull * bp.nblk - 1);
+            const uint32_t r1 = mod_below(x, p, rp);
+            const uint64_t mlo = qb + (r0 ? 1 : 0), mhi = qb + uint32_t(x - r1) * pinv;
             if (mhi < mlo) continue;
             const uint64_t m0 = bp.m0;
             if (mlo < m0 || mhi > bp.m1) {
@@ -413,17 +425,35 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
             uint32_t *map = bp.map;
             const uint32_t wpc = bp.wpc;
             const uint32_t *mtab = bp.mtab;
+            // table bytes b0..b1; in the end bytes only the classes inside [mlo, mhi]
             const uint64_t b0 = (mlo - m0) / 30, b1 = (mhi - m0) / 30;
-            for (uint64_t w = b0 >> 2; w <= (b1 >> 2); ++w) {
-                uint32_t v = mtab[w];
+            const uint32_t dl = uint32_t(mlo - m0 - 30 * b0), dh = uint32_t(mhi - m0 - 30 * b1);
+            const uint32_t lo_byte = (0xFFu << __popc(kUnits & ((1u << dl) - 1u))) & 0xFFu;
+            const uint32_t hi_byte = (1u << __popc(kUnits & ((2u << dh) - 1u))) - 1u;
+            const uint64_t w0 = b0 >> 2, w1 = b1 >> 2;
+            const uint32_t lo_mask = (0xFFFFFFFFu << (8 * (b0 & 3))) & ~(0xFFu << (8 * (b0 & 3))) |
+                                     (lo_byte << (8 * (b0 & 3)));
+            const uint32_t hi_shift = 8 * uint32_t(b1 & 3);
+            const uint32_t hi_mask = (hi_shift ? (0xFFFFFFFFu >> (32 - hi_shift)) : 0u) | (hi_byte << hi_shift);
+            // q - base - u_q = xw + p (30 jb + u_m) - u_q for byte jb of word
+            // w, xw = p (m0 + 120 w) - base: a multiple of 30 below 2^64, and
+            // the class bit t = that / 30 < 2^31, so its low 32 bits suffice:
+            // bits 1..32 of it times 15^-1 mod 2^32
+            const uint32_t *tw = mtab + w0;
+            const uint32_t nw = uint32_t(w1 - w0);
+            const uint64_t step = 120ull * p;
+            uint64_t xw = uint64_t(p) * m0 - base + step * w0;
+            for (uint32_t iw = 0; iw <= nw; ++iw, xw += step) {
+                uint32_t v = __ldg(tw + iw);
+                if (iw == 0) v &= lo_mask;
+                if (iw == nw) v &= hi_mask;
                 while (v) {
                     const uint32_t j = __ffs(v) - 1u;
                     v &= v - 1u;
-                    const uint32_t k = j & 7;
-                    const uint64_t m = m0 + 30 * (4 * w + (j >> 3)) + unit30(k);
-                    if (m < mlo || m > mhi) continue;
-                    const uint64_t t = (uint64_t(p) * m - base) / 30;
-                    atomicAnd(map + size_t(s_cls[kp][k]) * wpc + (t >> 5), ~(1u << (t & 31)));
+                    const uint32_t e = s_cls[kp][j & 7];
+                    const uint64_t xq = xw + uint64_t(p) * (30u * (j >> 3) + (e >> 16)) - ((e >> 8) & 0xFFu);
+                    const uint32_t t = uint32_t(xq >> 1) * kInv15;
+                    atomicAnd(map + size_t(e & 0xFFu) * wpc + (t >> 5), ~(1u << (t & 31)));
                 }
             }
         }
