@@ -74,18 +74,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from profiles/ncu_traffic.txt (one
-    ncu capture of the same workload; lines "kernel bytes_per_launch note")."""
+def ncu_counters():
+    """kernel -> (DRAM bytes, warp instructions) per launch from
+    profiles/ncu_counters.txt (one-pass ncu captures of the headline
+    workload; lines "kernel dram_bytes warp_inst note")."""
+    out = {}
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.txt")) as f:
+        with open(os.path.join(ROOT, "profiles", "ncu_counters.txt")) as f:
             for ln in f:
                 t = ln.split()
-                if len(t) >= 2 and t[0] == kernel:
-                    return float(t[1])
+                if len(t) >= 3 and not ln.startswith("#"):
+                    out[t[0]] = (float(t[1]), float(t[2]))
     except OSError:
         pass
-    return None
+    return out
 
 
 class Clocks:
@@ -462,25 +464,50 @@ def main():
         ex_ms, ex_stage = device_run(ctx, exb, limit, 1, gbc)
         exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9 if exb else None
         cfg = ctx.cfg
+        cst = ctx.stats()
     hbm, kind = peaks()
-    # per stage: launches per step and algorithmic HBM bytes per launch
-    seg_map = 8 * (SEG / 30) / 8                        # a segment's class map: one bit per q coprime to 30
+    # The dominant kernel of each stage and its algorithmic bytes per launch
+    # (one launch per batch: the kernels are persistent over the batch's
+    # segments). A segment's class map is one bit per q coprime to 30:
+    # SEG / 30 bytes. The hit-list stage reads its primes once and makes one
+    # 4-byte read-modify-write per semiprime mark (the marks counted by the
+    # density of q = p m, p >= p_hl, m prime) plus the table bytes of the
+    # primes' multiplier ranges.
+    import math
+    seg_map = SEG / 30
+    W = args.batch * SEG
+    q_top = float(limit)
+    p_max = math.sqrt(q_top)
+    p_hl = float(cst.p_hl) if cst.p_hl else p_max
+    L, u0, u1 = math.log(q_top), math.log(p_hl), math.log(p_max)
+    marks = W * math.log(u1 * (L - u0) / (u0 * (L - u1))) / L if u1 > u0 else 0.0
+    n_hl = NPRIMES_4E18 - p_hl / (math.log(p_hl) - 1.08366) if u1 > u0 else 0.0
+    table_bytes = W / 30 * math.log(u1 / u0) if u1 > u0 else 0.0
     per_stage = {
-        "tile": (1, seg_map * args.batch),              # one write of the batch's map
-        "large": (1, 4 * NPRIMES_4E18),                 # the sieving-prime stream (hit lists / large primes)
-        "check": (args.batch, seg_map),                 # one read of the segment's map
-        "count": (args.batch, seg_map),                 # one read of the segment's map
+        "tile": ("k_tile", args.batch * seg_map),                     # one write of the batch's maps
+        "large": ("k_hitlist", 4 * n_hl + 8 * marks + table_bytes),   # primes + marks + table ranges
+        "check": ("k_verify", args.batch * seg_map),                  # one read of the maps
+        "count": ("k_count", args.batch * seg_map),                   # one read of the maps
     }
-    kernels = {"tile": "k_tile", "large": "k_hitlist", "check": "k_verify", "count": "k_count"}
+    counters = ncu_counters()
+    sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+    issue_peak = cst.sm_count * 4 * sm_mhz * 1e6                    # warp instructions per second
     stage_bw = {}
-    for s, (nl, b) in per_stage.items():
-        ms = stage[s] / args.steps / nl
-        stage_bw[s] = {"kernel": kernels[s], "ms_per_launch": ms, "alg_bytes_per_launch": b,
-                       "achieved_gbs": b / (ms / 1e3) / 1e9 if ms > 0 else None}
+    for s_, (kern, b) in per_stage.items():
+        ms = stage[s_] / args.steps
+        row = {"kernel": kern, "ms_per_launch": ms, "alg_bytes_per_launch": b,
+               "achieved_gbs": b / (ms / 1e3) / 1e9 if ms > 0 else None,
+               "frac_hbm": b / (ms / 1e3) / 1e9 / hbm if ms > 0 else None}
+        c = counters.get(kern)
+        if c:
+            row["ncu_dram_bytes_per_launch"] = c[0]
+            row["ncu_warp_inst_per_launch"] = c[1]
+            row["issue_frac"] = c[1] / (ms / 1e3) / issue_peak if ms > 0 else None
+        stage_bw[s_] = row
     dom = max(stage, key=stage.get)                     # the stage with the most device time per step
-    kernel = kernels[dom]
+    kernel = per_stage[dom][0]
     achieved = stage_bw[dom]["achieved_gbs"]
-    traffic = ncu_traffic(kernel)
+    traffic = counters.get(kernel, (None,))[0]
     out = {
         "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -490,7 +517,8 @@ def main():
                    "segments_per_step": args.batch, "evens_per_step": evens_per_step,
                    "stats": f"every {args.sample_every}th segment p(n) of every even, the others funnel verify "
                             f"+ exact p(n) >= plan bound; primes, twins, gap walk, map hash on every segment",
-                   "l2": "inputs larger than L2: 250 MB class map + 393 MB sieving primes per step",
+                   "l2": f"inputs larger than L2: {args.batch * SEG / 30 / 1e6:.0f} MB of class maps + 393 MB "
+                         f"of sieving primes per step",
                    "tile_log2": cfg.tile_log2, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
                    "mtab_max_gb": cfg.mtab_max_gb, "plan_funnels": cfg.plan_funnels,
                    "launch": "graph replay" if cfg.launch_mode != 2 else "direct launches",
@@ -506,7 +534,8 @@ def main():
         "roofline": {"bound": "hbm", "kernel": kernel, "stage": dom, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic, "peak_kind": kind,
                      "alg_bytes_per_launch": stage_bw[dom]["alg_bytes_per_launch"],
-                     "ms_per_launch": stage_bw[dom]["ms_per_launch"], "stages": stage_bw},
+                     "ms_per_launch": stage_bw[dom]["ms_per_launch"],
+                     "issue_peak_warp_inst_per_s": issue_peak, "stages": stage_bw},
         "clocks": clk.summary(),
     }
     if args.plain_segments:

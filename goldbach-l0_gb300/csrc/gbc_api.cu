@@ -537,6 +537,9 @@ extern "C" int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out)
     out->mtab_bytes = ctx->mtab_bytes;
     out->mtab_build_ms = ctx->mtab_build_ms;
     out->device_bytes = ctx->device_bytes;
+    out->p_hl = ctx->hl_on ? ctx->p_hl : 0;
+    out->sm_count = uint32_t(ctx->grids.sm);
+    out->pad = 0;
     return GBC_OK;
 }
 

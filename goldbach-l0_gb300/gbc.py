@@ -64,7 +64,8 @@ class BatchTimes(C.Structure):
 class CtxStats(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("batches", C.c_uint64), ("graph_replays", C.c_uint64),
                 ("selfchecks", C.c_uint64), ("mtab_builds", C.c_uint64), ("mtab_bytes", C.c_uint64),
-                ("mtab_build_ms", C.c_double), ("device_bytes", C.c_uint64)]
+                ("mtab_build_ms", C.c_double), ("device_bytes", C.c_uint64), ("p_hl", C.c_uint64),
+                ("sm_count", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class RunResult(C.Structure):

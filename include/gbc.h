@@ -221,6 +221,9 @@ typedef struct gbc_ctx_stats {
     uint64_t mtab_builds, mtab_bytes;
     double mtab_build_ms;
     uint64_t device_bytes;
+    uint64_t p_hl;            /* first hit-listed prime (0: hit lists off) */
+    uint32_t sm_count;        /* multiprocessors of the context's device */
+    uint32_t pad;
 } gbc_ctx_stats;
 int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out);
 
