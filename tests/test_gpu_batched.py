@@ -153,3 +153,45 @@ def test_server_results_same_alone_and_in_the_mix(sample_every):
         for w in wins[:4]:
             if sample_every == 1:
                 assert got[w][1] == oracle.stats_line(w[0], w[1], oracle.SIEVE)
+
+
+def test_plain_1e12_window_config_c1():
+    """All evens in [1e12, 1e12 + 1e9] through the plain form (one segment
+    per batch, tile + mid stages only at this height) against the oracle's
+    exact sieve: the whole stats_ref line (every p(n), primes, twins, gaps)."""
+    a, b = 10**12, 10**12 + 10**9
+    with gbc.Context(limit=b, segment_even=100_000_000, max_batch=1, launch_mode=2) as c:
+        res, line, _ = c.verify_range(a, b)
+        assert c.stats().p_hl == 0  # no hit lists below 1e13
+    assert res.evens == 500_000_001
+    assert line == oracle.stats_line(a, b, oracle.SIEVE)
+
+
+def uneven_windows(n=256, seed=7):
+    """The batched uneven-window workload: widths log-uniform in [1e6, 1e10],
+    starts uniform in [1e15, 5e18], both even (seed 7)."""
+    import math
+    rnd = random.Random(seed)
+    out = []
+    for _ in range(n):
+        w = int(math.exp(rnd.uniform(math.log(1e6), math.log(1e10)))) // 2 * 2
+        a = int(rnd.uniform(1e15, 5e18)) // 2 * 2
+        out.append((a, a + w))
+    return out
+
+
+def test_uneven_windows_sampled_against_oracle_config_c4():
+    """All 256 windows in shared batches; 8 sampled windows (seed 8, among
+    those under 2e7 wide so the oracle finishes in seconds) against the
+    oracle's exact sieve, every window against its run alone."""
+    wins = uneven_windows()
+    small = [i for i, (a, b) in enumerate(wins) if b - a < 2 * 10**7]
+    pick = random.Random(8).sample(small, 8)
+    limit = max(b for _, b in wins)
+    with gbc.Context(limit=limit, segment_even=gbc.DEFAULT_SEGMENT, max_batch=16, max_runs=16, nslots=3) as c:
+        out, summ = c.verify_windows(wins)
+        assert summ.runs >= 256 and summ.batches < summ.segments
+        for i in pick:
+            assert out[i][1] == oracle.stats_line(wins[i][0], wins[i][1], oracle.SIEVE), wins[i]
+        for i in random.Random(9).sample(range(len(wins)), 16):
+            assert out[i][1] == c.verify_range(*wins[i])[1], wins[i]
