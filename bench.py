@@ -93,8 +93,9 @@ def ncu_counters():
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
-    def __init__(self):
+    def __init__(self, index=None):
         self.rows, self.proc = [], None
+        self.index = str(index) if index is not None else os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
 
     def __enter__(self):
         try:
@@ -103,7 +104,7 @@ class Clocks:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,"
                  "temperature.gpu",
-                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "--format=csv,noheader,nounits", "-i", self.index,
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -135,6 +136,41 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "mem_mhz": statistics.median(mem) if mem else None, "temp_c": max(temp) if temp else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+class Replicas:
+    """N independent replicas (python -m torch.distributed.run ...
+    bench.py --gpus N): rank r verifies its own consecutive segments on GPU
+    LOCAL_RANK. The path shards by segment with no exchange, so the only
+    communication is host-side: a barrier on both sides of the timed
+    region and the max over ranks of the time (gloo)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist and self.dist.is_initialized():
+            self.dist.destroy_process_group()
 
 
 def batches(start, first_seg, nbatch, batch):
@@ -411,9 +447,14 @@ def main():
         return run_reference(args)
     if args.slice:
         return slice_mode(args)
-    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
-        print(json.dumps({"error": "one GPU per process: run N independent replicas for N > 1"}))
-        return 2
+    rep = Replicas()
+    try:
+        return run_gb300(args, rep)
+    finally:
+        rep.close()
+
+
+def run_gb300(args, rep):
     import gbc
 
     start = workload_start()
@@ -429,38 +470,44 @@ def main():
         if tuned:
             knobs.update(tuned)
     args.batch = knobs["max_batch"]
-    allb = batches(start, 0, nb, args.batch)
+    # rank r: its own consecutive segments, after those of the ranks below
+    allb = batches(start, rep.rank * nb * args.batch, nb, args.batch)
     limit = allb[-1][-1][2]
     evens_per_step = sum((e - s) // 2 + 1 for _, s, e in allb[0])
     with gbc.Context(limit=limit, segment_even=SEG, hl_mode=args.hl_mode, launch_mode=args.launch_mode,
-                     **knobs) as ctx:
+                     device=rep.local, **knobs) as ctx:
         device_run(ctx, allb[:args.warmup], limit, args.sample_every, gbc)   # warm-up (builds the tables)
         launches0 = ctx.launches()
         timed = allb[args.warmup:args.warmup + args.steps]
-        with Clocks() as clk:
+        rep.barrier()
+        with Clocks(rep.local) as clk:
             t0 = time.perf_counter()
             dev_ms, stage = device_run(ctx, timed, limit, args.sample_every, gbc)
             wall = time.perf_counter() - t0
+        rep.barrier()
+        dev_ms = rep.max(dev_ms)
+        wall = rep.max(wall)
         launches = ctx.launches() - launches0
-        value = evens_per_step * args.steps / (dev_ms / 1e3) / 1e9
+        value = rep.world * evens_per_step * args.steps / (dev_ms / 1e3) / 1e9
         # e2e: the caller's loop, two slots in flight, results to host memory
         off = args.warmup + args.steps
         e2eb = allb[off:off + args.steps]
+        rep.barrier()
+        t0 = time.perf_counter()
         for i in range(min(2, args.steps)):
             segs, flags = seg_args(e2eb[i], args.sample_every, gbc)
             ctx.enqueue_batch(i, segs, limit, flags)
-        t0 = time.perf_counter()
         for i in range(args.steps):
             slot = i & 1
             ctx.collect(slot, len(e2eb[i]))
             if i + 2 < args.steps:
                 segs, flags = seg_args(e2eb[i + 2], args.sample_every, gbc)
                 ctx.enqueue_batch(slot, segs, limit, flags)
-        e2e_wall = time.perf_counter() - t0
-        e2e = evens_per_step * args.steps / e2e_wall / 1e9
+        e2e_wall = rep.max(time.perf_counter() - t0)
+        e2e = rep.world * evens_per_step * args.steps / e2e_wall / 1e9
         d2h = args.batch * ctypes.sizeof(gbc.SegmentResult)
         # p(n) of every even on every segment
-        exb = allb[off + args.steps + 2:off + args.steps + 2 + args.exact_steps]
+        exb = allb[off + args.steps + 2:off + args.steps + 2 + args.exact_steps] if rep.world == 1 else []
         ex_ms, ex_stage = device_run(ctx, exb, limit, 1, gbc)
         exact_all = evens_per_step * len(exb) / (ex_ms / 1e3) / 1e9 if exb else None
         cfg = ctx.cfg
@@ -509,12 +556,15 @@ def main():
     achieved = stage_bw[dom]["achieved_gbs"]
     traffic = counters.get(kernel, (None,))[0]
     out = {
-        "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": rep.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"production segments of {SEG} integers from {start} (4e18 + k*467.5e6, k seed 1), "
                                f"{args.batch} segments per step",
                    "segments_per_step": args.batch, "evens_per_step": evens_per_step,
+                   "parallelism": f"{rep.world} independent replicas (each rank its own segments, "
+                                  f"a barrier and a max over ranks of the time; no collective)"
+                   if rep.world > 1 else "one GPU",
                    "stats": f"every {args.sample_every}th segment p(n) of every even, the others funnel verify "
                             f"+ exact p(n) >= plan bound; primes, twins, gap walk, map hash on every segment",
                    "l2": f"inputs larger than L2: {args.batch * SEG / 30 / 1e6:.0f} MB of class maps + 393 MB "
@@ -538,6 +588,11 @@ def main():
                      "issue_peak_warp_inst_per_s": issue_peak, "stages": stage_bw},
         "clocks": clk.summary(),
     }
+    if rep.world > 1:
+        # N independent replicas: the headline and e2e legs only, rank 0 reports
+        if rep.rank == 0:
+            print(json.dumps(out))
+        return 0
     if args.plain_segments:
         out["plain"] = plain_leg(gbc, start, args.plain_segments, nb * args.batch, knobs)
         out["batched_over_plain"] = {"device": value / out["plain"]["value"],
