@@ -216,6 +216,34 @@ extern "C" int gbc_candidates(uint16_t *out, int cap)
 // checkers' window reads, rounded to 32 words (128-byte aligned maps)
 static uint64_t run_wpc(uint64_t nblk) { return align_up((nblk + 64 + 31) / 32, 32); }
 
+// Expected hit-list marks per class bit of a run whose q reach qmax: the
+// density among integers of q = p m with p a prime in [p_hl, p_max] and m
+// prime, 1 / L * ln(u1 (L - u0) / (u0 (L - u1))) (L = ln q, u = ln p; the
+// sum over p of 1 / (p ln(q / p)) with the prime density 1 / ln), times
+// 30 / 8 (every such q is coprime to 30).
+static double hl_density(double qmax, double p_hl, double p_max)
+{
+    const double L = std::log(qmax), u0 = std::log(p_hl), u1 = std::log(std::min(p_max, std::sqrt(qmax)));
+    if (u1 <= u0) return 0;
+    return std::log(u1 * (L - u0) / (u0 * (L - u1))) / L * 30.0 / 8.0;
+}
+
+// Region bins of a one-run batch: regions of 2^rlog class bits (at least
+// 2^28, so that all of k_hl_apply's CTAs share one region of <= 32 MB of one
+// class at a time), at most kHlMaxBins / 8 per class.
+static void hl_regions(uint64_t nblk, uint32_t &rlog, uint32_t &nreg)
+{
+    rlog = 28;
+    while (((nblk + (uint64_t(1) << rlog) - 1) >> rlog) > gbk::kHlMaxBins / 8) ++rlog;
+    nreg = uint32_t((nblk + (uint64_t(1) << rlog) - 1) >> rlog);
+}
+
+// Offsets per (harvest CTA, bin): the expected marks + 25%, + 64, whole lines.
+static uint32_t hl_quota(double marks, uint32_t ctas, uint32_t nbin)
+{
+    return uint32_t(align_up(size_t(1.25 * marks / (double(ctas) * nbin)) + 64, 32));
+}
+
 static int slot_alloc(gbc_ctx *ctx, Slot &s)
 {
     const auto &cfg = ctx->cfg;
@@ -237,6 +265,19 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
     // leaves ~1e-4 of the evens; an overflow fails the batch closed)
     s.pend_cap = uint32_t(std::max<uint64_t>(4096, (cfg.segment_even / 2 / 32 + 64) / 16));
     CK(dev_alloc(ctx, &s.pend, size_t(cfg.max_batch) * s.pend_cap * sizeof(uint2)));
+    if (ctx->hl_on) {
+        // binned hit lists for a one-run batch of max_batch full segments at
+        // the density of the context's top
+        const uint64_t nblk = uint64_t(ctx->wpc_cap) * 32;
+        uint32_t rlog, nreg;
+        hl_regions(nblk, rlog, nreg);
+        const uint32_t ctas = uint32_t(ctx->grids.sm) * gbh::kHitlistCtasPerSm;
+        const double marks = 8.0 * double(nblk) *
+                             hl_density(double(cfg.limit) + 3, double(ctx->p_hl), double(ctx->primes.back()));
+        s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks, ctas, 8 * nreg);
+        CK(dev_alloc(ctx, &s.hl_buf, std::max<size_t>(s.hl_buf_words, 1) * 4));
+        CK(dev_alloc(ctx, &s.hl_cnt, size_t(ctas) * gbk::kHlMaxBins * 4));
+    }
     CK(cudaMallocHost(&s.desc_host, ctx->layout.bytes));
     std::memset(s.desc_host, 0, ctx->layout.bytes);
     CK(dev_alloc(ctx, &s.desc_dev, ctx->layout.bytes));
@@ -259,6 +300,8 @@ static void slot_free(Slot &s)
     cudaFree(s.pn);
     cudaFree(s.pend);
     cudaFree(s.desc_dev);
+    cudaFree(s.hl_buf);
+    cudaFree(s.hl_cnt);
     if (s.desc_host) cudaFreeHost(s.desc_host);
     cudaFree(s.chk_map);
     cudaFree(s.chk_desc_dev);
@@ -676,6 +719,25 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
     }
     img.h->nrun = nrun;
     img.h->nseg = uint32_t(nseg);
+    // a batch of one hit-listed run: marks binned by map region
+    if (nrun == 1 && s.hl_buf && img.runs[0].n_hl < img.runs[0].n_all) {
+        gbk::BatchParams &bp = img.runs[0];
+        uint32_t rlog, nreg;
+        hl_regions(bp.nblk, rlog, nreg);
+        const uint32_t ctas = uint32_t(ctx->grids.sm) * gbh::kHitlistCtasPerSm, nbin = 8 * nreg;
+        const double marks = 8.0 * double(bp.nblk) *
+                             hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
+                                        double(ctx->primes[bp.n_all - 1]));
+        const uint32_t quota = hl_quota(marks, ctas, nbin);
+        if (size_t(ctas) * nbin * quota <= s.hl_buf_words) {
+            bp.hl_buf = s.hl_buf;
+            bp.hl_cnt = s.hl_cnt;
+            bp.hl_quota = quota;
+            bp.hl_rlog = rlog;
+            bp.hl_nreg = nreg;
+            bp.hl_ctas = ctas;
+        }
+    }
     finish_desc(ctx, img);
     return GBC_OK;
 }
@@ -818,7 +880,8 @@ extern "C" int gbc_prepare(gbc_ctx *ctx, uint64_t lo, uint64_t hi)
 
 // The pipeline of one batch on the slot's stream (the same calls are
 // captured into the slot's graph): descriptor upload, result init, first
-// bits, tiles | large primes, hit lists | checker | counts.
+// bits, tiles | large primes, hit lists (filed by region, then applied
+// region by region) | checker | counts.
 static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
 {
     cudaStream_t st = s.st;
@@ -832,6 +895,7 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     CK(cudaEventRecordWithFlags(s.ev[1], st, rec));
     gbh::launch_large(d, g, st);
     gbh::launch_hitlist(d, g, st);
+    gbh::launch_hl_apply(d, g, st);
     CK(cudaEventRecordWithFlags(s.ev[2], st, rec));
     gbh::launch_check(d, ctx->ct, g, st);
     gbh::launch_verify(d, ctx->vt, g, st);
@@ -842,7 +906,7 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     return GBC_OK;
 }
 
-constexpr int kPipelineKernels = 11;
+constexpr int kPipelineKernels = 12;
 
 static int capture_slot(gbc_ctx *ctx, Slot &s)
 {
@@ -885,6 +949,7 @@ static int issue_selfcheck(gbc_ctx *ctx, Slot &s)
         gbk::BatchParams &bp = ci.runs[r];
         bp.map = s.chk_map + (bp.map - s.map);
         bp.n_hl = bp.n_all;
+        bp.hl_quota = 0;
     }
     ci.h->n_hl_max = ci.h->n_all_max;
     ci.h->n_hl_min = ci.h->n_all_max;

@@ -85,6 +85,13 @@ struct BatchParams {
     const uint32_t *mtab;     // bit k of byte i <-> m = m0 + 30 i + u_k is prime
     uint64_t m0, m1;          // the table covers m in [m0, m1]
     uint32_t bm1, bm2;        // base mod 1001 and mod 7429
+    // binned hit lists (a batch of one run): the harvest files each mark's
+    // offset in its (harvest CTA, region bin) quota, bin = class * hl_nreg +
+    // (t >> hl_rlog); k_hl_apply clears them region by region. hl_quota = 0:
+    // marks are cleared directly.
+    uint32_t *hl_buf;         // hl_ctas * hl_nbin * hl_quota offsets
+    uint32_t *hl_cnt;         // hl_ctas * hl_nbin counts (capped at the quota when read)
+    uint32_t hl_quota, hl_rlog, hl_nreg, hl_ctas;
 };
 
 struct GroupInfo {
@@ -136,14 +143,15 @@ struct BatchHeader {
     uint32_t n_hl_min, n_all_max;  // hit-listed primes: [n_hl_min, n_all_max)
     uint32_t chk_vb, ver_vb, cnt_vb; // virtual CTAs of k_check, k_verify, k_count
     uint32_t nlow;                 // segments that need the generic low checker
-    uint32_t pad[3];
+    uint32_t pad[2];
     // work counters of the persistent kernels (CTAs take their next item
     // with an atomic add); zero in the host image, so every batch's
     // descriptor copy resets them
-    uint32_t work[4];
+    uint32_t work[5];
 };
 
-constexpr int kWorkTile = 0, kWorkCheck = 1, kWorkVerify = 2, kWorkCount = 3;
+constexpr int kWorkTile = 0, kWorkCheck = 1, kWorkVerify = 2, kWorkCount = 3, kWorkHlApply = 4;
+constexpr uint32_t kHlMaxBins = 64;  // region bins of a binned batch (8 classes x up to 8 regions)
 
 struct BatchDesc {
     const BatchHeader *h;
@@ -290,6 +298,8 @@ void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t til
                  cudaStream_t st);
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_hl_apply(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+constexpr int kHitlistCtasPerSm = 8;  // k_hitlist's grid: SMs x this
 void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st);
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st);
 void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st);

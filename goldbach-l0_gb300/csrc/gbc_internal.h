@@ -47,6 +47,10 @@ struct Slot {
     uint64_t pn_stride = 0;
     uint2 *pend = nullptr;             // max_batch * pend_cap phase-A pending words
     uint32_t pend_cap = 0;
+    // binned hit lists of one-run batches (k_hitlist's CTAs x region bins x quota)
+    uint32_t *hl_buf = nullptr;
+    size_t hl_buf_words = 0;
+    uint32_t *hl_cnt = nullptr;
     // the batch descriptor: pinned host image, device copy
     uint8_t *desc_host = nullptr, *desc_dev = nullptr;
     DescImage img;

@@ -390,9 +390,16 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
     } else if (threadIdx.x < 96) {
         s_res[threadIdx.x - 64] = uint8_t(class_of(threadIdx.x - 64));
     }
+    __shared__ uint32_t s_hcnt[kHlMaxBins];
+    if (threadIdx.x < kHlMaxBins) s_hcnt[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t nrun = d.h->nrun;
     if (!nrun) return;
+    // a batch of one run files its marks in region bins (see k_hl_apply)
+    const BatchParams &r0 = d.runs[0];
+    const uint32_t quota = nrun == 1 ? r0.hl_quota : 0u;
+    const uint32_t rlog = r0.hl_rlog, nreg = r0.hl_nreg, nbin = 8 * nreg;
+    uint32_t *const hl_mine = quota ? r0.hl_buf + size_t(blockIdx.x) * nbin * quota : nullptr;
     // bit r set for the units r mod 30: the classes below a residue
     constexpr uint32_t kUnits = (1u << 1) | (1u << 7) | (1u << 11) | (1u << 13) | (1u << 17) | (1u << 19) |
                                 (1u << 23) | (1u << 29);
@@ -453,10 +460,51 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
                     const uint32_t e = s_cls[kp][j & 7];
                     const uint64_t xq = xw + uint64_t(p) * (30u * (j >> 3) + (e >> 16)) - ((e >> 8) & 0xFFu);
                     const uint32_t t = uint32_t(xq >> 1) * kInv15;
+                    if (quota) {
+                        const uint32_t bin = (e & 0xFFu) * nreg + (t >> rlog);
+                        const uint32_t pos = atomicAdd(&s_hcnt[bin], 1u);
+                        if (pos < quota) {
+                            hl_mine[size_t(bin) * quota + pos] = t & ((1u << rlog) - 1u);
+                            continue;
+                        }
+                    }
                     atomicAnd(map + size_t(e & 0xFFu) * wpc + (t >> 5), ~(1u << (t & 31)));
                 }
             }
         }
+    }
+    if (quota) {
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < nbin; b += blockDim.x) r0.hl_cnt[blockIdx.x * nbin + b] = s_hcnt[b];
+    }
+}
+
+// Binned hit lists, applied: every CTA's marks of region bin 0 first (all
+// CTAs of the kernel on one map region of at most 2^28 bits of one class at
+// a time), then bin 1, ..., so the atomic ANDs find their words in L2
+// instead of making a DRAM read-modify-write each.
+__global__ void __launch_bounds__(256) k_hl_apply(BatchDesc d)
+{
+    __shared__ uint32_t s_j;
+    if (d.h->nrun != 1) return;
+    const BatchParams &bp = d.runs[0];
+    const uint32_t quota = bp.hl_quota;
+    if (!quota) return;
+    const uint32_t nreg = bp.hl_nreg, nbin = 8 * nreg, ctas = bp.hl_ctas, rlog = bp.hl_rlog;
+    const uint32_t items = nbin * ctas, wpc = bp.wpc;
+    for (;;) {
+        const uint32_t j = next_item(d.work + kWorkHlApply, &s_j);
+        if (j >= items) break;
+        const uint32_t bin = j / ctas, c = j - bin * ctas;
+        const uint32_t k = bin / nreg, reg = bin - k * nreg;
+        const uint32_t n = min(bp.hl_cnt[size_t(c) * nbin + bin], quota);
+        const uint32_t *e = bp.hl_buf + (size_t(c) * nbin + bin) * quota;
+        uint32_t *wk = bp.map + size_t(k) * wpc + (size_t(reg) << (rlog - 5));
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const uint32_t off = __ldcs(e + i);
+            atomicAnd(wk + (off >> 5), ~(1u << (off & 31)));
+        }
+        __syncthreads();
     }
 }
 
@@ -548,7 +596,12 @@ void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 
 void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 {
-    gbk::k_hitlist<<<g.sm * 8, 256, 0, st>>>(d);
+    gbk::k_hitlist<<<g.sm * kHitlistCtasPerSm, 256, 0, st>>>(d);
+}
+
+void launch_hl_apply(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_hl_apply<<<g.sm * 8, 256, 0, st>>>(d);
 }
 
 void launch_xfirst1(const gbk::BatchParams &bp, cudaStream_t st)
