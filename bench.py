@@ -513,13 +513,14 @@ def run_gb300(args, rep):
         cfg = ctx.cfg
         cst = ctx.stats()
     hbm, kind = peaks()
-    # The dominant kernel of each stage and its algorithmic bytes per launch
-    # (one launch per batch: the kernels are persistent over the batch's
+    # The kernels of each stage and their algorithmic bytes per launch (one
+    # launch per batch: the kernels are persistent over the batch's
     # segments). A segment's class map is one bit per q coprime to 30:
-    # SEG / 30 bytes. The hit-list stage reads its primes once and makes one
-    # 4-byte read-modify-write per semiprime mark (the marks counted by the
-    # density of q = p m, p >= p_hl, m prime) plus the table bytes of the
-    # primes' multiplier ranges.
+    # SEG / 30 bytes. The hit-list stage reads its primes once and the table
+    # bytes of their multiplier ranges, writes and reads back one 4-byte
+    # offset per semiprime mark (the marks counted by the density of q = p m,
+    # p >= p_hl, m prime), and reads and writes the maps once while it
+    # clears the marks region by region.
     import math
     seg_map = SEG / 30
     W = args.batch * SEG
@@ -530,31 +531,32 @@ def run_gb300(args, rep):
     marks = W * math.log(u1 * (L - u0) / (u0 * (L - u1))) / L if u1 > u0 else 0.0
     n_hl = NPRIMES_4E18 - p_hl / (math.log(p_hl) - 1.08366) if u1 > u0 else 0.0
     table_bytes = W / 30 * math.log(u1 / u0) if u1 > u0 else 0.0
+    maps = args.batch * seg_map
     per_stage = {
-        "tile": ("k_tile", args.batch * seg_map),                     # one write of the batch's maps
-        "large": ("k_hitlist", 4 * n_hl + 8 * marks + table_bytes),   # primes + marks + table ranges
-        "check": ("k_verify", args.batch * seg_map),                  # one read of the maps
-        "count": ("k_count", args.batch * seg_map),                   # one read of the maps
+        "tile": (["k_tile"], maps),                                              # the maps, written once
+        "large": (["k_hitlist", "k_hl_apply"], 4 * n_hl + table_bytes + 8 * marks + 2 * maps),
+        "check": (["k_verify", "k_tail"], maps),                                 # the maps, read once
+        "count": (["k_count"], maps),                                            # the maps, read once
     }
     counters = ncu_counters()
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = cst.sm_count * 4 * sm_mhz * 1e6                    # warp instructions per second
     stage_bw = {}
-    for s_, (kern, b) in per_stage.items():
+    for s_, (kerns, b) in per_stage.items():
         ms = stage[s_] / args.steps
-        row = {"kernel": kern, "ms_per_launch": ms, "alg_bytes_per_launch": b,
+        row = {"kernel": "+".join(kerns), "ms_per_launch": ms, "alg_bytes_per_launch": b,
                "achieved_gbs": b / (ms / 1e3) / 1e9 if ms > 0 else None,
                "frac_hbm": b / (ms / 1e3) / 1e9 / hbm if ms > 0 else None}
-        c = counters.get(kern)
-        if c:
-            row["ncu_dram_bytes_per_launch"] = c[0]
-            row["ncu_warp_inst_per_launch"] = c[1]
-            row["issue_frac"] = c[1] / (ms / 1e3) / issue_peak if ms > 0 else None
+        have = [counters[k] for k in kerns if k in counters]
+        if have:
+            row["ncu_dram_bytes_per_launch"] = sum(c[0] for c in have)
+            row["ncu_warp_inst_per_launch"] = sum(c[1] for c in have)
+            row["issue_frac"] = row["ncu_warp_inst_per_launch"] / (ms / 1e3) / issue_peak if ms > 0 else None
         stage_bw[s_] = row
     dom = max(stage, key=stage.get)                     # the stage with the most device time per step
-    kernel = per_stage[dom][0]
+    kernel = stage_bw[dom]["kernel"]
     achieved = stage_bw[dom]["achieved_gbs"]
-    traffic = counters.get(kernel, (None,))[0]
+    traffic = stage_bw[dom].get("ncu_dram_bytes_per_launch")
     out = {
         "metric": METRIC, "value": value, "unit": "G evens/s", "n_gpus": rep.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
