@@ -198,11 +198,33 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
         if (l >= tl) continue;
         for (uint32_t b = l + lane * p; b < tl; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
     }
-    // the rest: a thread per prime
-    for (uint32_t i = bp.i_warp + tid; i < bp.n_mid; i += bs) {
-        const uint32_t p = bp.primes[i];
-        const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tl);
-        for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+    // the rest: a thread per prime, the next prime's three loads issued
+    // before the current prime's marks
+    {
+        const uint32_t *pr = bp.primes, *mg = bp.magic;
+        const uint32_t n = bp.n_mid;
+        uint32_t i = bp.i_warp + tid;
+        uint32_t p = 0, x = kNone, m = 0;
+        if (i < n) {
+            p = __ldg(pr + i);
+            x = __ldg(xk + i);
+            m = __ldg(mg + i);
+        }
+        while (i < n) {
+            const uint32_t j = i + bs;
+            uint32_t pn = 0, xn = kNone, mn = 0;
+            if (j < n) {
+                pn = __ldg(pr + j);
+                xn = __ldg(xk + j);
+                mn = __ldg(mg + j);
+            }
+            const uint32_t l = local_start(x, t0, p, m, tl);
+            for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+            i = j;
+            p = pn;
+            x = xn;
+            m = mn;
+        }
     }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(bp.map + size_t(k) * bp.wpc + (t0 >> 5));
