@@ -34,7 +34,7 @@ KNOBS = {
     "mtab_max_gb": [48, 96, 160],
     "tile_log2": [19, 20],
     "max_batch": [16, 32, 48, 64],
-    "plan_funnels": [24, 32, 40],
+    "plan_funnels": [8, 16, 24, 32],
 }
 DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 40}
 DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")

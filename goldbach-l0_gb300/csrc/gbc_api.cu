@@ -332,7 +332,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.plan_funnels) cfg.plan_funnels = 40;
     if (!cfg.ridge_min) cfg.ridge_min = GBC_TAIL_T;
     if (!cfg.launch_mode) cfg.launch_mode = 1;
-    if (cfg.plan_funnels > 256) cfg.plan_funnels = 256;
+    if (cfg.plan_funnels > 64) cfg.plan_funnels = 64;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
@@ -442,13 +442,14 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         ctx->ct.cnt[cr] = uint32_t(list.size()) - ctx->ct.off[cr];
     }
     // verify plan (the reference's make_plan30, include/check30.hpp:88-174,
-    // with our own greedy order): per class, the smallest useful candidates
-    // below GBC_TAIL_T in ascending order, each uncovered one opening a
-    // funnel with the uncovered primes among p + 30, ..., p + 120 of the same
-    // residue (all below the bound), plan_funnels funnels; the rest lists
-    // hold every useful candidate no funnel tests, ascending, for the exact
-    // continuation.
-    std::vector<uint32_t> fun;
+    // with our own greedy order): per class, the useful candidates below
+    // GBC_TAIL_T in ascending order, each uncovered one p opening a funnel
+    // with every uncovered prime of its residue among p + 30, ..., p + 930
+    // (the 32 positions one 64-bit window read covers: member p + 30 d is
+    // the top member's window shifted by its distance), plan_funnels funnels;
+    // the rest lists hold every useful candidate no funnel tests, ascending,
+    // for the exact continuation.
+    std::vector<uint2> fun;
     std::vector<uint16_t> rest;
     {
         std::vector<int> cidx(GBC_MAX_CAND + 1, -1);
@@ -463,15 +464,14 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
                 if (covered[i]) continue;
                 uint32_t mask = 1;
                 covered[i] = 1;
-                // every uncovered prime among p + 30, ..., p + 120 joins (gaps allowed:
-                // the window read covers all five positions)
-                for (uint32_t d = 1; d <= 4; ++d) {
+                for (uint32_t d = 1; d < 32; ++d) {
                     const uint32_t q = cand[i] + 30 * d;
-                    if (q >= GBC_TAIL_T || q > GBC_MAX_CAND || cidx[q] < 0 || covered[cidx[q]]) continue;
+                    if (q >= GBC_TAIL_T || q > GBC_MAX_CAND) break;
+                    if (cidx[q] < 0 || covered[cidx[q]]) continue;
                     covered[cidx[q]] = 1;
                     mask |= 1u << d;
                 }
-                fun.push_back(uint32_t(i) | (mask << 16));
+                fun.push_back(make_uint2(uint32_t(i), mask));
             }
             ctx->vt.fun_cnt[cr] = uint32_t(fun.size()) - ctx->vt.fun_off[cr];
             ctx->vt.rest_off[cr] = uint32_t(rest.size());
@@ -508,8 +508,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->ct.cand = ctx->d_cand;
     ctx->ct.list = ctx->d_list;
     ctx->ct.ridge_min = cfg.ridge_min;
-    CK(dev_alloc(ctx, &ctx->d_fun, std::max<size_t>(fun.size(), 1) * 4));
-    if (!fun.empty()) CK(cudaMemcpy(ctx->d_fun, fun.data(), fun.size() * 4, cudaMemcpyHostToDevice));
+    CK(dev_alloc(ctx, &ctx->d_fun, std::max<size_t>(fun.size(), 1) * sizeof(uint2)));
+    if (!fun.empty()) CK(cudaMemcpy(ctx->d_fun, fun.data(), fun.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     CK(dev_alloc(ctx, &ctx->d_rest, std::max<size_t>(rest.size(), 1) * 2));
     if (!rest.empty()) CK(cudaMemcpy(ctx->d_rest, rest.data(), rest.size() * 2, cudaMemcpyHostToDevice));
     ctx->vt.cand = ctx->d_cand;

@@ -199,7 +199,7 @@ struct CheckTables {
 // of its exact continuation (phase B), per class r / 2.
 struct VerifyTables {
     const uint16_t *cand;
-    const uint32_t *fun;    // funnel: candidate index of its first member | mask << 16 (bit d: p + 30 d)
+    const uint2 *fun;       // funnel: candidate index of its smallest member p, members (bit d: p + 30 d, d < 32)
     const uint16_t *rest;   // candidates no funnel tests, ascending
     uint32_t fun_off[GBC_NCLASS], fun_cnt[GBC_NCLASS];
     uint32_t rest_off[GBC_NCLASS], rest_cnt[GBC_NCLASS];

@@ -76,7 +76,7 @@ struct gbc_ctx {
     DescLayout layout;
     uint32_t *d_primes = nullptr, *d_magic = nullptr, *d_pat = nullptr, *d_skip = nullptr;
     uint16_t *d_inv = nullptr, *d_cand = nullptr, *d_list = nullptr;
-    uint32_t *d_fun = nullptr;
+    uint2 *d_fun = nullptr;
     uint16_t *d_rest = nullptr;
     gbk::GroupInfo gi{};
     gbk::CheckTables ct{};

@@ -305,17 +305,20 @@ __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
 }
 
 constexpr uint32_t kVWin = 84;     // staged words per class array per warp (verify)
-constexpr uint32_t kMaxFun = 256;  // funnels per class the verify kernel holds
+constexpr uint32_t kMaxFun = 64;   // funnels per class the verify kernel holds
 
 // Phase A (the reference's check30_a, kernels/goldbach.cl:2029-2189): any
-// witness. Each funnel is a run of plan members p, p + 30, ..., p + 30 d
-// of one residue class, all prime, whose windows are the same staged words
-// shifted by 0..d bits, so one 96-bit read tests up to five candidates for
-// 32 evens. No statistics here: evens left without a plan witness go to a
+// witness. Each funnel is a set of plan members p + 30 d (d < 32) of one
+// residue class, all prime, whose windows are the same staged words shifted
+// by their distance in bits, so one 96-bit read and one funnel shift per
+// member test up to 32 candidates for 32 evens. No statistics here: evens left without a plan witness go to a
 // pending list of (class, word, bits) for k_tail.
 __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
 {
-    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member shifts << 21
+    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member groups << 21
+    // per funnel, the other members' window offsets above the top member's,
+    // four bytes per word, padded with 0 (the top member again)
+    __shared__ uint32_t s_fsh[kMaxFun][8];
     __shared__ uint32_t s_win[kCheckWarps][8 * kVWin];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
@@ -354,8 +357,8 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
         __syncthreads();
         // the lowest window bit of each funnel: its top member p + 30 d
         for (uint32_t f = tid; f < nfun; f += blockDim.x) {
-            const uint32_t e = vt.fun[vt.fun_off[cr] + f];
-            const uint32_t p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(e >> 16);
+            const uint2 e = vt.fun[vt.fun_off[cr] + f];
+            const uint32_t p0 = vt.cand[e.x], dm = 31 - __clz(e.y);
             const uint32_t u = (r + 30 - p0 % 30) % 30;
             const uint32_t dlow = uint32_t((n0 - base - p0 - u) / 30) - dm;
             atomicMin(&s_dmin, dlow);
@@ -365,15 +368,23 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
         const uint32_t dlo = s_dmin & ~31u;
         const uint32_t nstage = (s_dmax - dlo) / 32 + 68;  // <= kVWin
         for (uint32_t f = tid; f < nfun; f += blockDim.x) {
-            const uint32_t e = vt.fun[vt.fun_off[cr] + f];
-            const uint32_t mask = e >> 16, p0 = vt.cand[e & 0xFFFF], dm = 31 - __clz(mask);
+            const uint2 e = vt.fun[vt.fun_off[cr] + f];
+            const uint32_t p0 = vt.cand[e.x], dm = 31 - __clz(e.y);
             const uint32_t u = (r + 30 - p0 % 30) % 30;
             const uint32_t dd = uint32_t((n0 - base - p0 - u) / 30) - dm - dlo;
-            // member d's window starts dm - d bits above the top member's
-            uint32_t sm = 0;
-            for (uint32_t d = 0; d <= dm; ++d)
-                if ((mask >> d) & 1u) sm |= 1u << (dm - d);
-            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (sm << 21);
+            // member p0 + 30 d's window starts dm - d bits above the top member's
+            uint32_t sm = (__brev(e.y) >> (31 - dm)) & ~1u, ng = 0;
+            while (sm) {
+                uint32_t word = 0;
+#pragma unroll
+                for (uint32_t j = 0; j < 4; ++j)
+                    if (sm) {
+                        word |= uint32_t(__ffs(sm) - 1) << (8 * j);
+                        sm &= sm - 1u;
+                    }
+                s_fsh[f][ng++] = word;
+            }
+            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (ng << 21);
         }
         __syncthreads();
 
@@ -390,22 +401,24 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
             uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
             const uint32_t *wl = win + lane;
             for (uint32_t f = 0; f < nfun; ++f) {
-                if ((f & 3) == 0 && !__any_sync(~0u, uA | uB)) break;
+                if (!__any_sync(~0u, uA | uB)) break;
                 const uint32_t e = s_fent[f];
                 const uint32_t *w = wl + (e & 0xFFFF);
-                const uint32_t sh = (e >> 16) & 31, sm = e >> 21;
+                const uint32_t sh = (e >> 16) & 31, ng = e >> 21;
                 const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
                 // the top member's 64-bit window; every other member's is
-                // the same shifted down by 1..4 bits (bit s of sm)
+                // the same shifted down by 1..31 bits, four shifts per word
+                // (a funnel shift uses the low 5 bits of its shift operand)
                 const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
                 const uint32_t bl = __funnelshift_r(y0, y1, sh), bh = __funnelshift_r(y1, y2, sh);
                 uint32_t wa = al, wb = bl;
-#pragma unroll
-                for (uint32_t k = 1; k <= 4; ++k)
-                    if ((sm >> k) & 1u) {
-                        wa |= __funnelshift_r(al, ah, k);
-                        wb |= __funnelshift_r(bl, bh, k);
-                    }
+                for (uint32_t g = 0; g < ng; ++g) {
+                    const uint32_t q = s_fsh[f][g], q1 = q >> 8, q2 = q >> 16, q3 = q >> 24;
+                    wa |= __funnelshift_r(al, ah, q) | __funnelshift_r(al, ah, q1) | __funnelshift_r(al, ah, q2) |
+                          __funnelshift_r(al, ah, q3);
+                    wb |= __funnelshift_r(bl, bh, q) | __funnelshift_r(bl, bh, q1) | __funnelshift_r(bl, bh, q2) |
+                          __funnelshift_r(bl, bh, q3);
+                }
                 uA &= ~wa;
                 uB &= ~wb;
             }
