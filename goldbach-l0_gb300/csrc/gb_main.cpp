@@ -73,8 +73,11 @@ bool parse_count(const char *s, uint64_t &out)
 int usage()
 {
     std::fprintf(stderr,
-                 "usage: goldbach_gb300 [--start N] --limit N [--segment N] [--batch N] [--csv] [--stats] "
-                 "[--verbose]\n");
+                 "usage: goldbach_gb300 [--start N] --limit N [--segment N] [--batch N] [--stats-sample N] [--csv] "
+                 "[--stats] [--verbose]\n"
+                 "       goldbach_gb300 --start N --limit N --slice N --journal FILE [--release ID] [--stop-file F]\n"
+                 "                      [--segment N] [--batch N] [--stats-sample N]   (journaled slices; exit 3 "
+                 "on the stop file)\n");
     return 2;
 }
 
@@ -82,8 +85,9 @@ int usage()
 
 int main(int argc, char **argv)
 {
-    uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8, sample = 1;
+    uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8, sample = 1, slice = 0;
     bool csv = false, stats = false, verbose = false;
+    std::string journal, release = "gb300-1.0", stop_file;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto val = [&](uint64_t &dst) {
@@ -101,6 +105,11 @@ int main(int argc, char **argv)
             if (!val(batch) || !batch || batch > 256) return usage();
         } else if (a == "--stats-sample") {
             if (!val(sample) || !sample || sample > (1u << 30)) return usage();
+        } else if (a == "--slice") {
+            if (!val(slice) || slice < 4 || (slice & 1)) return usage();
+        } else if (a == "--journal" || a == "--release" || a == "--stop-file") {
+            if (i + 1 >= argc) return usage();
+            (a == "--journal" ? journal : a == "--release" ? release : stop_file) = argv[++i];
         } else if (a == "--csv") csv = true;
         else if (a == "--stats") stats = true;
         else if (a == "--verbose") verbose = true;
@@ -115,17 +124,38 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "limit %" PRIu64 " is above the supported maximum 2^64 - 2^40\n", limit);
         return 1;
     }
+    if (slice || !journal.empty()) {
+        if (!slice || journal.empty()) return usage();
+        gbc_config cfg{};
+        cfg.limit = limit & ~uint64_t(1);
+        cfg.segment_even = segment;
+        cfg.max_batch = uint32_t(batch);
+        cfg.sample_every = uint32_t(sample);
+        gbc_ctx *ctx = nullptr;
+        const int rc = gbc_create(&cfg, &ctx);
+        if (rc != GBC_OK) {
+            std::fprintf(stderr, "FAIL: gbc_create: %s\n", gbc_last_error(ctx));
+            gbc_destroy(ctx);
+            return rc == GBC_E_ARG ? 2 : 1;
+        }
+        int code = 0;
+        try {
+            int stopped = 0;
+            gb::run_slices(ctx, start, limit, slice, journal, release, stop_file.empty() ? nullptr : stop_file.c_str(),
+                           stdout, &stopped);
+            code = stopped ? 3 : 0;
+        } catch (const gb::GbcError &e) {
+            std::fprintf(stderr, "FAIL: %s\n", e.what());
+            code = e.code == GBC_E_ARG ? 2 : 1;
+        }
+        gbc_destroy(ctx);
+        return code;
+    }
     try {
         const gb::RunStats st = gb::run_gpu(limit, segment, verbose, start, uint32_t(batch), nullptr, uint32_t(sample));
         const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
         if (csv)
-            std::printf("result=PASS,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64 ",segments=%" PRIu64
-                        ",leftovers=%" PRIu64 ",pmax=%" PRIu64 ",primes=%" PRIu64 ",twins=%" PRIu64
-                        ",gpu_s=%.6f,total_s=%.6f,evens_per_sec=%.6e,sieve_s=%.6f,large_s=%.6f,verify_s=%.6f,"
-                        "count_s=%.6f\n",
-                        st.start, st.limit, st.evens, st.segments, st.leftovers, st.pmax, st.primes, st.twins,
-                        st.gpu_seconds, st.wall_seconds, eps, st.tile_ms / 1e3, st.large_ms / 1e3,
-                        st.check_ms / 1e3, st.count_ms / 1e3);
+            std::printf("%s\n", gb::csv_line(st, segment).c_str());
         else
             std::printf("PASS: every even n in [%" PRIu64 ", %" PRIu64 "] is a sum of two primes "
                         "(%" PRIu64 " evens, largest p(n) %" PRIu64 ", %.3f G evens/s)\n",

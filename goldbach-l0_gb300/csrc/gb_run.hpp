@@ -6,6 +6,7 @@
 // never report a PASS that did not happen.
 #pragma once
 #include <cstdint>
+#include <cstdio>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -97,6 +98,15 @@ std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_
 // gets p(n) of every even, the others the funnel verify + exact tail.
 RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
                    uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every = 1);
+
+// The reference's --csv key=value line of a run (src/main.cpp:191-215).
+std::string csv_line(const RunStats &st, uint64_t segment);
+
+// Journaled slices (gb_journal.cpp): the resume point of a journal, and a
+// run of [start, limit] in slices that appends PASS / RETRY rows.
+uint64_t journal_resume(const std::string &path, uint64_t start);
+uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
+                    const std::string &release, const char *stop_file, FILE *log, int *stopped);
 
 // gb::run_gpu: creates a context, runs, destroys it.
 RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even = 4,

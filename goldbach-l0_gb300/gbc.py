@@ -122,6 +122,9 @@ SIGNATURES = {
     "gbc_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     "gbc_server_error": (C.c_char_p, [C.c_void_p]),
     "gbc_server_stop": (C.c_int, [C.c_void_p]),
+    "gbc_journal_resume": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gbc_run_slices": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_char_p, C.c_char_p,
+                                 C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
@@ -269,6 +272,14 @@ class Context:
             out.append((res[i], chunk[:chunk.index(b"\0")].decode()))
         return out, summ
 
+    def run_slices(self, start, limit, slice_, journal, release="gb300-1.0", stop_file=None):
+        """Journaled slices (tools/run_range.sh's contract): (slices done now, stopped)."""
+        done, stopped = C.c_uint64(), C.c_int()
+        self._check(self.lib.gbc_run_slices(self.h, start, limit, slice_, str(journal).encode(), release.encode(),
+                                            str(stop_file).encode() if stop_file else None, C.byref(done),
+                                            C.byref(stopped)))
+        return done.value, bool(stopped.value)
+
     def verify_range(self, start, limit, want_pn=False):
         """Returns (RunResult, stats_ref line, p(n) array or None)."""
         res = RunResult()
@@ -278,6 +289,16 @@ class Context:
             pn = (C.c_uint16 * ((limit - start) // 2 + 1))()
         self._check(self.lib.gbc_verify_range(self.h, start, limit, C.byref(res), line, len(line), pn))
         return res, line.value.decode(), pn
+
+
+def journal_resume(path, start):
+    """Where a journaled run of [start, ...] resumes: after the journal's
+    contiguous chain of PASS slices from start."""
+    n = C.c_uint64()
+    rc = load().gbc_journal_resume(str(path).encode(), start, C.byref(n))
+    if rc:
+        raise GbcError(rc, "journal")
+    return n.value
 
 
 class Server:

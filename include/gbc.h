@@ -345,6 +345,20 @@ const char *gbc_server_error(gbc_server *srv);
  * context is the caller's again. Returns the worker's error, if any. */
 int gbc_server_stop(gbc_server *srv);
 
+/* ---- journaled slices -------------------------------------------------------
+ * The reference's slice runner (tools/run_range.sh, docs/PIPELINE.md:12-24,
+ * 114-122) on one resident context: [start, limit] in slices of `slice`
+ * integers, one journal row per slice: "PASS a b <UTC time> <the --csv
+ * key=value line> release=<release>" (" attempts=2" when it passed on the
+ * retry), "RETRY a b <time> reason=<code>" for a failed first attempt; a
+ * slice that fails twice stops the run with its error. A run resumes after
+ * the last slice of the journal's contiguous PASS chain from start. A stop
+ * file present before a slice ends the run cleanly (*stopped = 1), the
+ * resume point intact. */
+int gbc_journal_resume(const char *path, uint64_t start, uint64_t *next);
+int gbc_run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const char *journal,
+                   const char *release, const char *stop_file, uint64_t *slices_done, int *stopped);
+
 /* ---- allocation-free class map ---------------------------------------------
  * This entry point has no counterpart in the reference.
  *

@@ -195,3 +195,26 @@ def test_uneven_windows_sampled_against_oracle_config_c4():
             assert out[i][1] == oracle.stats_line(wins[i][0], wins[i][1], oracle.SIEVE), wins[i]
         for i in random.Random(9).sample(range(len(wins)), 16):
             assert out[i][1] == c.verify_range(*wins[i])[1], wins[i]
+
+
+def test_journaled_slices_resume_and_stop(tmp_path):
+    """The slice runner: PASS rows per slice, a stop file ends the run with
+    the resume point intact, a second call resumes after the PASS chain;
+    each slice's counts equal the oracle's for that slice."""
+    a, b, w = 10**12, 10**12 + 8_000_000 - 2, 2_000_000
+    j, stop = tmp_path / "journal.txt", tmp_path / "stop"
+    with gbc.Context(limit=b, segment_even=1_000_000, max_batch=4) as c:
+        assert c.run_slices(a, a + 2 * w - 2, w, j) == (2, False)
+        stop.write_text("")
+        assert c.run_slices(a, b, w, j, stop_file=stop) == (0, True)
+        stop.unlink()
+        assert gbc.journal_resume(j, a) == a + 2 * w
+        assert c.run_slices(a, b, w, j, stop_file=stop) == (2, False)
+    rows = [r.split() for r in j.read_text().splitlines()]
+    assert [r[0] for r in rows] == ["PASS"] * 4
+    assert [(int(r[1]), int(r[2])) for r in rows] == [(a + i * w, a + i * w + w - 2) for i in range(4)]
+    for r in rows:
+        got = dict(t.split("=", 1) for t in r[4:] if "=" in t)
+        want = dict(t.split("=", 1) for t in oracle.stats_line(int(r[1]), int(r[2]), oracle.SIEVE).split())
+        assert got["result"] == "PASS" and got["release"] == "gb300-1.0"
+        assert (got["primes"], got["twins"], got["stats_pmax"]) == (want["primes"], want["twins"], want["pmax"])
