@@ -33,10 +33,10 @@ KNOBS = {
     "p_mid": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
     "mtab_max_gb": [48, 96, 160],
     "tile_log2": [19, 20],
-    "max_batch": [16, 32, 48, 64],
-    "plan_funnels": [8, 16, 24, 32],
+    "max_batch": [32, 48, 64, 96, 128],
+    "plan_funnels": [4, 6, 8, 12, 16],
 }
-DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 40}
+DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 8}
 DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")
 
 
@@ -76,7 +76,11 @@ def tune(start, rounds=2, nseg=192, log=print):
         key = tuple(sorted(k.items()))
         if key not in cache:
             t0 = time.perf_counter()
-            v = measure(k, start, nseg)
+            try:
+                v = measure(k, start, nseg)
+            except gbc.GbcError as e:   # e.g. the device memory of a large batch
+                log(f"  {k} failed: {e}")
+                v = 0.0
             cache[key] = v
             trials.append({"knobs": dict(k), "g_evens_s": v, "seconds": time.perf_counter() - t0})
             log(f"  {k} -> {v:.2f} G evens/s")

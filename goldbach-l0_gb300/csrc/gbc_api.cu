@@ -329,10 +329,10 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.mtab_max_gb) cfg.mtab_max_gb = 48;
     if (!cfg.nslots) cfg.nslots = 2;
     if (!cfg.sample_every) cfg.sample_every = 1;
-    if (!cfg.plan_funnels) cfg.plan_funnels = 40;
+    if (!cfg.plan_funnels) cfg.plan_funnels = 8;
     if (!cfg.ridge_min) cfg.ridge_min = GBC_TAIL_T;
     if (!cfg.launch_mode) cfg.launch_mode = 1;
-    if (cfg.plan_funnels > 64) cfg.plan_funnels = 64;
+    if (cfg.plan_funnels > gbk::kVerifyMaxFun) cfg.plan_funnels = gbk::kVerifyMaxFun;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))

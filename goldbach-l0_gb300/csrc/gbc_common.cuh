@@ -216,6 +216,69 @@ constexpr uint32_t kErrTable = 1u << 5;   // a multiplier outside the prime-mult
 constexpr uint32_t kErrPendOverflow = 1u << 6;
 constexpr uint32_t kErrRidgeOverflow = 1u << 7;
 constexpr uint32_t kErrSelfCheck = 1u << 8;  // the map self-check found differing words
+constexpr uint32_t kErrStaging = 1u << 9;    // a bulk copy into shared memory missed its wait limit
+
+// funnels per class the verify kernel holds (the plan has at most this many)
+constexpr uint32_t kVerifyMaxFun = 32;
+
+// ---------------------------------------------------------------------------
+// Bulk copies global -> shared memory (cp.async.bulk, the TMA unit's
+// untiled form) completing on an mbarrier. Source and destination 16-byte
+// aligned, sizes multiples of 16 bytes. Waits are bounded: kStageSpin
+// try_wait rounds of at most about a microsecond each.
+constexpr uint32_t kStageSpin = 1u << 16;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// makes initialised mbarriers visible to the async proxy
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// orders this thread's earlier generic shared-memory accesses (and those it
+// synchronised with) before its later async-proxy copies into shared memory
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(1000u)
+        : "memory");
+    return ok != 0;
+}
+
+// waits for the phase of the given parity; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kStageSpin; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
 
 // ---------------------------------------------------------------------------
 // 64-bit Miller-Rabin in Montgomery form (the GPU retry of evens without a

@@ -304,27 +304,53 @@ __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
     }
 }
 
-constexpr uint32_t kVWin = 84;     // staged words per class array per warp (verify)
-constexpr uint32_t kMaxFun = 64;   // funnels per class the verify kernel holds
+constexpr uint32_t kVWin = 76;  // staged words per class array and buffer: 64 + funnel span (<= 5) + 4 + alignment (<= 3)
+constexpr uint32_t kMaxFun = kVerifyMaxFun;
+
+// one chunk's eight class-array windows into a staging buffer: 8 bulk
+// copies of `bytes` each, completing on bar (issued by one lane)
+__device__ __forceinline__ void stage_chunk(uint32_t *dst, uint64_t *bar, const uint32_t *src, uint32_t wpc,
+                                            uint32_t bytes)
+{
+    mbar_arrive_expect_tx(bar, 8 * bytes);
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) bulk_copy_g2s(dst + k * kVWin, src + size_t(k) * wpc, bytes, bar);
+}
 
 // Phase A (the reference's check30_a, kernels/goldbach.cl:2029-2189): any
 // witness. Each funnel is a set of plan members p + 30 d (d < 32) of one
 // residue class, all prime, whose windows are the same staged words shifted
 // by their distance in bits, so one 96-bit read and one funnel shift per
-// member test up to 32 candidates for 32 evens. No statistics here: evens left without a plan witness go to a
-// pending list of (class, word, bits) for k_tail.
+// member test up to 32 candidates for 32 evens. No statistics here: evens
+// left without a plan witness go to a pending list of (class, word, bits)
+// for k_tail.
+//
+// Staging: each warp double-buffers its 64-word chunks in shared memory;
+// one lane moves the next chunk's eight class-array windows with bulk
+// copies (cp.async.bulk on an mbarrier) while the warp tests the current
+// one. The windows start 16-byte aligned (the class arrays are, and chunks
+// are 64 words apart), o = 0..3 words below the lowest word a funnel reads.
 __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
 {
     __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member groups << 21
-    // per funnel, the other members' window offsets above the top member's,
-    // four bytes per word, padded with 0 (the top member again)
-    __shared__ uint32_t s_fsh[kMaxFun][8];
-    __shared__ uint32_t s_win[kCheckWarps][8 * kVWin];
+    // per funnel and group of four other members: their window offsets
+    // above the top member's, padded with 0 (the top member again)
+    __shared__ uint4 s_fsh[kMaxFun][8];
+    __shared__ __align__(16) uint32_t s_win[kCheckWarps][2][8 * kVWin];
+    __shared__ __align__(8) uint64_t s_bar[kCheckWarps][2];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
 
     __shared__ uint32_t s_vb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint64_t *bar = s_bar[warp];
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    uint32_t phase = 0;  // bit b: parity of buffer b's next completion
     const uint32_t total = d.h->ver_vb, nseg = d.h->nseg;
     for (;;) {
         const uint32_t vb = next_item(d.work + kWorkVerify, &s_vb);
@@ -365,8 +391,15 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
             atomicMax(&s_dmax, dlow);
         }
         __syncthreads();
-        const uint32_t dlo = s_dmin & ~31u;
-        const uint32_t nstage = (s_dmax - dlo) / 32 + 68;  // <= kVWin
+        const uint32_t dlo = s_dmin & ~31u, o = (dlo >> 5) & 3u;
+        // words each class copy moves: the chunk, the funnels' span and the
+        // three words a 96-bit read needs, from the aligned start
+        const uint32_t cwords = nfun ? ((s_dmax - dlo) / 32 + 68 + o + 3) & ~3u : 0u;
+        if (cwords > kVWin) {  // funnel span beyond the staging buffer: nothing tested
+            if (tid == 0) atomicOr(&res->err, kErrStaging);
+            __syncthreads();
+            continue;
+        }
         for (uint32_t f = tid; f < nfun; f += blockDim.x) {
             const uint2 e = vt.fun[vt.fun_off[cr] + f];
             const uint32_t p0 = vt.cand[e.x], dm = 31 - __clz(e.y);
@@ -375,79 +408,104 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
             // member p0 + 30 d's window starts dm - d bits above the top member's
             uint32_t sm = (__brev(e.y) >> (31 - dm)) & ~1u, ng = 0;
             while (sm) {
-                uint32_t word = 0;
+                uint32_t q[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
                 for (uint32_t j = 0; j < 4; ++j)
                     if (sm) {
-                        word |= uint32_t(__ffs(sm) - 1) << (8 * j);
+                        q[j] = uint32_t(__ffs(sm) - 1);
                         sm &= sm - 1u;
                     }
-                s_fsh[f][ng++] = word;
+                s_fsh[f][ng++] = make_uint4(q[0], q[1], q[2], q[3]);
             }
-            s_fent[f] = (class_of(u) * kVWin + (dd >> 5)) | ((dd & 31) << 16) | (ng << 21);
+            s_fent[f] = (class_of(u) * kVWin + o + (dd >> 5)) | ((dd & 31) << 16) | (ng << 21);
         }
         __syncthreads();
 
-        uint32_t *win = s_win[warp];
         uint32_t pend = 0;
-        for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps) {
-            const uint32_t J = ch * 64;
-            const uint32_t *src = map + (dlo >> 5) + J;
+        if (nfun) {
+            const uint32_t step = gx * kCheckWarps, bytes = cwords * 4;
+            const uint32_t *src0 = map + ((dlo >> 5) - o);
+            uint32_t ch = bx * kCheckWarps + warp, buf = 0;
+            if (ch * 64 < nwords && lane == 0) {
+                fence_proxy_async();
+                stage_chunk(s_win[warp][0], bar, src0 + size_t(ch) * 64, wpc, bytes);
+            }
+            for (; ch * 64 < nwords; ch += step, buf ^= 1u) {
+                const uint32_t nx = ch + step;
+                if (nx * 64 < nwords) {
+                    __syncwarp();  // every lane is done with the other buffer (the chunk before)
+                    if (lane == 0) {
+                        fence_proxy_async();
+                        stage_chunk(s_win[warp][buf ^ 1u], bar + (buf ^ 1u), src0 + size_t(nx) * 64, wpc, bytes);
+                    }
+                }
+                if (!mbar_wait(bar + buf, (phase >> buf) & 1u)) {
+                    atomicOr(&res->err, kErrStaging);
+                    mbar_wait(bar + buf, (phase >> buf) & 1u);
+                }
+                phase ^= 1u << buf;
+                const uint32_t J = ch * 64;
+                const uint32_t jA = J + lane, jB = J + 32 + lane;
+                uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+                const uint32_t *wl = s_win[warp][buf] + lane;
+                for (uint32_t f = 0; f < nfun; ++f) {
+                    if (!__any_sync(~0u, uA | uB)) break;
+                    const uint32_t e = s_fent[f];
+                    const uint32_t *w = wl + (e & 0xFFFF);
+                    const uint32_t sh = (e >> 16) & 31, ng = e >> 21;
+                    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
+                    // the top member's 64-bit window; every other member's
+                    // is the same shifted down by 1..31 bits
+                    const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
+                    const uint32_t bl = __funnelshift_r(y0, y1, sh), bh = __funnelshift_r(y1, y2, sh);
+                    uint32_t wa = al, wb = bl;
+                    for (uint32_t g = 0; g < ng; ++g) {
+                        const uint4 q = s_fsh[f][g];
+                        wa |= __funnelshift_r(al, ah, q.x) | __funnelshift_r(al, ah, q.y) |
+                              __funnelshift_r(al, ah, q.z) | __funnelshift_r(al, ah, q.w);
+                        wb |= __funnelshift_r(bl, bh, q.x) | __funnelshift_r(bl, bh, q.y) |
+                              __funnelshift_r(bl, bh, q.z) | __funnelshift_r(bl, bh, q.w);
+                    }
+                    uA &= ~wa;
+                    uB &= ~wb;
+                }
+                // pending words: one reservation per warp
+                const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
+                uint32_t pre = has;
 #pragma unroll
-            for (uint32_t k = 0; k < 8; ++k)
-                for (uint32_t i = lane; i < nstage; i += 32) win[k * kVWin + i] = __ldg(src + size_t(k) * wpc + i);
-            __syncwarp();
-            const uint32_t jA = J + lane, jB = J + 32 + lane;
-            uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
-            const uint32_t *wl = win + lane;
-            for (uint32_t f = 0; f < nfun; ++f) {
-                if (!__any_sync(~0u, uA | uB)) break;
-                const uint32_t e = s_fent[f];
-                const uint32_t *w = wl + (e & 0xFFFF);
-                const uint32_t sh = (e >> 16) & 31, ng = e >> 21;
-                const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
-                // the top member's 64-bit window; every other member's is
-                // the same shifted down by 1..31 bits, four shifts per word
-                // (a funnel shift uses the low 5 bits of its shift operand)
-                const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
-                const uint32_t bl = __funnelshift_r(y0, y1, sh), bh = __funnelshift_r(y1, y2, sh);
-                uint32_t wa = al, wb = bl;
-                for (uint32_t g = 0; g < ng; ++g) {
-                    const uint32_t q = s_fsh[f][g], q1 = q >> 8, q2 = q >> 16, q3 = q >> 24;
-                    wa |= __funnelshift_r(al, ah, q) | __funnelshift_r(al, ah, q1) | __funnelshift_r(al, ah, q2) |
-                          __funnelshift_r(al, ah, q3);
-                    wb |= __funnelshift_r(bl, bh, q) | __funnelshift_r(bl, bh, q1) | __funnelshift_r(bl, bh, q2) |
-                          __funnelshift_r(bl, bh, q3);
+                for (int o2 = 1; o2 < 32; o2 <<= 1) {
+                    const uint32_t n = __shfl_up_sync(~0u, pre, o2);
+                    if (lane >= uint32_t(o2)) pre += n;
                 }
-                uA &= ~wa;
-                uB &= ~wb;
+                const uint32_t tot = __shfl_sync(~0u, pre, 31);
+                if (tot) {
+                    uint32_t at0 = 0;
+                    if (lane == 31) at0 = atomicAdd(&res->npend, tot);
+                    at0 = __shfl_sync(~0u, at0, 31);
+                    uint32_t at = at0 + pre - has;
+                    if (uA) {
+                        if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jA, uA);
+                        else atomicOr(&res->err, kErrPendOverflow);
+                        ++at;
+                    }
+                    if (uB) {
+                        if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jB, uB);
+                        else atomicOr(&res->err, kErrPendOverflow);
+                    }
+                }
+                pend += __popc(uA) + __popc(uB);
             }
-            // pending words: one reservation per warp
-            const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
-            uint32_t pre = has;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t n = __shfl_up_sync(~0u, pre, o);
-                if (lane >= uint32_t(o)) pre += n;
-            }
-            const uint32_t tot = __shfl_sync(~0u, pre, 31);
-            if (tot) {
-                uint32_t at0 = 0;
-                if (lane == 31) at0 = atomicAdd(&res->npend, tot);
-                at0 = __shfl_sync(~0u, at0, 31);
-                uint32_t at = at0 + pre - has;
-                if (uA) {
-                    if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jA, uA);
+        } else {
+            // no funnels for the class: every word of the warp's chunks is pending
+            for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps)
+                for (uint32_t jj = ch * 64 + lane; jj < ch * 64 + 64; jj += 32) {
+                    const uint32_t uw = word_mask(jj, ecount);
+                    if (!uw) continue;
+                    const uint32_t at = atomicAdd(&res->npend, 1u);
+                    if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jj, uw);
                     else atomicOr(&res->err, kErrPendOverflow);
-                    ++at;
+                    pend += __popc(uw);
                 }
-                if (uB) {
-                    if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jB, uB);
-                    else atomicOr(&res->err, kErrPendOverflow);
-                }
-            }
-            pend += __popc(uA) + __popc(uB);
-            __syncwarp();
         }
         pend = __reduce_add_sync(~0u, pend);
         if (lane == 0 && pend) atomicAdd(&s_pend, (unsigned long long)pend);
