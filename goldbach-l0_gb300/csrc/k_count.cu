@@ -9,9 +9,10 @@
 // of a prime counted in the segment has its lower prime inside the map and
 // needs no stitching: one thread per 32 blocks of 30 (8 words, one per class
 // array); the 8 x 32 bits are transposed to one byte per block so the primes
-// come out in natural order; a block-wide max-scan of the last prime
-// position gives each thread its predecessor, a backward word search the
-// first thread's. Positions are 32-bit offsets from the CTA's first block.
+// come out in natural order; a block-wide sum-scan of the prime counts
+// places every thread's primes in one shared list in natural order, whose
+// previous entry is each prime's predecessor (a backward word search gives
+// the first one's). Positions are 32-bit offsets from the CTA's first block.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -71,14 +72,16 @@ __device__ __forceinline__ uint32_t unit_of(uint32_t k) { return __byte_perm(0x0
 
 constexpr int kCountThreads = 256;
 constexpr int32_t kNoPos = INT32_MIN;
+constexpr uint32_t kCountCap = 8192;  // prime positions the CTA's list holds per round
 
 // Persistent: a fixed grid takes the virtual CTAs of every segment of the
 // batch (per segment: one per 256 words of its hashed range) from a work
 // counter.
-__global__ void __launch_bounds__(kCountThreads) k_count(BatchDesc d)
+__global__ void __launch_bounds__(kCountThreads, 5) k_count(BatchDesc d)
 {
     __shared__ uint32_t s_ghist[GBC_GBINS];
-    __shared__ int32_t s_wlast[kCountThreads / 32];
+    __shared__ uint32_t s_wsum[kCountThreads / 32];
+    __shared__ int32_t s_pos[kCountCap];
     __shared__ int32_t s_prev0;
     __shared__ uint32_t s_cnt[8 + 3 + 1];
     __shared__ uint32_t s_key;
@@ -152,47 +155,58 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchDesc d)
             T[2 * g + 1] = uint32_t(t >> 32);
         }
         const int32_t cbase = int32_t(960 * tid);  // position of this thread's first block
-        int32_t mylast = kNoPos;
         uint32_t nh = 0;
     #pragma unroll
-        for (int i = 7; i >= 0; --i)
-            if (T[i] && mylast == kNoPos) {
-                const uint32_t b = 31 - __clz(T[i]);
-                mylast = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
-            }
-        // exclusive max-scan of mylast over the CTA
-        int32_t v = mylast;
+        for (int i = 0; i < 8; ++i) nh += __popc(T[i]);
+        // exclusive sum-scan of the prime counts over the CTA: this thread's
+        // primes are entries [off, off + nh) of the CTA's list in natural order
+        uint32_t v = nh;
     #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int32_t n = __shfl_up_sync(~0u, v, o);
-            if (lane >= uint32_t(o) && n > v) v = n;
+            const uint32_t n = __shfl_up_sync(~0u, v, o);
+            if (lane >= uint32_t(o)) v += n;
         }
-        int32_t excl = __shfl_up_sync(~0u, v, 1);
-        if (lane == 0) excl = kNoPos;
-        if (lane == 31) s_wlast[warp] = v;
+        if (lane == 31) s_wsum[warp] = v;
         __syncthreads();
-        int32_t prev = s_prev0;
-        if (excl > prev) prev = excl;
-        for (uint32_t i = 0; i < warp; ++i)
-            if (s_wlast[i] > prev) prev = s_wlast[i];
+        uint32_t off = v - nh, total = 0;
+        for (uint32_t i = 0; i < kCountThreads / 32; ++i) {
+            const uint32_t sw = s_wsum[i];
+            if (i < warp) off += sw;
+            total += sw;
+        }
 
-        // the primes in natural order: gaps of the counted ones, the hash of all
+        // the primes in natural order, kCountCap at a time: each thread
+        // writes its own into the list (phase 1), then the CTA takes the list
+        // in stride (phase 2: the hash of all, the gaps of the counted ones),
+        // so the per-prime work has no divergence between lanes
         const bool hash = !(sp.flags & GBC_SEG_NOHASH);
         uint64_t hsum = 0;
         uint32_t key = 0, err = 0;
         int32_t cfirst = INT32_MAX, clast = kNoPos;
+        int32_t carry = s_prev0;  // the prime before the round's first entry
+        for (uint32_t lo = 0; lo < total; lo += kCountCap) {
+            const uint32_t n = total - lo < kCountCap ? total - lo : kCountCap;
+            if (off < lo + n && off + nh > lo) {
+                uint32_t idx = off - lo;  // wraps below the round: skipped by idx < n
     #pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) {
-            uint32_t x = T[i];
-            nh += __popc(x);
-            while (x) {
-                const uint32_t b = __ffs(x) - 1u;
-                x &= x - 1u;
-                const int32_t pos = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+                for (uint32_t i = 0; i < 8; ++i) {
+                    uint32_t x = T[i];
+                    while (x) {
+                        const uint32_t b = __ffs(x) - 1u;
+                        x &= x - 1u;
+                        if (idx < n) s_pos[idx] = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+                        ++idx;
+                    }
+                }
+            }
+            __syncthreads();
+            for (uint32_t k = tid; k < n; k += kCountThreads) {
+                const int32_t pos = s_pos[k];
+                const int32_t prev = k ? s_pos[k - 1] : carry;
                 if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
                 if (pos >= clo && pos <= chi) {
                     if (pos < cfirst) cfirst = pos;
-                    clast = pos;
+                    if (pos > clast) clast = pos;
                     if (prev != kNoPos) {
                         const uint32_t g = uint32_t(pos - prev);
                         if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
@@ -211,8 +225,9 @@ __global__ void __launch_bounds__(kCountThreads) k_count(BatchDesc d)
                         err |= kErrNoPred;
                     }
                 }
-                prev = pos;
             }
+            carry = s_pos[n - 1];
+            __syncthreads();  // the list is rewritten by the next round
         }
         if (err) atomicOr(&sp.res->err, err);
 
