@@ -520,17 +520,53 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
 // ascending order (every plan member already failed for it), one thread per
 // pending word. The histogram and first occurrences of these evens hold
 // every even with p(n) >= the plan bound; ridges above the floor are listed.
-__global__ void __launch_bounds__(128) k_tail(BatchDesc d, VerifyTables vt)
+// The pending words of all segments of the batch form one index space (a
+// prefix over the segments' counts), so the segments' words are settled
+// side by side rather than one segment after another.
+constexpr int kTailThreads = 256;
+static_assert(kTailThreads >= 256, "one thread per segment of a batch for the prefix");
+
+__global__ void __launch_bounds__(kTailThreads) k_tail(BatchDesc d, VerifyTables vt)
 {
-    const uint32_t nseg = d.h->nseg;
-    for (uint32_t si = 0; si < nseg; ++si) {
+    __shared__ uint32_t s_pref[2][257];
+    const uint32_t nseg = d.h->nseg, tid = threadIdx.x;
+    // s_pref[.][s]: pending words of the segments before s (Hillis-Steele)
+    {
+        uint32_t c = 0;
+        if (tid < nseg) {
+            const SegParams &sp = d.segs[tid];
+            const uint32_t np = sp.res->npend;
+            c = sp.sampled ? 0u : (np < sp.pend_cap ? np : sp.pend_cap);
+        }
+        s_pref[0][tid + 1] = c;
+        if (tid == 0) s_pref[0][0] = s_pref[1][0] = 0;
+        __syncthreads();
+        uint32_t src = 0;
+        for (uint32_t o = 1; o < 256; o <<= 1, src ^= 1u) {
+            uint32_t v = s_pref[src][tid + 1];
+            if (tid >= o) v += s_pref[src][tid + 1 - o];
+            s_pref[src ^ 1u][tid + 1] = v;
+            __syncthreads();
+        }
+        if (src) {  // the result in s_pref[0]
+            s_pref[0][tid + 1] = s_pref[1][tid + 1];
+            __syncthreads();
+        }
+    }
+    const uint32_t total = s_pref[0][nseg];
+    for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = nseg;  // s_pref[lo] <= g < s_pref[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_pref[0][mid] <= g) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t si = lo, i = g - s_pref[0][lo];
         const SegParams &sp = d.segs[si];
-        if (sp.sampled) continue;
         const BatchParams &bp = d.runs[sp.run];
         gbc_segment_result *res = sp.res;
-        const uint32_t np = res->npend < sp.pend_cap ? res->npend : sp.pend_cap;
         const uint64_t seg_start = sp.seg_start, base = bp.base;
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        {
             const uint2 e = sp.pend[i];
             const uint32_t cr = e.x >> 27, j = e.x & ((1u << 27) - 1), r = 2 * cr;
             uint32_t mask = e.y;
@@ -606,7 +642,7 @@ void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Gri
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st)
 {
     gbk::k_verify<<<g.sm * g.verify, gbk::kCheckThreads, 0, st>>>(d, vt);
-    gbk::k_tail<<<g.sm * 2, 128, 0, st>>>(d, vt);
+    gbk::k_tail<<<g.sm * 2, gbk::kTailThreads, 0, st>>>(d, vt);
 }
 
 void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st)

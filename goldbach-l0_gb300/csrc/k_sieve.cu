@@ -520,11 +520,26 @@ __global__ void __launch_bounds__(256) k_hl_apply(BatchDesc d)
         const uint32_t bin = j / ctas, c = j - bin * ctas;
         const uint32_t k = bin / nreg, reg = bin - k * nreg;
         const uint32_t n = min(bp.hl_cnt[size_t(c) * nbin + bin], quota);
-        const uint32_t *e = bp.hl_buf + (size_t(c) * nbin + bin) * quota;
+        // the quota is a multiple of 32 words: 16-byte aligned groups of four
+        const uint4 *e = reinterpret_cast<const uint4 *>(bp.hl_buf + (size_t(c) * nbin + bin) * quota);
         uint32_t *wk = bp.map + size_t(k) * wpc + (size_t(reg) << (rlog - 5));
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            const uint32_t off = __ldcs(e + i);
-            atomicAnd(wk + (off >> 5), ~(1u << (off & 31)));
+        const uint32_t n4 = (n + 3) / 4;
+        // four groups per thread in flight before their marks
+        for (uint32_t i = threadIdx.x; i < n4; i += 4 * blockDim.x) {
+            uint4 v[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) {
+                const uint32_t iu = i + u * blockDim.x;
+                v[u] = iu < n4 ? __ldcs(e + iu) : make_uint4(0u, 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) {
+                const uint32_t at = 4 * (i + u * blockDim.x);
+                const uint32_t o4[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+                for (uint32_t x = 0; x < 4; ++x)
+                    if (at + x < n) atomicAnd(wk + (o4[x] >> 5), ~(1u << (o4[x] & 31)));
+            }
         }
         __syncthreads();
     }
