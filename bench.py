@@ -517,10 +517,11 @@ def run_gb300(args, rep):
     # launch per batch: the kernels are persistent over the batch's
     # segments). A segment's class map is one bit per q coprime to 30:
     # SEG / 30 bytes. The hit-list stage reads its primes once and the table
-    # bytes of their multiplier ranges, writes and reads back one 4-byte
-    # offset per semiprime mark (the marks counted by the density of q = p m,
-    # p >= p_hl, m prime), and reads and writes the maps once while it
-    # clears the marks region by region.
+    # bytes of their multiplier ranges and writes one 4-byte offset per
+    # semiprime mark (the marks counted by the density of q = p m, p >= p_hl,
+    # m prime) into region bins, then reads them back and writes them into
+    # tile bins; the tile stage reads the tile bins once and writes the maps
+    # once.
     import math
     seg_map = SEG / 30
     W = args.batch * SEG
@@ -533,8 +534,8 @@ def run_gb300(args, rep):
     table_bytes = W / 30 * math.log(u1 / u0) if u1 > u0 else 0.0
     maps = args.batch * seg_map
     per_stage = {
-        "tile": (["k_tile"], maps),                                              # the maps, written once
-        "large": (["k_hitlist", "k_hl_apply"], 4 * n_hl + table_bytes + 8 * marks + 2 * maps),
+        "tile": (["k_tile"], maps + 4 * marks),                                  # tile bins read, maps written
+        "large": (["k_hitlist", "k_binsort"], 4 * n_hl + table_bytes + 12 * marks),
         "check": (["k_verify", "k_tail"], maps),                                 # the maps, read once
         "count": (["k_count"], maps),                                            # the maps, read once
     }

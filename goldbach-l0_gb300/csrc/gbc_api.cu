@@ -244,6 +244,15 @@ static uint32_t hl_quota(double marks, uint32_t ctas, uint32_t nbin)
     return uint32_t(align_up(size_t(1.25 * marks / (double(ctas) * nbin)) + 64, 32));
 }
 
+// Offsets per tile bin: the expected marks of a tile + 15%, + 2048, whole
+// lines (the density is that of the run's top, where it is highest).
+static size_t tb_capacity(double marks_per_bit, uint32_t tile_log2)
+{
+    return align_up(size_t(1.15 * marks_per_bit * double(1u << tile_log2)) + 2048, 32);
+}
+
+constexpr uint32_t kOverflowCap = 1u << 22;  // overflow marks a binned batch may leave
+
 static int slot_alloc(gbc_ctx *ctx, Slot &s)
 {
     const auto &cfg = ctx->cfg;
@@ -277,6 +286,15 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks, ctas, 8 * nreg);
         CK(dev_alloc(ctx, &s.hl_buf, std::max<size_t>(s.hl_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.hl_cnt, size_t(ctas) * gbk::kHlMaxBins * 4));
+        // tile bins: wpc_cap is a whole number of tiles
+        const uint32_t tl2 = cfg.tile_log2;
+        s.tb_cnt_words = size_t(8) * ((size_t(ctx->wpc_cap) * 32) >> tl2);
+        s.tb_buf_words = s.tb_cnt_words * tb_capacity(marks / (8.0 * double(nblk)), tl2);
+        CK(dev_alloc(ctx, &s.tb_buf, std::max<size_t>(s.tb_buf_words, 1) * 4));
+        CK(dev_alloc(ctx, &s.tb_cnt, std::max<size_t>(s.tb_cnt_words, 1) * 4));
+        s.ovf_cap = kOverflowCap;
+        CK(dev_alloc(ctx, &s.ovf_buf, size_t(s.ovf_cap) * sizeof(uint2)));
+        CK(dev_alloc(ctx, &s.ovf_cnt, 4));
     }
     CK(cudaMallocHost(&s.desc_host, ctx->layout.bytes));
     std::memset(s.desc_host, 0, ctx->layout.bytes);
@@ -302,6 +320,10 @@ static void slot_free(Slot &s)
     cudaFree(s.desc_dev);
     cudaFree(s.hl_buf);
     cudaFree(s.hl_cnt);
+    cudaFree(s.tb_buf);
+    cudaFree(s.tb_cnt);
+    cudaFree(s.ovf_buf);
+    cudaFree(s.ovf_cnt);
     if (s.desc_host) cudaFreeHost(s.desc_host);
     cudaFree(s.chk_map);
     cudaFree(s.chk_desc_dev);
@@ -725,7 +747,7 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
     }
     img.h->nrun = nrun;
     img.h->nseg = uint32_t(nseg);
-    // a batch of one hit-listed run: marks binned by map region
+    // a batch of one hit-listed run: marks binned by map region, then by tile
     if (nrun == 1 && s.hl_buf && img.runs[0].n_hl < img.runs[0].n_all) {
         gbk::BatchParams &bp = img.runs[0];
         uint32_t rlog, nreg;
@@ -735,13 +757,23 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
                              hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
                                         double(ctx->primes[bp.n_all - 1]));
         const uint32_t quota = hl_quota(marks, ctas, nbin);
-        if (size_t(ctas) * nbin * quota <= s.hl_buf_words) {
+        const uint32_t tl2 = ctx->cfg.tile_log2;
+        const size_t tiles = size_t(8) * bp.tiles_pc, tcap = tb_capacity(marks / (8.0 * double(bp.nblk)), tl2);
+        const bool tb_fit = rlog >= tl2 && (uint64_t(1) << (rlog - tl2)) <= gbk::kSortMaxTiles &&
+                            tiles <= s.tb_cnt_words && tiles * tcap <= s.tb_buf_words && tcap < (1ull << 31);
+        if (size_t(ctas) * nbin * quota <= s.hl_buf_words && tb_fit) {
             bp.hl_buf = s.hl_buf;
             bp.hl_cnt = s.hl_cnt;
             bp.hl_quota = quota;
             bp.hl_rlog = rlog;
             bp.hl_nreg = nreg;
             bp.hl_ctas = ctas;
+            bp.tb_buf = s.tb_buf;
+            bp.tb_cnt = s.tb_cnt;
+            bp.tb_cap = uint32_t(tcap);
+            bp.ovf_buf = s.ovf_buf;
+            bp.ovf_cnt = s.ovf_cnt;
+            bp.ovf_cap = s.ovf_cap;
         }
     }
     finish_desc(ctx, img);
@@ -897,11 +929,13 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     CK(cudaMemcpyAsync(s.desc_dev, s.desc_host, ctx->layout.bytes, cudaMemcpyHostToDevice, st));
     gbh::launch_init(d, g, st);
     gbh::launch_xfirst(d, g, st);
-    gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, g, st);
+    gbh::launch_hitlist(d, false, g, st);  // binned batches: harvest into region bins
+    gbh::launch_binsort(d, g, st);         // ... then into tile bins
     CK(cudaEventRecordWithFlags(s.ev[1], st, rec));
+    gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, g, st);  // with the tile bins' marks
     gbh::launch_large(d, g, st);
-    gbh::launch_hitlist(d, g, st);
-    gbh::launch_hl_apply(d, g, st);
+    gbh::launch_hitlist(d, true, g, st);   // other batches: direct marks
+    gbh::launch_hl_overflow(d, g, st);
     CK(cudaEventRecordWithFlags(s.ev[2], st, rec));
     gbh::launch_check(d, ctx->ct, g, st);
     gbh::launch_verify(d, ctx->vt, g, st);
@@ -912,7 +946,7 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     return GBC_OK;
 }
 
-constexpr int kPipelineKernels = 12;
+constexpr int kPipelineKernels = 14;
 
 static int capture_slot(gbc_ctx *ctx, Slot &s)
 {
@@ -956,6 +990,7 @@ static int issue_selfcheck(gbc_ctx *ctx, Slot &s)
         bp.map = s.chk_map + (bp.map - s.map);
         bp.n_hl = bp.n_all;
         bp.hl_quota = 0;
+        bp.tb_cap = 0;
     }
     ci.h->n_hl_max = ci.h->n_all_max;
     ci.h->n_hl_min = ci.h->n_all_max;
@@ -1085,8 +1120,8 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
         cudaEventElapsedTime(&d, s.ev[3], s.ev[4]);
         if (s.did_selfcheck) cudaEventElapsedTime(&e, s.ev[4], s.ev[5]);
         times->ms_setup = 0;
-        times->ms_tile = a;
-        times->ms_large = b;
+        times->ms_large = a;  // hit lists: harvest and sort
+        times->ms_tile = b;   // the map: tiles with the sorted marks, large primes, other marks
         times->ms_check = c;
         times->ms_count = d;
         times->ms_selfcheck = e;

@@ -85,14 +85,29 @@ struct BatchParams {
     const uint32_t *mtab;     // bit k of byte i <-> m = m0 + 30 i + u_k is prime
     uint64_t m0, m1;          // the table covers m in [m0, m1]
     uint32_t bm1, bm2;        // base mod 1001 and mod 7429
-    // binned hit lists (a batch of one run): the harvest files each mark's
-    // offset in its (harvest CTA, region bin) quota, bin = class * hl_nreg +
-    // (t >> hl_rlog); k_hl_apply clears them region by region. hl_quota = 0:
-    // marks are cleared directly.
+    // binned hit lists (a batch of one run, hl_quota and tb_cap both set):
+    // the harvest files each mark's offset in its (harvest CTA, region bin)
+    // quota, bin = class * hl_nreg + (t >> hl_rlog); k_binsort moves them to
+    // one bin per tile; the tile kernel clears its tile's marks in shared
+    // memory before storing the tile. Marks beyond a quota or a tile bin's
+    // capacity go to the overflow list, cleared after the tiles. Otherwise
+    // the harvest clears its marks directly, after the tiles.
     uint32_t *hl_buf;         // hl_ctas * hl_nbin * hl_quota offsets
     uint32_t *hl_cnt;         // hl_ctas * hl_nbin counts (capped at the quota when read)
     uint32_t hl_quota, hl_rlog, hl_nreg, hl_ctas;
+    uint32_t *tb_buf;         // 8 * tiles_pc tile bins of tb_cap offsets within the tile
+    uint32_t *tb_cnt;         // 8 * tiles_pc counts (capped at tb_cap when read)
+    uint32_t tb_cap;          // multiple of 32
+    uint32_t ovf_cap;
+    uint2 *ovf_buf;           // (class, bit) of each overflow mark
+    uint32_t *ovf_cnt;
 };
+
+// a one-run batch whose hit lists go through the tile bins
+__host__ __device__ __forceinline__ bool hl_binned(const BatchParams &bp, uint32_t nrun)
+{
+    return nrun == 1 && bp.hl_quota != 0 && bp.tb_cap != 0;
+}
 
 struct GroupInfo {
     uint32_t P[kNumGroups];       // period (product of the group's primes)
@@ -150,7 +165,7 @@ struct BatchHeader {
     uint32_t work[5];
 };
 
-constexpr int kWorkTile = 0, kWorkCheck = 1, kWorkVerify = 2, kWorkCount = 3, kWorkHlApply = 4;
+constexpr int kWorkTile = 0, kWorkCheck = 1, kWorkVerify = 2, kWorkCount = 3, kWorkBinsort = 4;
 constexpr uint32_t kHlMaxBins = 64;  // region bins of a binned batch (8 classes x up to 8 regions)
 
 struct BatchDesc {
@@ -217,9 +232,13 @@ constexpr uint32_t kErrPendOverflow = 1u << 6;
 constexpr uint32_t kErrRidgeOverflow = 1u << 7;
 constexpr uint32_t kErrSelfCheck = 1u << 8;  // the map self-check found differing words
 constexpr uint32_t kErrStaging = 1u << 9;    // a bulk copy into shared memory missed its wait limit
+constexpr uint32_t kErrHlOverflow = 1u << 10; // more hit-list overflow marks than the overflow list holds
 
 // funnels per class the verify kernel holds (the plan has at most this many)
 constexpr uint32_t kVerifyMaxFun = 32;
+
+// tiles per hit-list region k_binsort handles
+constexpr uint32_t kSortMaxTiles = 1024;
 
 // ---------------------------------------------------------------------------
 // Bulk copies global -> shared memory (cp.async.bulk, the TMA unit's
@@ -360,8 +379,11 @@ void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
                  cudaStream_t st);
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
-void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
-void launch_hl_apply(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+// direct = false: the binned harvest (before the tiles); true: the direct
+// marks of every other batch (after the tiles)
+void launch_hitlist(const gbk::BatchDesc &d, bool direct, const Grids &g, cudaStream_t st);
+void launch_binsort(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
+void launch_hl_overflow(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 constexpr int kHitlistCtasPerSm = 8;  // k_hitlist's grid: SMs x this
 void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st);
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st);

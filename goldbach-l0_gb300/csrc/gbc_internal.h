@@ -34,8 +34,9 @@ struct DescImage {
 // reference's pipeline slot, src/verifier.cpp:48-50).
 struct Slot {
     cudaStream_t st = nullptr;
-    // 0 start, 1 tiles done, 2 large primes done, 3 checker done, 4 counts
-    // done (end of the pipeline), 5 end of the batch (after a self-check)
+    // 0 start, 1 hit lists harvested and sorted, 2 map done (tiles, large
+    // primes, direct and overflow marks), 3 checker done, 4 counts done (end
+    // of the pipeline), 5 end of the batch (after a self-check)
     cudaEvent_t ev[6] = {};
     uint32_t *map = nullptr;           // class maps of the batch's runs, back to back
     size_t map_words = 0;              // capacity (words, without the pad)
@@ -51,6 +52,15 @@ struct Slot {
     uint32_t *hl_buf = nullptr;
     size_t hl_buf_words = 0;
     uint32_t *hl_cnt = nullptr;
+    // their tile bins (8 x tiles per class of a full run, tb_cap offsets
+    // each) and the overflow list
+    uint32_t *tb_buf = nullptr;
+    size_t tb_buf_words = 0;
+    uint32_t *tb_cnt = nullptr;
+    size_t tb_cnt_words = 0;
+    uint2 *ovf_buf = nullptr;
+    uint32_t *ovf_cnt = nullptr;
+    uint32_t ovf_cap = 0;
     // the batch descriptor: pinned host image, device copy
     uint8_t *desc_host = nullptr, *desc_dev = nullptr;
     DescImage img;

@@ -594,7 +594,8 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(BatchDesc d, VerifyTables
 }
 
 // Result areas of the batch's segments: zero, except the first-occurrence
-// indices and the first prime (all ones: none yet); the slot's error word.
+// indices and the first prime (all ones: none yet); the slot's error word;
+// a binned batch's tile-bin and overflow counts.
 __global__ void __launch_bounds__(256) k_init(BatchDesc d)
 {
     constexpr uint32_t kWords = sizeof(gbc_segment_result) / 4;
@@ -603,6 +604,11 @@ __global__ void __launch_bounds__(256) k_init(BatchDesc d)
     const uint32_t nseg = d.h->nseg;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid == 0 && d.h->nrun) *d.runs[0].err = 0;
+    if (hl_binned(d.runs[0], d.h->nrun)) {  // the tile bins' counts and the overflow count
+        const BatchParams &bp = d.runs[0];
+        for (uint32_t i = tid; i < 8 * bp.tiles_pc; i += gridDim.x * blockDim.x) bp.tb_cnt[i] = 0;
+        if (tid == 0) *bp.ovf_cnt = 0;
+    }
     for (uint32_t si = 0; si < nseg; ++si) {
         uint32_t *w = reinterpret_cast<uint32_t *>(d.segs[si].res);
         for (uint32_t i = tid; i < kWords; i += gridDim.x * blockDim.x)

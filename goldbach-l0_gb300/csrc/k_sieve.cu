@@ -226,6 +226,29 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
             m = mn;
         }
     }
+    // a binned batch: the hit-list marks of this tile (offsets within it)
+    if (bp.tb_cap && bp.hl_quota) {
+        const uint32_t tile = k * bp.tiles_pc + (t0 >> bp.tile_log2);
+        const uint32_t n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
+        const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap);
+        // four groups of four per thread in flight before their marks
+        for (uint32_t i = tid; 4 * i < n; i += 4 * bs) {
+            uint4 v[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) {
+                const uint32_t g = i + u * bs;
+                v[u] = 4 * g < n ? __ldcs(e + g) : make_uint4(0u, 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) {
+                const uint32_t at = 4 * (i + u * bs);
+                if (at < n) atomicAnd(&s[v[u].x >> 5], ~(1u << (v[u].x & 31)));
+                if (at + 1 < n) atomicAnd(&s[v[u].y >> 5], ~(1u << (v[u].y & 31)));
+                if (at + 2 < n) atomicAnd(&s[v[u].z >> 5], ~(1u << (v[u].z & 31)));
+                if (at + 3 < n) atomicAnd(&s[v[u].w >> 5], ~(1u << (v[u].w & 31)));
+            }
+        }
+    }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(bp.map + size_t(k) * bp.wpc + (t0 >> 5));
     const uint4 *src = reinterpret_cast<const uint4 *>(s);
@@ -399,8 +422,20 @@ __device__ __forceinline__ uint32_t inv_mod_2_32(uint32_t p)
 // is cleared with an atomic AND. Every such q is a semiprime whose factors
 // are both above the sieving bound of the other stages, so the bit is set
 // and no read is needed.
-__global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
+__device__ __forceinline__ void ovf_push(const BatchParams &bp, uint32_t k, uint32_t t)
 {
+    const uint32_t slot = atomicAdd(bp.ovf_cnt, 1u);
+    if (slot < bp.ovf_cap) bp.ovf_buf[slot] = make_uint2(k, t);
+}
+
+// direct = 0: a binned batch's harvest (launched before the tiles); direct =
+// 1: every other batch's direct marks (launched after the tiles)
+__global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
+{
+    const uint32_t nrun = d.h->nrun;
+    if (!nrun) return;
+    const bool binned = hl_binned(d.runs[0], nrun);
+    if (binned == (direct != 0)) return;
     // per (class of p, class of m): the class kq of q = p m, its residue
     // u_kq and u_m, as kq | u_kq << 8 | u_m << 16; the class of a residue
     __shared__ uint32_t s_cls[8][8];
@@ -415,13 +450,11 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
     __shared__ uint32_t s_hcnt[kHlMaxBins];
     if (threadIdx.x < kHlMaxBins) s_hcnt[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t nrun = d.h->nrun;
-    if (!nrun) return;
-    // a batch of one run files its marks in region bins (see k_hl_apply)
-    const BatchParams &r0 = d.runs[0];
-    const uint32_t quota = nrun == 1 ? r0.hl_quota : 0u;
-    const uint32_t rlog = r0.hl_rlog, nreg = r0.hl_nreg, nbin = 8 * nreg;
-    uint32_t *const hl_mine = quota ? r0.hl_buf + size_t(blockIdx.x) * nbin * quota : nullptr;
+    // a binned batch files its marks in region bins (k_binsort takes them on)
+    const BatchParams &run0 = d.runs[0];
+    const uint32_t quota = binned ? run0.hl_quota : 0u;
+    const uint32_t rlog = run0.hl_rlog, nreg = run0.hl_nreg, nbin = 8 * nreg;
+    uint32_t *const hl_mine = quota ? run0.hl_buf + size_t(blockIdx.x) * nbin * quota : nullptr;
     // bit r set for the units r mod 30: the classes below a residue
     constexpr uint32_t kUnits = (1u << 1) | (1u << 7) | (1u << 11) | (1u << 13) | (1u << 17) | (1u << 19) |
                                 (1u << 23) | (1u << 29);
@@ -485,10 +518,9 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
                     if (quota) {
                         const uint32_t bin = (e & 0xFFu) * nreg + (t >> rlog);
                         const uint32_t pos = atomicAdd(&s_hcnt[bin], 1u);
-                        if (pos < quota) {
-                            hl_mine[size_t(bin) * quota + pos] = t & ((1u << rlog) - 1u);
-                            continue;
-                        }
+                        if (pos < quota) hl_mine[size_t(bin) * quota + pos] = t & ((1u << rlog) - 1u);
+                        else ovf_push(run0, e & 0xFFu, t);
+                        continue;
                     }
                     atomicAnd(map + size_t(e & 0xFFu) * wpc + (t >> 5), ~(1u << (t & 31)));
                 }
@@ -497,51 +529,124 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d)
     }
     if (quota) {
         __syncthreads();
-        for (uint32_t b = threadIdx.x; b < nbin; b += blockDim.x) r0.hl_cnt[blockIdx.x * nbin + b] = s_hcnt[b];
+        for (uint32_t b = threadIdx.x; b < nbin; b += blockDim.x) run0.hl_cnt[blockIdx.x * nbin + b] = s_hcnt[b];
     }
 }
 
-// Binned hit lists, applied: every CTA's marks of region bin 0 first (all
-// CTAs of the kernel on one map region of at most 2^28 bits of one class at
-// a time), then bin 1, ..., so the atomic ANDs find their words in L2
-// instead of making a DRAM read-modify-write each.
-__global__ void __launch_bounds__(256) k_hl_apply(BatchDesc d)
+// exclusive prefix sums of in[0, n) into out (n <= 4 * 256; 256 threads;
+// the caller synchronises before reading out or reusing s_wsum)
+__device__ __forceinline__ void block_excl_scan4(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *s_wsum)
 {
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t v[4], sum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; ++j) {
+        const uint32_t idx = 4 * tid + j;
+        v[j] = idx < n ? in[idx] : 0u;
+        sum += v[j];
+    }
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(~0u, x, o);
+        if (lane >= uint32_t(o)) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t run = x - sum;
+    for (uint32_t i = 0; i < warp; ++i) run += s_wsum[i];
+#pragma unroll
+    for (uint32_t j = 0; j < 4; ++j) {
+        const uint32_t idx = 4 * tid + j;
+        if (idx < n) out[idx] = run;
+        run += v[j];
+    }
+}
+
+constexpr uint32_t kSortPer = 16;                   // offsets per thread and chunk (four uint4)
+constexpr uint32_t kSortChunk = 256 * kSortPer;     // offsets a CTA sorts in shared memory at a time
+
+// Binned hit lists, sorted by tile: every (harvest CTA, region bin) list,
+// kSortChunk offsets at a time (read once, into registers), is counted per
+// tile of its region, given room in each tile's bin by one atomic add per
+// tile, sorted by tile in shared memory and stored tile run by tile run
+// (consecutive threads, consecutive addresses). Offsets beyond a tile bin's
+// capacity go to the overflow list. The lists start 16-byte aligned (the
+// quota is a multiple of 32 words).
+__global__ void __launch_bounds__(256) k_binsort(BatchDesc d)
+{
+    __shared__ uint32_t s_out[kSortChunk];
+    __shared__ uint32_t s_cnt[kSortMaxTiles], s_start[kSortMaxTiles], s_gbase[kSortMaxTiles];
+    __shared__ uint32_t s_wsum[8];
     __shared__ uint32_t s_j;
-    if (d.h->nrun != 1) return;
+    if (!hl_binned(d.runs[0], d.h->nrun)) return;
     const BatchParams &bp = d.runs[0];
-    const uint32_t quota = bp.hl_quota;
-    if (!quota) return;
-    const uint32_t nreg = bp.hl_nreg, nbin = 8 * nreg, ctas = bp.hl_ctas, rlog = bp.hl_rlog;
-    const uint32_t items = nbin * ctas, wpc = bp.wpc;
+    const uint32_t tid = threadIdx.x, bs = blockDim.x;
+    const uint32_t quota = bp.hl_quota, nreg = bp.hl_nreg, nbin = 8 * nreg, ctas = bp.hl_ctas;
+    const uint32_t rlog = bp.hl_rlog, tl2 = bp.tile_log2, tpr = 1u << (rlog - tl2), tmask = (1u << tl2) - 1u;
+    const uint32_t items = nbin * ctas, cap = bp.tb_cap;
     for (;;) {
-        const uint32_t j = next_item(d.work + kWorkHlApply, &s_j);
+        const uint32_t j = next_item(d.work + kWorkBinsort, &s_j);
         if (j >= items) break;
         const uint32_t bin = j / ctas, c = j - bin * ctas;
         const uint32_t k = bin / nreg, reg = bin - k * nreg;
         const uint32_t n = min(bp.hl_cnt[size_t(c) * nbin + bin], quota);
-        // the quota is a multiple of 32 words: 16-byte aligned groups of four
-        const uint4 *e = reinterpret_cast<const uint4 *>(bp.hl_buf + (size_t(c) * nbin + bin) * quota);
-        uint32_t *wk = bp.map + size_t(k) * wpc + (size_t(reg) << (rlog - 5));
-        const uint32_t n4 = (n + 3) / 4;
-        // four groups per thread in flight before their marks
-        for (uint32_t i = threadIdx.x; i < n4; i += 4 * blockDim.x) {
-            uint4 v[4];
+        const uint32_t *e = bp.hl_buf + (size_t(c) * nbin + bin) * quota;
+        const uint32_t tile0 = k * bp.tiles_pc + (reg << (rlog - tl2));
+        for (uint32_t cs = 0; cs < n; cs += kSortChunk) {
+            const uint32_t m = min(n - cs, kSortChunk);
+            for (uint32_t t = tid; t < tpr; t += bs) s_cnt[t] = 0;
+            // this thread's offsets: groups of four at tid + 256 u (kNone past the end)
+            uint32_t v[kSortPer];
+            const uint4 *e4 = reinterpret_cast<const uint4 *>(e + cs);
 #pragma unroll
-            for (uint32_t u = 0; u < 4; ++u) {
-                const uint32_t iu = i + u * blockDim.x;
-                v[u] = iu < n4 ? __ldcs(e + iu) : make_uint4(0u, 0u, 0u, 0u);
+            for (uint32_t u = 0; u < kSortPer / 4; ++u) {
+                const uint32_t g = tid + bs * u;
+                const uint4 q = 4 * g < m ? __ldcs(e4 + g) : make_uint4(kNone, kNone, kNone, kNone);
+                v[4 * u] = q.x;
+                v[4 * u + 1] = 4 * g + 1 < m ? q.y : kNone;
+                v[4 * u + 2] = 4 * g + 2 < m ? q.z : kNone;
+                v[4 * u + 3] = 4 * g + 3 < m ? q.w : kNone;
             }
+            __syncthreads();
 #pragma unroll
-            for (uint32_t u = 0; u < 4; ++u) {
-                const uint32_t at = 4 * (i + u * blockDim.x);
-                const uint32_t o4[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-#pragma unroll
-                for (uint32_t x = 0; x < 4; ++x)
-                    if (at + x < n) atomicAnd(wk + (o4[x] >> 5), ~(1u << (o4[x] & 31)));
+            for (uint32_t u = 0; u < kSortPer; ++u)
+                if (v[u] != kNone) atomicAdd(&s_cnt[v[u] >> tl2], 1u);
+            __syncthreads();
+            block_excl_scan4(s_cnt, s_start, tpr, s_wsum);
+            __syncthreads();
+            for (uint32_t t = tid; t < tpr; t += bs) {
+                const uint32_t cn = s_cnt[t];
+                s_gbase[t] = cn ? atomicAdd(bp.tb_cnt + tile0 + t, cn) : 0u;
+                s_cnt[t] = s_start[t];
             }
+            __syncthreads();
+#pragma unroll
+            for (uint32_t u = 0; u < kSortPer; ++u)
+                if (v[u] != kNone) s_out[atomicAdd(&s_cnt[v[u] >> tl2], 1u)] = v[u];
+            __syncthreads();
+            for (uint32_t i = tid; i < m; i += bs) {
+                const uint32_t off = s_out[i], t = off >> tl2;
+                const uint32_t pos = s_gbase[t] + (i - s_start[t]);
+                if (pos < cap) bp.tb_buf[size_t(tile0 + t) * cap + pos] = off & tmask;
+                else ovf_push(bp, k, (reg << rlog) + off);
+            }
+            __syncthreads();
         }
-        __syncthreads();
+    }
+}
+
+// The overflow list of a binned batch, cleared after the tiles.
+__global__ void __launch_bounds__(256) k_hl_overflow(BatchDesc d)
+{
+    if (!hl_binned(d.runs[0], d.h->nrun)) return;
+    const BatchParams &bp = d.runs[0];
+    const uint32_t cnt = *bp.ovf_cnt;
+    if (cnt > bp.ovf_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bp.err, kErrHlOverflow);
+    const uint32_t n = min(cnt, bp.ovf_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint2 e = bp.ovf_buf[i];
+        atomicAnd(bp.map + size_t(e.x) * bp.wpc + (e.y >> 5), ~(1u << (e.y & 31)));
     }
 }
 
@@ -631,14 +736,19 @@ void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
     gbk::k_large<<<g.sm * 8, 256, 0, st>>>(d);
 }
 
-void launch_hitlist(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+void launch_hitlist(const gbk::BatchDesc &d, bool direct, const Grids &g, cudaStream_t st)
 {
-    gbk::k_hitlist<<<g.sm * kHitlistCtasPerSm, 256, 0, st>>>(d);
+    gbk::k_hitlist<<<g.sm * kHitlistCtasPerSm, 256, 0, st>>>(d, direct ? 1u : 0u);
 }
 
-void launch_hl_apply(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+void launch_binsort(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 {
-    gbk::k_hl_apply<<<g.sm * 8, 256, 0, st>>>(d);
+    gbk::k_binsort<<<g.sm * 4, 256, 0, st>>>(d);
+}
+
+void launch_hl_overflow(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
+{
+    gbk::k_hl_overflow<<<g.sm * 2, 256, 0, st>>>(d);
 }
 
 void launch_xfirst1(const gbk::BatchParams &bp, cudaStream_t st)
