@@ -70,6 +70,35 @@ bool parse_count(const char *s, uint64_t &out)
     return true;
 }
 
+// The run's ridge store, records file and live snapshot at the reference's
+// paths (src/verifier.cpp:725-745, include/gstats.hpp:474-478):
+// GB_RIDGE_FILE (goldbach_ridges.csv; GB_RIDGE=0 turns ridges off),
+// GB_RECORDS_FILE (goldbach_records.txt), GB_STATS_LIVE (goldbach_live.json);
+// a variable set but empty turns its output off. The record hook is
+// GB_RECORD_HOOK (set but empty: none), else scripts/notify_record.sh when
+// present.
+void attach_outputs(gbc_ctx *ctx)
+{
+    auto path = [](const char *var, const char *def) -> std::string {
+        const char *v = std::getenv(var);
+        return v ? v : def;
+    };
+    const char *rg = std::getenv("GB_RIDGE");
+    const bool ridge_on = !(rg && (!std::strcmp(rg, "0") || !std::strcmp(rg, "off")));
+    const std::string ridge = ridge_on ? path("GB_RIDGE_FILE", "goldbach_ridges.csv") : "";
+    const std::string rec = path("GB_RECORDS_FILE", "goldbach_records.txt");
+    const std::string live = path("GB_STATS_LIVE", "goldbach_live.json");
+    const char *hk = std::getenv("GB_RECORD_HOOK");
+    std::string hook = hk ? hk : "";
+    if (!hk)
+        if (std::FILE *f = std::fopen("scripts/notify_record.sh", "rb")) {
+            std::fclose(f);
+            hook = "bash scripts/notify_record.sh";
+        }
+    if (gbc_set_outputs(ctx, ridge.c_str(), rec.c_str(), live.c_str(), hook.c_str()) != GBC_OK)
+        std::fprintf(stderr, "outputs: %s\n", gbc_last_error(ctx));
+}
+
 int usage()
 {
     std::fprintf(stderr,
@@ -124,20 +153,21 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "limit %" PRIu64 " is above the supported maximum 2^64 - 2^40\n", limit);
         return 1;
     }
-    if (slice || !journal.empty()) {
-        if (!slice || journal.empty()) return usage();
-        gbc_config cfg{};
-        cfg.limit = limit & ~uint64_t(1);
-        cfg.segment_even = segment;
-        cfg.max_batch = uint32_t(batch);
-        cfg.sample_every = uint32_t(sample);
-        gbc_ctx *ctx = nullptr;
-        const int rc = gbc_create(&cfg, &ctx);
-        if (rc != GBC_OK) {
-            std::fprintf(stderr, "FAIL: gbc_create: %s\n", gbc_last_error(ctx));
-            gbc_destroy(ctx);
-            return rc == GBC_E_ARG ? 2 : 1;
-        }
+    if ((slice != 0) != !journal.empty()) return usage();
+    gbc_config cfg{};
+    cfg.limit = limit & ~uint64_t(1);
+    cfg.segment_even = segment;
+    cfg.max_batch = uint32_t(batch);
+    cfg.sample_every = uint32_t(sample);
+    gbc_ctx *ctx = nullptr;
+    const int rc = gbc_create(&cfg, &ctx);
+    if (rc != GBC_OK) {
+        std::fprintf(stderr, "FAIL: gbc_create: %s\n", gbc_last_error(ctx));
+        gbc_destroy(ctx);
+        return rc == GBC_E_ARG ? 2 : 1;
+    }
+    attach_outputs(ctx);
+    if (slice) {
         int code = 0;
         try {
             int stopped = 0;
@@ -151,11 +181,17 @@ int main(int argc, char **argv)
         gbc_destroy(ctx);
         return code;
     }
+    int code = 0;
     try {
-        const gb::RunStats st = gb::run_gpu(limit, segment, verbose, start, uint32_t(batch), nullptr, uint32_t(sample));
+        gbc_get_config(ctx, &cfg);
+        const gb::RunStats st = gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, nullptr, nullptr,
+                                              cfg.sample_every);
+        if (verbose)
+            std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",
+                         st.start, st.limit, st.segments, st.gpu_seconds, st.wall_seconds);
         const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
         if (csv)
-            std::printf("%s\n", gb::csv_line(st, segment).c_str());
+            std::printf("%s\n", gb::csv_line(st, cfg.segment_even).c_str());
         else
             std::printf("PASS: every even n in [%" PRIu64 ", %" PRIu64 "] is a sum of two primes "
                         "(%" PRIu64 " evens, largest p(n) %" PRIu64 ", %.3f G evens/s)\n",
@@ -164,12 +200,13 @@ int main(int argc, char **argv)
             std::printf("%s\n", st.gbstats_line.c_str());
             if (!st.stats_line.empty()) std::printf("%s\n", st.stats_line.c_str());
         }
-        return 0;
     } catch (const gb::GbcError &e) {
         std::fprintf(stderr, "FAIL: %s\n", e.what());
-        return e.code == GBC_E_ARG ? 2 : 1;
+        code = e.code == GBC_E_ARG ? 2 : 1;
     } catch (const std::exception &e) {
         std::fprintf(stderr, "FAIL: %s\n", e.what());
-        return 1;
+        code = 1;
     }
+    gbc_destroy(ctx);
+    return code;
 }

@@ -129,7 +129,7 @@ void RunAccumulator::add_beyond(uint64_t n, uint64_t p)
 void RunAccumulator::note_ridge(uint64_t n, uint64_t p)
 {
     const Ridge x{n, p};
-    auto better = [](const Ridge &a, const Ridge &b) { return a.p != b.p ? a.p > b.p : a.n < b.n; };
+    auto better = [](const Ridge &a, const Ridge &b) { return a.p != b.p ? a.p > b.p : a.n > b.n; };
     for (const Ridge &r : ridges_)
         if (r.n == n) return;
     if (ridges_.size() == 30 && !better(x, ridges_.back())) return;
@@ -222,6 +222,28 @@ uint64_t RunAccumulator::tail_evens() const
     for (uint64_t v : tail_) t += v;
     for (auto &b : beyond_) t += b.second.first;
     return t;
+}
+
+uint64_t RunAccumulator::count_ge(uint64_t p) const
+{
+    uint64_t t = 0;
+    for (int i = 0; i < GBC_NCAND; ++i)
+        if (cand_[i] >= p) t += tail_[i];
+    for (auto &b : beyond_)
+        if (b.first >= p) t += b.second.first;
+    return t;
+}
+
+std::pair<uint64_t, uint64_t> RunAccumulator::pmax_first() const
+{
+    std::pair<uint64_t, uint64_t> m{0, 0};
+    for (int i = GBC_NCAND - 1; i >= 0 && !m.first; --i) {
+        if (tail_[i] && first_tail_[i]) m = {cand_[i], first_tail_[i]};
+        else if (first_all_[i]) m = {cand_[i], first_all_[i]};
+    }
+    for (auto &b : beyond_)
+        if (b.first > m.first) m = {b.first, b.second.second};
+    return m;
 }
 
 uint64_t RunAccumulator::gap_count() const
@@ -409,6 +431,9 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
     }
     std::vector<gbc_segment_result> out[2];
     double gpu_ms = 0;
+    Outputs *outs = outputs_of(ctx);
+    const std::vector<uint16_t> cand = outs ? candidates() : std::vector<uint16_t>();
+    const uint64_t evens_total = (limit - start) / 2 + 1;
     auto collect = [&](size_t b) {
         const int slot = int(b & 1);
         const int n = int(batches[b].size());
@@ -422,11 +447,16 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
         st.count_ms += tm.ms_count;
         for (int i = 0; i < n; ++i) {
             acc.add_segment(out[slot][i]);
+            if (outs) outs->add_segment(out[slot][i], cand);
             if (pn) {
                 const auto &r = out[slot][i];
                 check(ctx, gbc_copy_pn(ctx, slot, i, pn + (r.seg_start - start) / 2, r.evens), "copy p(n)");
             }
         }
+        if (outs)
+            outs->write_live(start, limit, acc.evens(), evens_total,
+                             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), acc,
+                             b + 1 == batches.size());
     };
     for (size_t b = 0; b < batches.size(); ++b) {
         std::vector<uint64_t> bounds;
@@ -454,6 +484,7 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
     st.stats_line = acc.stats_ref_line();
     st.gbstats_line = acc.gbstats_line("gb300-1.0");
     st.ridges = acc.ridges();
+    if (outs) outs->finish_run();
     if (acc_out) *acc_out = acc;
     return st;
 }

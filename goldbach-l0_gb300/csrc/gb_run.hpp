@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <map>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -23,7 +24,7 @@ struct GbcError : std::runtime_error {
 };
 
 // Top-30 smallest-witness records (the reference's RidgeTracker,
-// include/ridge.hpp:98-237): (even n, p(n)), p descending, n ascending on ties.
+// include/ridge.hpp:63-237): (even n, p(n)), p descending, n descending on ties.
 struct Ridge {
     uint64_t n = 0, p = 0;
 };
@@ -59,6 +60,8 @@ public:
     uint64_t twins() const;
     uint64_t pmax() const;        // largest p(n) seen (tail or sampled)
     uint64_t tail_evens() const;
+    uint64_t count_ge(uint64_t p) const;               // evens with p(n) >= p (p >= the tail bound)
+    std::pair<uint64_t, uint64_t> pmax_first() const;  // largest p(n) and its first even
     uint64_t gap_count() const;
     bool fully_sampled() const { return evens_sampled_ == evens_; }
     std::string stats_ref_line() const;
@@ -88,6 +91,62 @@ private:
     std::map<uint32_t, std::pair<uint64_t, uint64_t>> tail_gaps_; // g -> (count, first lower)
     std::vector<Ridge> ridges_;
 };
+
+// Deterministic 64-bit primality (Miller-Rabin) and p(n) by an ascending
+// scan: the CPU re-proof of ridges and record events (gb_records.cpp).
+bool is_prime_u64(uint64_t n);
+uint64_t pn_exact(uint64_t n);
+
+struct RidgeRow {
+    uint64_t n = 0, p = 0, q = 0, seg = 0, found = 0;
+};
+
+// The top 30 ridges with every entry proved on the CPU (include/ridge.hpp:
+// 63-237): larger p first, the larger even first on ties.
+class RidgeStore {
+public:
+    static constexpr size_t kKeep = 30;
+    explicit RidgeStore(uint32_t floor = GBC_TAIL_T) : floor_(floor) {}
+    bool consider(uint64_t n, uint64_t p, uint64_t seg, uint64_t found = UINT64_MAX);
+    bool load(const std::string &path);
+    bool save(const std::string &path);  // rewritten atomically when the top changed
+    const std::vector<RidgeRow> &top() const { return top_; }
+    uint64_t appends() const { return appends_; }
+    uint64_t dropped() const { return dropped_; }
+
+private:
+    std::vector<RidgeRow> top_;
+    uint32_t floor_;
+    uint64_t appends_ = 0, dropped_ = 0;
+    bool changed_ = false;
+};
+
+class RunAccumulator;
+
+// A context's ridge store, records file (+ hook) and live snapshot.
+class Outputs {
+public:
+    Outputs(const char *ridge_csv, const char *records, const char *live_json, const char *hook,
+            uint32_t ridge_floor);
+    void add_segment(const gbc_segment_result &r, const std::vector<uint16_t> &cand);
+    void note_beyond(uint64_t n, uint64_t p);
+    void note_first(uint64_t n, uint64_t p);
+    void write_live(uint64_t start, uint64_t limit, uint64_t evens_done, uint64_t evens_total, double elapsed,
+                    const RunAccumulator &acc, bool force);
+    void finish_run();
+    const RidgeStore &ridges() const { return ridges_; }
+
+private:
+    void record(uint64_t n, uint64_t p, const char *kind, const char *what);
+    std::string ridge_csv_, records_, live_json_, hook_;
+    RidgeStore ridges_;
+    std::set<uint64_t> sp_seen_;
+    std::vector<std::pair<uint64_t, uint64_t>> events_;  // (n, p) recorded by this context
+    long long live_t_ = 0;
+};
+
+// the outputs attached to a context by gbc_set_outputs, or nullptr
+Outputs *outputs_of(gbc_ctx *ctx);
 
 // Segments of a run: segment_even integers each, the lowest one short
 // (it takes the generic checker), the last one ragged.

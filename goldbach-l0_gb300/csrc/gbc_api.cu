@@ -554,6 +554,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
 extern "C" void gbc_destroy(gbc_ctx *ctx)
 {
     if (!ctx) return;
+    if (ctx->outputs && ctx->outputs_del) ctx->outputs_del(ctx->outputs);
     for (auto &s : ctx->slot) slot_free(s);
     cudaFree(ctx->d_fun);
     cudaFree(ctx->d_rest);
@@ -569,6 +570,15 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
 }
 
 // the run driver's (gb_run.cpp) failure text for gbc_last_error
+void gbh_set_outputs(gbc_ctx *ctx, void *p, void (*del)(void *))
+{
+    if (ctx->outputs && ctx->outputs_del) ctx->outputs_del(ctx->outputs);
+    ctx->outputs = p;
+    ctx->outputs_del = del;
+}
+
+void *gbh_outputs(gbc_ctx *ctx) { return ctx ? ctx->outputs : nullptr; }
+
 void gbh_set_error(gbc_ctx *ctx, const char *msg)
 {
     if (ctx) ctx->err = msg;

@@ -93,6 +93,9 @@ struct gbc_ctx {
     gbk::VerifyTables vt{};
     std::vector<Slot> slot;
     std::string err;
+    // host outputs of runs on this context (gb_records.cpp), owned
+    void *outputs = nullptr;
+    void (*outputs_del)(void *) = nullptr;
     uint64_t launches = 0, batches = 0, graph_replays = 0, selfchecks = 0, hl_batches = 0;
     uint64_t device_bytes = 0;
     // prime-multiplier table (hit lists for the primes >= p_hl)

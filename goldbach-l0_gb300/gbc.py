@@ -125,6 +125,11 @@ SIGNATURES = {
     "gbc_journal_resume": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "gbc_run_slices": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_char_p, C.c_char_p,
                                  C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
+    "gbc_set_outputs": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p]),
+    "gbc_ridges_merge": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                   C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "gbc_record_event": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint64, C.c_uint64, C.c_int]),
+    "gbc_pn_exact": (C.c_uint64, [C.c_uint64]),
     "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
@@ -280,6 +285,12 @@ class Context:
                                             C.byref(stopped)))
         return done.value, bool(stopped.value)
 
+    def set_outputs(self, ridge_csv=None, records=None, live_json=None, hook=None):
+        """Ridge store, records file (+ hook) and live snapshot of this
+        context's runs; None turns one off."""
+        enc = lambda x: str(x).encode() if x else None  # noqa: E731
+        self._check(self.lib.gbc_set_outputs(self.h, enc(ridge_csv), enc(records), enc(live_json), enc(hook)))
+
     def verify_range(self, start, limit, want_pn=False):
         """Returns (RunResult, stats_ref line, p(n) array or None)."""
         res = RunResult()
@@ -299,6 +310,33 @@ def journal_resume(path, start):
     if rc:
         raise GbcError(rc, "journal")
     return n.value
+
+
+def ridges_merge(path, entries, floor=3):
+    """Merges (n, p, segment start) entries into the ridge store at path
+    (each proved on the CPU first); returns the rows kept."""
+    k = len(entries)
+    n = (C.c_uint64 * max(k, 1))(*[e[0] for e in entries])
+    p = (C.c_uint64 * max(k, 1))(*[e[1] for e in entries])
+    sg = (C.c_uint64 * max(k, 1))(*[e[2] for e in entries])
+    kept = C.c_uint32()
+    rc = load().gbc_ridges_merge(str(path).encode(), n, p, sg, k, floor, C.byref(kept))
+    if rc:
+        raise GbcError(rc, "ridge store")
+    return kept.value
+
+
+def record_event(records, n, p, first=False, hook=None):
+    """One record event (RECORD / BEYOND, or SP with first=True) into the
+    records file."""
+    rc = load().gbc_record_event(str(records).encode(), str(hook).encode() if hook else None, n, p, 1 if first else 0)
+    if rc:
+        raise GbcError(rc, "record")
+
+
+def pn_exact(n):
+    """p(n) by a CPU Miller-Rabin scan (0: none)."""
+    return load().gbc_pn_exact(n)
 
 
 class Server:

@@ -359,6 +359,39 @@ int gbc_journal_resume(const char *path, uint64_t start, uint64_t *next);
 int gbc_run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const char *journal,
                    const char *release, const char *stop_file, uint64_t *slices_done, int *stopped);
 
+/* ---- ridge store, records, live snapshot ------------------------------------
+ * Host outputs of gbc_verify_range and gbc_run_slices on ctx (the
+ * reference's RidgeTracker store, include/ridge.hpp:31-35, 196-237, and its
+ * records file, hook and live snapshot, include/gstats.hpp:774-868; the
+ * reference opens them from GB_RIDGE_FILE, GB_RECORDS_FILE, GB_STATS_LIVE,
+ * GB_RECORD_HOOK, which the command-line front end reads):
+ *   ridge_csv  the top 30 ridges, "rank,even,p,q,segment_start,found_unix"
+ *              rows, loaded now (every row re-proved on the CPU: p, n - p
+ *              prime, no smaller witness), rewritten atomically at the end
+ *              of a run whose ridges changed it
+ *   records    appended with one line per RECORD (p(n) > 9781), BEYOND or
+ *              SP (the campaign's first even with p(n) = p for a p whose
+ *              first occurrence is unknown below 4e18; an SP line already in
+ *              the file marks p as found) event, each re-proved by a CPU scan
+ *   live_json  a one-line JSON snapshot, at most every 2 s and at the end
+ *   hook       run in the background per event as `hook KIND P N Q CHECK`
+ * NULL or "" turns one off; all NULL detaches the outputs. */
+int gbc_set_outputs(gbc_ctx *ctx, const char *ridge_csv, const char *records, const char *live_json,
+                    const char *hook);
+
+/* The ridge store at path with count more (n, p, segment start) candidates
+ * merged (each proved first; floor: the smallest p kept); *kept = rows. */
+int gbc_ridges_merge(const char *path, const uint64_t *n, const uint64_t *p, const uint64_t *seg, uint32_t count,
+                     uint32_t floor, uint32_t *kept);
+
+/* One record event for (n, p) into the records file: first = 0: RECORD or
+ * BEYOND; first = 1: SP when p is one of the unknown-S(p) primes and no SP
+ * line for p is in the file. */
+int gbc_record_event(const char *records, const char *hook, uint64_t n, uint64_t p, int first);
+
+/* p(n) by an ascending Miller-Rabin scan on the CPU (0: none <= n / 2). */
+uint64_t gbc_pn_exact(uint64_t n);
+
 /* ---- allocation-free class map ---------------------------------------------
  * This entry point has no counterpart in the reference.
  *

@@ -218,3 +218,26 @@ def test_journaled_slices_resume_and_stop(tmp_path):
         want = dict(t.split("=", 1) for t in oracle.stats_line(int(r[1]), int(r[2]), oracle.SIEVE).split())
         assert got["result"] == "PASS" and got["release"] == "gb300-1.0"
         assert (got["primes"], got["twins"], got["stats_pmax"]) == (want["primes"], want["twins"], want["pmax"])
+
+
+def test_run_outputs_ridges_live_records(tmp_path):
+    """A run's ridge store, live snapshot and records file: the top 30
+    ridges, the totals and the largest p(n) equal the oracle's; no record
+    events at 1e15."""
+    import json
+    a, count = 10**15, 2_000_000
+    b = a + 2 * (count - 1)
+    st, live, rec = tmp_path / "ridges.csv", tmp_path / "live.json", tmp_path / "records.txt"
+    with gbc.Context(limit=b, segment_even=1_000_000, max_batch=4, ridge_min=1000) as c:
+        c.set_outputs(st, rec, live)
+        res, _, _ = c.verify_range(a, b)
+    pn = list(oracle.pn_range(a, count))
+    want = sorted(((a + 2 * i, p) for i, p in enumerate(pn) if p >= 1000), key=lambda e: (-e[1], -e[0]))[:30]
+    got = [tuple(int(x) for x in ln.split(",")[1:3]) for ln in st.read_text().splitlines()
+           if ln and not ln.startswith("#")]
+    assert got == want
+    j = json.loads(live.read_text())
+    assert (j["start"], j["limit"], j["evens_done"], j["evens_total"]) == (a, b, count, count)
+    assert (j["primes"], j["twins"]) == (res.primes, res.twins)
+    assert (j["pmax"], j["pmax_n"]) == (max(pn), a + 2 * pn.index(max(pn)))
+    assert j["events"] == [] and (not rec.exists() or rec.read_text() == "")
