@@ -254,7 +254,8 @@ def plain_leg(gbc, start, nseg, first_seg, knobs=None):
     loop."""
     segs = [(start + i * SEG, start + i * SEG + SEG - 2) for i in range(first_seg, first_seg + 2 * nseg + 1)]
     limit = segs[-1][1]
-    k = {n: v for n, v in (knobs or {}).items() if n in ("p_mid", "mtab_max_gb", "tile_log2", "plan_funnels")}
+    k = {n: v for n, v in (knobs or {}).items()
+         if n in ("p_mid", "mtab_max_gb", "tile_log2", "plan_funnels", "verify_funnels")}
     with gbc.Context(limit=limit, segment_even=SEG, max_batch=1, launch_mode=2, hl_mode=1, **k) as ctx:
         for sl in (0, 1):                                     # warm-up: tables, both slots
             ctx.enqueue_batch(sl, [segs[0]], limit, [gbc.SEG_VERIFY])
@@ -574,6 +575,7 @@ def run_gb300(args, rep):
                          f"of sieving primes per step",
                    "tile_log2": cfg.tile_log2, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
                    "mtab_max_gb": cfg.mtab_max_gb, "plan_funnels": cfg.plan_funnels,
+                   "verify_funnels": cfg.verify_funnels,
                    "launch": "graph replay" if cfg.launch_mode != 2 else "direct launches",
                    "tuning": ("autotuner record " + os.path.relpath(args.tuning or autotune.DEFAULT_RECORD, ROOT))
                    if tuned else "defaults"},

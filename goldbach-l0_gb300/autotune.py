@@ -1,7 +1,8 @@
 """Autotuner of the batched form (the knobs the reference fixes by hand in
 include/config.hpp: SMEM tile size, the tile / large-prime split, the
 hit-list split through the prime-multiplier table's budget, segments per
-batch, and the verify plan's funnel count).
+batch, the verify plan's funnel count and how many of them every word takes
+before the unresolved words are gathered).
 
 Coordinate descent on calibration batches of the workload: from the
 defaults, each knob in turn takes the value with the highest throughput
@@ -34,9 +35,11 @@ KNOBS = {
     "mtab_max_gb": [48, 96, 160],
     "tile_log2": [19, 20],
     "max_batch": [32, 48, 64, 96, 128],
-    "plan_funnels": [4, 6, 8, 12, 16],
+    "plan_funnels": [6, 8, 12, 16],
+    "verify_funnels": [2, 3, 4],
 }
-DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 8}
+DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 8,
+            "verify_funnels": 3}
 DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")
 
 

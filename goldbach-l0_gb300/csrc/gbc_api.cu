@@ -355,6 +355,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.ridge_min) cfg.ridge_min = GBC_TAIL_T;
     if (!cfg.launch_mode) cfg.launch_mode = 1;
     if (cfg.plan_funnels > gbk::kVerifyMaxFun) cfg.plan_funnels = gbk::kVerifyMaxFun;
+    if (!cfg.verify_funnels) cfg.verify_funnels = 3;
+    if (cfg.verify_funnels > cfg.plan_funnels) cfg.verify_funnels = cfg.plan_funnels;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
     else if (cfg.segment_even < 1000 || cfg.segment_even > (1ull << 33))
@@ -544,6 +546,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->vt.fun = ctx->d_fun;
     ctx->vt.rest = ctx->d_rest;
     ctx->vt.ridge_min = cfg.ridge_min;
+    ctx->vt.f1 = cfg.verify_funnels;
     ctx->slot.resize(cfg.nslots);
     for (auto &s : ctx->slot)
         if (int r = slot_alloc(ctx, s)) return r;

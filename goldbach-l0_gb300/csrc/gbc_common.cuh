@@ -219,6 +219,7 @@ struct VerifyTables {
     uint32_t fun_off[GBC_NCLASS], fun_cnt[GBC_NCLASS];
     uint32_t rest_off[GBC_NCLASS], rest_cnt[GBC_NCLASS];
     uint32_t ridge_min;     // evens with p(n) >= ridge_min are listed with their p(n)
+    uint32_t f1;            // funnels every word takes before the unresolved ones are gathered (>= 1)
 };
 
 // device error flags

@@ -304,7 +304,11 @@ __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
     }
 }
 
-constexpr uint32_t kVWin = 76;  // staged words per class array and buffer: 64 + funnel span (<= 5) + 4 + alignment (<= 3)
+constexpr int kVerifyThreads = 128;
+constexpr uint32_t kVerifyWarps = kVerifyThreads / 32;
+constexpr uint32_t kVW = 4;                // words per lane in a chunk
+constexpr uint32_t kVChunk = 32 * kVW;     // words per warp chunk
+constexpr uint32_t kVWin = kVChunk + 12;   // staged words per class array and buffer: chunk + funnel span (<= 5) + 3 + alignment (<= 3), a multiple of 4
 constexpr uint32_t kMaxFun = kVerifyMaxFun;
 
 // one chunk's eight class-array windows into a staging buffer: 8 bulk
@@ -317,6 +321,39 @@ __device__ __forceinline__ void stage_chunk(uint32_t *dst, uint64_t *bar, const 
     for (uint32_t k = 0; k < 8; ++k) bulk_copy_g2s(dst + k * kVWin, src + size_t(k) * wpc, bytes, bar);
 }
 
+// position of the k-th set bit (from 0) of m; m has more than k set bits
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k)
+{
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t s = 16; s > 0; s >>= 1) {
+        const uint32_t lo = __popc(m & ((1u << s) - 1u));
+        if (k >= lo) {
+            k -= lo;
+            m >>= s;
+            pos += s;
+        }
+    }
+    return pos;
+}
+
+// The OR over one funnel's members of the 32 candidates' bits of word
+// window w (three staged words from w): the top member's 64-bit window at
+// bit sh, every other member's the same shifted down by its distance, four
+// shifts per uint4 (a funnel shift uses the low 5 bits of its operand).
+__device__ __forceinline__ uint32_t funnel_hits(const uint32_t *w, uint32_t sh, const uint4 *fsh, uint32_t ng)
+{
+    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2];
+    const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
+    uint32_t wa = al;
+    for (uint32_t g = 0; g < ng; ++g) {
+        const uint4 q = fsh[g];
+        wa |= __funnelshift_r(al, ah, q.x) | __funnelshift_r(al, ah, q.y) | __funnelshift_r(al, ah, q.z) |
+              __funnelshift_r(al, ah, q.w);
+    }
+    return wa;
+}
+
 // Phase A (the reference's check30_a, kernels/goldbach.cl:2029-2189): any
 // witness. Each funnel is a set of plan members p + 30 d (d < 32) of one
 // residue class, all prime, whose windows are the same staged words shifted
@@ -325,19 +362,26 @@ __device__ __forceinline__ void stage_chunk(uint32_t *dst, uint64_t *bar, const 
 // left without a plan witness go to a pending list of (class, word, bits)
 // for k_tail.
 //
-// Staging: each warp double-buffers its 64-word chunks in shared memory;
+// Staging: each warp double-buffers its 128-word chunks in shared memory;
 // one lane moves the next chunk's eight class-array windows with bulk
 // copies (cp.async.bulk on an mbarrier) while the warp tests the current
 // one. The windows start 16-byte aligned (the class arrays are, and chunks
-// are 64 words apart), o = 0..3 words below the lowest word a funnel reads.
-__global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
+// are 128 words apart), o = 0..3 words below the lowest word a funnel reads.
+//
+// Work balance: every lane holds four words (words l, l + 32, l + 64, l + 96
+// of the chunk) through the plan's first f1 funnels, which leave about one
+// word in ten with an even still unresolved; the warp then gathers those
+// words, one per lane (in rounds of 32), for the plan's other funnels, so
+// the last funnels cost one word per lane instead of four and no lane waits
+// for the slowest even of 4096.
+__global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
 {
     __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member groups << 21
     // per funnel and group of four other members: their window offsets
     // above the top member's, padded with 0 (the top member again)
     __shared__ uint4 s_fsh[kMaxFun][8];
-    __shared__ __align__(16) uint32_t s_win[kCheckWarps][2][8 * kVWin];
-    __shared__ __align__(8) uint64_t s_bar[kCheckWarps][2];
+    __shared__ __align__(16) uint32_t s_win[kVerifyWarps][2][8 * kVWin];
+    __shared__ __align__(8) uint64_t s_bar[kVerifyWarps][2];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
 
@@ -371,6 +415,7 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
         const uint64_t ecount = (sp.seg_end - n0) / 30 + 1;
         const uint32_t nwords = uint32_t((ecount + 31) / 32);
         const uint32_t nfun = vt.fun_cnt[cr] < kMaxFun ? vt.fun_cnt[cr] : kMaxFun;
+        const uint32_t f1 = vt.f1 < nfun ? vt.f1 : nfun;
         gbc_segment_result *res = sp.res;
         uint2 *pend_list = sp.pend;
         const uint32_t pend_cap = sp.pend_cap;
@@ -394,7 +439,7 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
         const uint32_t dlo = s_dmin & ~31u, o = (dlo >> 5) & 3u;
         // words each class copy moves: the chunk, the funnels' span and the
         // three words a 96-bit read needs, from the aligned start
-        const uint32_t cwords = nfun ? ((s_dmax - dlo) / 32 + 68 + o + 3) & ~3u : 0u;
+        const uint32_t cwords = nfun ? ((s_dmax - dlo) / 32 + kVChunk + 4 + o + 3) & ~3u : 0u;
         if (cwords > kVWin) {  // funnel span beyond the staging buffer: nothing tested
             if (tid == 0) atomicOr(&res->err, kErrStaging);
             __syncthreads();
@@ -422,21 +467,22 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
         __syncthreads();
 
         uint32_t pend = 0;
+        const uint32_t step = gx * kVerifyWarps;
         if (nfun) {
-            const uint32_t step = gx * kCheckWarps, bytes = cwords * 4;
+            const uint32_t bytes = cwords * 4;
             const uint32_t *src0 = map + ((dlo >> 5) - o);
-            uint32_t ch = bx * kCheckWarps + warp, buf = 0;
-            if (ch * 64 < nwords && lane == 0) {
+            uint32_t ch = bx * kVerifyWarps + warp, buf = 0;
+            if (ch * kVChunk < nwords && lane == 0) {
                 fence_proxy_async();
-                stage_chunk(s_win[warp][0], bar, src0 + size_t(ch) * 64, wpc, bytes);
+                stage_chunk(s_win[warp][0], bar, src0 + size_t(ch) * kVChunk, wpc, bytes);
             }
-            for (; ch * 64 < nwords; ch += step, buf ^= 1u) {
+            for (; ch * kVChunk < nwords; ch += step, buf ^= 1u) {
                 const uint32_t nx = ch + step;
-                if (nx * 64 < nwords) {
+                if (nx * kVChunk < nwords) {
                     __syncwarp();  // every lane is done with the other buffer (the chunk before)
                     if (lane == 0) {
                         fence_proxy_async();
-                        stage_chunk(s_win[warp][buf ^ 1u], bar + (buf ^ 1u), src0 + size_t(nx) * 64, wpc, bytes);
+                        stage_chunk(s_win[warp][buf ^ 1u], bar + (buf ^ 1u), src0 + size_t(nx) * kVChunk, wpc, bytes);
                     }
                 }
                 if (!mbar_wait(bar + buf, (phase >> buf) & 1u)) {
@@ -444,61 +490,77 @@ __global__ void __launch_bounds__(kCheckThreads, 5) k_verify(BatchDesc d, Verify
                     mbar_wait(bar + buf, (phase >> buf) & 1u);
                 }
                 phase ^= 1u << buf;
-                const uint32_t J = ch * 64;
-                const uint32_t jA = J + lane, jB = J + 32 + lane;
-                uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
-                const uint32_t *wl = s_win[warp][buf] + lane;
-                for (uint32_t f = 0; f < nfun; ++f) {
-                    if (!__any_sync(~0u, uA | uB)) break;
+                const uint32_t J = ch * kVChunk;
+                const uint32_t *win = s_win[warp][buf];
+                uint32_t u[kVW];
+#pragma unroll
+                for (uint32_t w = 0; w < kVW; ++w) u[w] = word_mask(J + lane + 32 * w, ecount);
+                // the first f1 funnels on all four words of every lane
+                for (uint32_t f = 0; f < f1; ++f) {
+                    if (!__any_sync(~0u, u[0] | u[1] | u[2] | u[3])) break;
                     const uint32_t e = s_fent[f];
-                    const uint32_t *w = wl + (e & 0xFFFF);
+                    const uint32_t *wl = win + lane + (e & 0xFFFF);
                     const uint32_t sh = (e >> 16) & 31, ng = e >> 21;
-                    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], y0 = w[32], y1 = w[33], y2 = w[34];
-                    // the top member's 64-bit window; every other member's
-                    // is the same shifted down by 1..31 bits
-                    const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
-                    const uint32_t bl = __funnelshift_r(y0, y1, sh), bh = __funnelshift_r(y1, y2, sh);
-                    uint32_t wa = al, wb = bl;
+                    uint32_t al[kVW], ah[kVW], wa[kVW];
+#pragma unroll
+                    for (uint32_t w = 0; w < kVW; ++w) {
+                        const uint32_t x0 = wl[32 * w], x1 = wl[32 * w + 1], x2 = wl[32 * w + 2];
+                        al[w] = __funnelshift_r(x0, x1, sh);
+                        ah[w] = __funnelshift_r(x1, x2, sh);
+                        wa[w] = al[w];
+                    }
                     for (uint32_t g = 0; g < ng; ++g) {
                         const uint4 q = s_fsh[f][g];
-                        wa |= __funnelshift_r(al, ah, q.x) | __funnelshift_r(al, ah, q.y) |
-                              __funnelshift_r(al, ah, q.z) | __funnelshift_r(al, ah, q.w);
-                        wb |= __funnelshift_r(bl, bh, q.x) | __funnelshift_r(bl, bh, q.y) |
-                              __funnelshift_r(bl, bh, q.z) | __funnelshift_r(bl, bh, q.w);
-                    }
-                    uA &= ~wa;
-                    uB &= ~wb;
-                }
-                // pending words: one reservation per warp
-                const uint32_t has = (uA ? 1u : 0u) + (uB ? 1u : 0u);
-                uint32_t pre = has;
 #pragma unroll
-                for (int o2 = 1; o2 < 32; o2 <<= 1) {
-                    const uint32_t n = __shfl_up_sync(~0u, pre, o2);
-                    if (lane >= uint32_t(o2)) pre += n;
-                }
-                const uint32_t tot = __shfl_sync(~0u, pre, 31);
-                if (tot) {
-                    uint32_t at0 = 0;
-                    if (lane == 31) at0 = atomicAdd(&res->npend, tot);
-                    at0 = __shfl_sync(~0u, at0, 31);
-                    uint32_t at = at0 + pre - has;
-                    if (uA) {
-                        if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jA, uA);
-                        else atomicOr(&res->err, kErrPendOverflow);
-                        ++at;
+                        for (uint32_t w = 0; w < kVW; ++w)
+                            wa[w] |= __funnelshift_r(al[w], ah[w], q.x) | __funnelshift_r(al[w], ah[w], q.y) |
+                                     __funnelshift_r(al[w], ah[w], q.z) | __funnelshift_r(al[w], ah[w], q.w);
                     }
-                    if (uB) {
-                        if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | jB, uB);
+#pragma unroll
+                    for (uint32_t w = 0; w < kVW; ++w) u[w] &= ~wa[w];
+                }
+                // the words still unresolved, gathered one per lane (word
+                // order: w-major, then lane) for the other funnels
+                uint32_t bal[kVW], c1 = 0, c2 = 0, c3 = 0, nun = 0;
+#pragma unroll
+                for (uint32_t w = 0; w < kVW; ++w) {
+                    bal[w] = __ballot_sync(~0u, u[w] != 0u);
+                    nun += __popc(bal[w]);
+                    if (w == 0) c1 = nun;
+                    if (w == 1) c2 = nun;
+                    if (w == 2) c3 = nun;
+                }
+                for (uint32_t r0 = 0; r0 < nun; r0 += 32) {
+                    const uint32_t t = r0 + lane;
+                    const uint32_t wt = t < c1 ? 0u : t < c2 ? 1u : t < c3 ? 2u : 3u;
+                    const uint32_t before = wt == 0 ? 0u : wt == 1 ? c1 : wt == 2 ? c2 : c3;
+                    const uint32_t bm = wt == 0 ? bal[0] : wt == 1 ? bal[1] : wt == 2 ? bal[2] : bal[3];
+                    const uint32_t srcl = t < nun ? nth_set_bit(bm, t - before) : 0u;
+                    uint32_t uu = 0;
+#pragma unroll
+                    for (uint32_t w = 0; w < kVW; ++w) {
+                        const uint32_t v = __shfl_sync(~0u, u[w], srcl);
+                        if (w == wt) uu = v;
+                    }
+                    if (t >= nun) uu = 0;
+                    const uint32_t jl = srcl + 32 * wt;  // the word within the chunk
+                    for (uint32_t f = f1; f < nfun; ++f) {
+                        if (!__any_sync(~0u, uu)) break;
+                        const uint32_t e = s_fent[f];
+                        uu &= ~funnel_hits(win + jl + (e & 0xFFFF), (e >> 16) & 31, s_fsh[f], e >> 21);
+                    }
+                    if (uu) {  // every funnel tried: pending (rare)
+                        const uint32_t at = atomicAdd(&res->npend, 1u);
+                        if (at < pend_cap) pend_list[at] = make_uint2((cr << 27) | (J + jl), uu);
                         else atomicOr(&res->err, kErrPendOverflow);
+                        pend += __popc(uu);
                     }
                 }
-                pend += __popc(uA) + __popc(uB);
             }
         } else {
             // no funnels for the class: every word of the warp's chunks is pending
-            for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps)
-                for (uint32_t jj = ch * 64 + lane; jj < ch * 64 + 64; jj += 32) {
+            for (uint32_t ch = bx * kVerifyWarps + warp; ch * kVChunk < nwords; ch += step)
+                for (uint32_t jj = ch * kVChunk + lane; jj < ch * kVChunk + kVChunk; jj += 32) {
                     const uint32_t uw = word_mask(jj, ecount);
                     if (!uw) continue;
                     const uint32_t at = atomicAdd(&res->npend, 1u);
@@ -647,7 +709,7 @@ void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Gri
 
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st)
 {
-    gbk::k_verify<<<g.sm * g.verify, gbk::kCheckThreads, 0, st>>>(d, vt);
+    gbk::k_verify<<<g.sm * g.verify, gbk::kVerifyThreads, 0, st>>>(d, vt);
     gbk::k_tail<<<g.sm * 2, gbk::kTailThreads, 0, st>>>(d, vt);
 }
 
@@ -662,7 +724,7 @@ void query_check_grids(Grids &g)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_check, gbk::kCheckThreads, 0);
     g.check = n > 0 ? n : 1;
     n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_verify, gbk::kCheckThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_verify, gbk::kVerifyThreads, 0);
     g.verify = n > 0 ? n : 1;
 }
 

@@ -86,7 +86,10 @@ typedef struct gbc_config {
     uint32_t selfcheck_every;/* every selfcheck_every-th batch that uses hit lists rebuilds its maps
                                 without them and compares every word (src/verifier.cpp:2057-2112);
                                 a mismatch fails the batch closed. 0: never (default) */
-    uint32_t reserved[4];
+    uint32_t verify_funnels; /* funnels of the plan every word of a chunk takes before the verify
+                                kernel gathers the words still without a witness, one per lane, for
+                                the plan's other funnels (default 3; at most plan_funnels) */
+    uint32_t reserved[3];
 } gbc_config;
 
 #define GBC_MAX_SLOTS 8
