@@ -6,7 +6,9 @@ before the unresolved words are gathered).
 
 Coordinate descent on calibration batches of the workload: from the
 defaults, each knob in turn takes the value with the highest throughput
-while the others stay fixed, for two rounds. Every trial verifies the same
+while the others stay fixed, until a round changes nothing (at most three);
+p_mid and the table budget move together, since the budget decides whether
+the hit lists can start at p_mid. Every trial verifies the same
 consecutive production segments (192 of them, whole batches for every
 batch size tried), timed on the device with the pipeline's own CUDA events, one
 slot, after a warm-up batch that builds the tables. The record holds every
@@ -31,8 +33,9 @@ import gbc  # noqa: E402
 
 SEG = 467_500_000
 KNOBS = {
-    "p_mid": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
-    "mtab_max_gb": [48, 96, 160],
+    # the tile / hit-list split and the table budget that sets where the hit
+    # lists start: one joint knob (a small budget pushes p_hl above p_mid)
+    ("p_mid", "mtab_max_gb"): [(p, g) for p in (1 << 20, 1 << 21, 1 << 22, 1 << 23) for g in (48, 96, 160)],
     "tile_log2": [19, 20],
     "max_batch": [32, 48, 64, 96, 128],
     "plan_funnels": [6, 8, 12, 16],
@@ -44,10 +47,12 @@ DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")
 
 
 def measure(knobs, start, nseg=192, sample_every=256):
-    """Device throughput (G evens/s) of nseg production segments from start
-    under the given knobs; segment i gets p(n) of every even when i is a
-    multiple of sample_every, else the funnel verify + exact tail."""
+    """Device throughput (G evens/s) of about nseg production segments from
+    start (whole batches, at least one) under the given knobs; segment i
+    gets p(n) of every even when i is a multiple of sample_every, else the
+    funnel verify + exact tail."""
     mb = knobs["max_batch"]
+    nseg = mb * max(1, round(nseg / mb))
     segs = [(start + i * SEG, start + i * SEG + SEG - 2) for i in range(nseg + mb)]
     limit = segs[-1][1]
     flags = [0 if i % sample_every == 0 else gbc.SEG_VERIFY for i in range(len(segs))]
@@ -70,7 +75,7 @@ def gpu_name():
         return "unknown"
 
 
-def tune(start, rounds=2, nseg=192, log=print):
+def tune(start, rounds=3, nseg=192, log=print):
     best = dict(DEFAULTS)
     trials = []
     cache = {}
@@ -90,17 +95,26 @@ def tune(start, rounds=2, nseg=192, log=print):
         return cache[key]
 
     base = run(best)
+    def get(k, name):
+        return tuple(k[n] for n in name) if isinstance(name, tuple) else k[name]
+
+    def put(k, name, v):
+        if isinstance(name, tuple):
+            k.update(zip(name, v))
+        else:
+            k[name] = v
+
     for r in range(rounds):
         changed = False
         for name, values in KNOBS.items():
             scores = {}
             for v in values:
                 k = dict(best)
-                k[name] = v
+                put(k, name, v)
                 scores[v] = run(k)
             pick = max(scores, key=scores.get)
-            if pick != best[name]:
-                best[name] = pick
+            if pick != get(best, name):
+                put(best, name, pick)
                 changed = True
         if not changed:
             break
@@ -108,7 +122,8 @@ def tune(start, rounds=2, nseg=192, log=print):
             "workload": {"start": start, "segment": SEG, "segments": nseg, "sample_every": 256,
                          "what": "consecutive production segments, funnel verify + exact tail, every 256th "
                                  "segment p(n) of every even"},
-            "method": "coordinate descent over the knobs, two rounds, device time of the pipeline's events",
+            "method": "coordinate descent over the knobs ((p_mid, table budget) as one), up to three rounds, "
+                      "device time of the pipeline's events",
             "defaults": DEFAULTS, "default_g_evens_s": base,
             "choice": best, "choice_g_evens_s": cache[tuple(sorted(best.items()))], "trials": trials}
 
@@ -126,7 +141,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--start", type=int, default=4000008233142500000)
     ap.add_argument("--segments", type=int, default=192)
-    ap.add_argument("--rounds", type=int, default=2)
+    ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--out", default=DEFAULT_RECORD)
     a = ap.parse_args()
     rec = tune(a.start, a.rounds, a.segments)

@@ -72,11 +72,12 @@ __device__ __forceinline__ uint32_t unit_of(uint32_t k) { return __byte_perm(0x0
 
 constexpr int kCountThreads = 256;
 constexpr int32_t kNoPos = INT32_MIN;
-constexpr uint32_t kCountCap = 8192;  // prime positions the CTA's list holds per round
+constexpr uint32_t kCountCap = 8192;  // prime positions the CTA's list holds at a time
+constexpr uint32_t kCountRounds = 4;  // rounds of kCountThreads words per item (positions stay below 2^20)
 
 // Persistent: a fixed grid takes the virtual CTAs of every segment of the
-// batch (per segment: one per 256 words of its hashed range) from a work
-// counter.
+// batch (per segment: one per 4 x 256 words of its hashed range, taken in
+// four rounds of 256) from a work counter.
 __global__ void __launch_bounds__(kCountThreads, 5) k_count(BatchDesc d)
 {
     __shared__ uint32_t s_ghist[GBC_GBINS];
@@ -100,134 +101,141 @@ __global__ void __launch_bounds__(kCountThreads, 5) k_count(BatchDesc d)
         const uint32_t vbx = vb - __ldg(d.cnt_pref + si);
         for (uint32_t i = tid; i < GBC_GBINS; i += blockDim.x) s_ghist[i] = 0;
         if (tid < 12) s_cnt[tid] = 0;
-        const uint32_t wc0 = cr.w_lo + vbx * blockDim.x;  // first word of the CTA
-        const uint64_t q0 = bp.base + 30ull * 32ull * wc0;         // q of relative position 0
+        const uint32_t wi0 = cr.w_lo + vbx * kCountThreads * kCountRounds;  // first word of the item
+        const uint64_t q0 = bp.base + 30ull * 32ull * wi0;                   // q of relative position 0
         if (tid == 0) {
             s_key = 0;
             s_first = INT32_MAX;
             s_last = kNoPos;
             s_hash = 0;
-            // last hashed prime before the CTA's first word (negative position)
+            // last hashed prime before the item's first word (negative position)
             int32_t pv = kNoPos;
-            for (int64_t ww = int64_t(wc0) - 1; ww >= int64_t(cr.w_lo) && pv == kNoPos; --ww) {
+            for (int64_t ww = int64_t(wi0) - 1; ww >= int64_t(cr.w_lo) && pv == kNoPos; --ww) {
                 for (uint32_t k = 0; k < 8; ++k) {
                     const uint32_t v = bp.map[size_t(k) * bp.wpc + ww] &
                                        range_mask(uint32_t(ww), cr.hash_t[k][0], cr.hash_t[k][1]);
                     if (v) {
                         const int32_t pos =
-                            int32_t(30 * (32 * (ww - int64_t(wc0)) + 31 - __clz(v))) + int32_t(unit_of(k));
+                            int32_t(30 * (32 * (ww - int64_t(wi0)) + 31 - __clz(v))) + int32_t(unit_of(k));
                         if (pos > pv) pv = pos;
                     }
                 }
             }
             s_prev0 = pv;
         }
-        // the counted range as positions relative to q0 (the CTA's positions
-        // stay within +-2^20, so clamping at +-2^30 changes nothing)
+        // the counted range as positions relative to q0 (the item's positions
+        // stay below 2^20, so clamping at +-2^30 changes nothing)
         const int32_t clo = rel_clamp(sp.cnt_lo, q0), chi = rel_clamp(sp.cnt_hi, q0);
-
-        const uint32_t w = wc0 + tid;
-        const bool valid = w <= cr.w_hi;
-        const bool inner = w >= cr.in_lo && w <= cr.in_hi;
-        uint32_t h[8], c[8], raw[8];
-    #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
-            raw[k] = valid ? bp.map[size_t(k) * bp.wpc + w] : 0u;
-            h[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
-            c[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]);
-        }
-        // twins (11, 13), (17, 19) inside a block; (29, 31) into the next block
-        const uint32_t next0 = valid ? bp.map[w + 1] : 0u;  // class 0, word w + 1
-        const uint32_t up29 = (raw[0] >> 1) | (next0 << 31);
-        const uint32_t tw0 = __popc(raw[2] & raw[3] & (inner ? ~0u : range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1])));
-        const uint32_t tw1 = __popc(raw[4] & raw[5] & (inner ? ~0u : range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1])));
-        const uint32_t tw2 = __popc(raw[7] & up29 & (inner ? ~0u : range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1])));
-
-        // one byte per block, natural order: word i of T holds blocks 4 i .. 4 i + 3
-        uint32_t T[8];
-    #pragma unroll
-        for (uint32_t g = 0; g < 4; ++g) {
-            const uint32_t sel = g | ((g + 4) << 4);
-            const uint32_t lo = __byte_perm(__byte_perm(h[0], h[1], sel), __byte_perm(h[2], h[3], sel), 0x5410);
-            const uint32_t hi = __byte_perm(__byte_perm(h[4], h[5], sel), __byte_perm(h[6], h[7], sel), 0x5410);
-            const uint64_t t = transpose8((uint64_t(hi) << 32) | lo);
-            T[2 * g] = uint32_t(t);
-            T[2 * g + 1] = uint32_t(t >> 32);
-        }
-        const int32_t cbase = int32_t(960 * tid);  // position of this thread's first block
-        uint32_t nh = 0;
-    #pragma unroll
-        for (int i = 0; i < 8; ++i) nh += __popc(T[i]);
-        // exclusive sum-scan of the prime counts over the CTA: this thread's
-        // primes are entries [off, off + nh) of the CTA's list in natural order
-        uint32_t v = nh;
-    #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(~0u, v, o);
-            if (lane >= uint32_t(o)) v += n;
-        }
-        if (lane == 31) s_wsum[warp] = v;
-        __syncthreads();
-        uint32_t off = v - nh, total = 0;
-        for (uint32_t i = 0; i < kCountThreads / 32; ++i) {
-            const uint32_t sw = s_wsum[i];
-            if (i < warp) off += sw;
-            total += sw;
-        }
-
-        // the primes in natural order, kCountCap at a time: each thread
-        // writes its own into the list (phase 1), then the CTA takes the list
-        // in stride (phase 2: the hash of all, the gaps of the counted ones),
-        // so the per-prime work has no divergence between lanes
         const bool hash = !(sp.flags & GBC_SEG_NOHASH);
         uint64_t hsum = 0;
-        uint32_t key = 0, err = 0;
+        uint32_t key = 0, err = 0, nh_all = 0, tw[3] = {0u, 0u, 0u}, cc[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
         int32_t cfirst = INT32_MAX, clast = kNoPos;
-        int32_t carry = s_prev0;  // the prime before the round's first entry
-        for (uint32_t lo = 0; lo < total; lo += kCountCap) {
-            const uint32_t n = total - lo < kCountCap ? total - lo : kCountCap;
-            if (off < lo + n && off + nh > lo) {
-                uint32_t idx = off - lo;  // wraps below the round: skipped by idx < n
+        int32_t carry = kNoPos;  // the prime before the current list's first entry
+
+        for (uint32_t rd = 0; rd < kCountRounds; ++rd) {
+            const uint32_t wr0 = wi0 + rd * kCountThreads;  // first word of the round
+            if (wr0 > cr.w_hi) break;
+            const uint32_t w = wr0 + tid;
+            const bool valid = w <= cr.w_hi;
+            const bool inner = w >= cr.in_lo && w <= cr.in_hi;
+            uint32_t h[8], raw[8];
     #pragma unroll
-                for (uint32_t i = 0; i < 8; ++i) {
-                    uint32_t x = T[i];
-                    while (x) {
-                        const uint32_t b = __ffs(x) - 1u;
-                        x &= x - 1u;
-                        if (idx < n) s_pos[idx] = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
-                        ++idx;
-                    }
-                }
+            for (uint32_t k = 0; k < 8; ++k) {
+                raw[k] = valid ? bp.map[size_t(k) * bp.wpc + w] : 0u;
+                h[k] = inner ? raw[k] : raw[k] & range_mask(w, cr.hash_t[k][0], cr.hash_t[k][1]);
+                cc[k] += __popc(inner ? raw[k] : raw[k] & range_mask(w, cr.cnt_t[k][0], cr.cnt_t[k][1]));
             }
+            // twins (11, 13), (17, 19) inside a block; (29, 31) into the next block
+            const uint32_t next0 = valid ? bp.map[w + 1] : 0u;  // class 0, word w + 1
+            const uint32_t up29 = (raw[0] >> 1) | (next0 << 31);
+            tw[0] += __popc(raw[2] & raw[3] & (inner ? ~0u : range_mask(w, cr.twin_t[2][0], cr.twin_t[2][1])));
+            tw[1] += __popc(raw[4] & raw[5] & (inner ? ~0u : range_mask(w, cr.twin_t[4][0], cr.twin_t[4][1])));
+            tw[2] += __popc(raw[7] & up29 & (inner ? ~0u : range_mask(w, cr.twin_t[7][0], cr.twin_t[7][1])));
+
+            // one byte per block, natural order: word i of T holds blocks 4 i .. 4 i + 3
+            uint32_t T[8];
+    #pragma unroll
+            for (uint32_t g = 0; g < 4; ++g) {
+                const uint32_t sel = g | ((g + 4) << 4);
+                const uint32_t lo = __byte_perm(__byte_perm(h[0], h[1], sel), __byte_perm(h[2], h[3], sel), 0x5410);
+                const uint32_t hi = __byte_perm(__byte_perm(h[4], h[5], sel), __byte_perm(h[6], h[7], sel), 0x5410);
+                const uint64_t t = transpose8((uint64_t(hi) << 32) | lo);
+                T[2 * g] = uint32_t(t);
+                T[2 * g + 1] = uint32_t(t >> 32);
+            }
+            const int32_t cbase = int32_t(960 * (rd * kCountThreads + tid));  // this thread's first block
+            uint32_t nh = 0;
+    #pragma unroll
+            for (int i = 0; i < 8; ++i) nh += __popc(T[i]);
+            nh_all += nh;
+            // exclusive sum-scan of the prime counts over the CTA: this thread's
+            // primes are entries [off, off + nh) of the round's list in natural order
+            uint32_t v = nh;
+    #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t n = __shfl_up_sync(~0u, v, o);
+                if (lane >= uint32_t(o)) v += n;
+            }
+            if (lane == 31) s_wsum[warp] = v;
             __syncthreads();
-            for (uint32_t k = tid; k < n; k += kCountThreads) {
-                const int32_t pos = s_pos[k];
-                const int32_t prev = k ? s_pos[k - 1] : carry;
-                if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
-                if (pos >= clo && pos <= chi) {
-                    if (pos < cfirst) cfirst = pos;
-                    if (pos > clast) clast = pos;
-                    if (prev != kNoPos) {
-                        const uint32_t g = uint32_t(pos - prev);
-                        if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
-                        else atomicAdd(&s_ghist[g / 2], 1u);
-                        // largest gap, the smallest lower prime on ties: g << 21 | ~(lower + 2^20)
-                        const uint32_t k2 = (g << 21) | (0x1FFFFFu - uint32_t(prev + (1 << 20)));
-                        if (k2 > key) key = k2;
-                        if (g >= GBC_GTAIL) {
-                            const uint32_t slot = atomicAdd(&sp.res->ntail, 1u);
-                            if (slot < GBC_TAIL_CAP) {
-                                sp.res->tail_g[slot] = g;
-                                sp.res->tail_lo[slot] = q0 + uint64_t(int64_t(prev));
-                            } else err |= kErrTailOverflow;
+            if (rd == 0) carry = s_prev0;
+            uint32_t off = v - nh, ntot = 0;
+            for (uint32_t i = 0; i < kCountThreads / 32; ++i) {
+                const uint32_t sw = s_wsum[i];
+                if (i < warp) off += sw;
+                ntot += sw;
+            }
+
+            // the primes in natural order, kCountCap at a time: each thread
+            // writes its own into the list (phase 1), then the CTA takes the
+            // list in stride (phase 2: the hash of all, the gaps of the
+            // counted ones), so the per-prime work has no divergence between
+            // lanes
+            for (uint32_t lo = 0; lo < ntot; lo += kCountCap) {
+                const uint32_t n = ntot - lo < kCountCap ? ntot - lo : kCountCap;
+                if (off < lo + n && off + nh > lo) {
+                    uint32_t idx = off - lo;  // wraps below the list: skipped by idx < n
+    #pragma unroll
+                    for (uint32_t i = 0; i < 8; ++i) {
+                        uint32_t x = T[i];
+                        while (x) {
+                            const uint32_t b = __ffs(x) - 1u;
+                            x &= x - 1u;
+                            if (idx < n) s_pos[idx] = cbase + int32_t(30 * (4 * i + (b >> 3)) + unit_of(b & 7));
+                            ++idx;
                         }
-                    } else if (q0 + uint64_t(int64_t(pos)) > 7) {
-                        err |= kErrNoPred;
                     }
                 }
+                __syncthreads();
+                for (uint32_t k = tid; k < n; k += kCountThreads) {
+                    const int32_t pos = s_pos[k];
+                    const int32_t prev = k ? s_pos[k - 1] : carry;
+                    if (hash) hsum += splitmix64(q0 + uint64_t(int64_t(pos)));
+                    if (pos >= clo && pos <= chi) {
+                        if (pos < cfirst) cfirst = pos;
+                        if (pos > clast) clast = pos;
+                        if (prev != kNoPos) {
+                            const uint32_t g = uint32_t(pos - prev);
+                            if (g / 2 >= GBC_GBINS) err |= kErrGapRange;
+                            else atomicAdd(&s_ghist[g / 2], 1u);
+                            // largest gap, the smallest lower prime on ties: g << 21 | ~(lower + 2^20)
+                            const uint32_t k2 = (g << 21) | (0x1FFFFFu - uint32_t(prev + (1 << 20)));
+                            if (k2 > key) key = k2;
+                            if (g >= GBC_GTAIL) {
+                                const uint32_t slot = atomicAdd(&sp.res->ntail, 1u);
+                                if (slot < GBC_TAIL_CAP) {
+                                    sp.res->tail_g[slot] = g;
+                                    sp.res->tail_lo[slot] = q0 + uint64_t(int64_t(prev));
+                                } else err |= kErrTailOverflow;
+                            }
+                        } else if (q0 + uint64_t(int64_t(pos)) > 7) {
+                            err |= kErrNoPred;
+                        }
+                    }
+                }
+                carry = s_pos[n - 1];
+                __syncthreads();  // the list is rewritten next
             }
-            carry = s_pos[n - 1];
-            __syncthreads();  // the list is rewritten by the next round
         }
         if (err) atomicOr(&sp.res->err, err);
 
@@ -239,11 +247,11 @@ __global__ void __launch_bounds__(kCountThreads, 5) k_count(BatchDesc d)
         clast = __reduce_max_sync(~0u, clast);
         uint32_t r8[12];
     #pragma unroll
-        for (int k = 0; k < 8; ++k) r8[k] = __reduce_add_sync(~0u, __popc(c[k]));
-        r8[8] = __reduce_add_sync(~0u, tw0);
-        r8[9] = __reduce_add_sync(~0u, tw1);
-        r8[10] = __reduce_add_sync(~0u, tw2);
-        r8[11] = __reduce_add_sync(~0u, nh);
+        for (int k = 0; k < 8; ++k) r8[k] = __reduce_add_sync(~0u, cc[k]);
+        r8[8] = __reduce_add_sync(~0u, tw[0]);
+        r8[9] = __reduce_add_sync(~0u, tw[1]);
+        r8[10] = __reduce_add_sync(~0u, tw[2]);
+        r8[11] = __reduce_add_sync(~0u, nh_all);
         if (lane == 0) {
     #pragma unroll
             for (int k = 0; k < 12; ++k) atomicAdd(&s_cnt[k], r8[k]);
@@ -357,7 +365,8 @@ uint32_t count_ranges(uint64_t base, const gbk::SegParams &sp, gbk::CountRanges 
     cr.in_lo = std::max({a0, b0, c0});
     cr.in_hi = std::min({a1, b1, c1});
     const uint32_t nw = cr.w_hi - cr.w_lo + 1;
-    return (nw + gbk::kCountThreads - 1) / gbk::kCountThreads;
+    constexpr uint32_t kPerItem = gbk::kCountThreads * gbk::kCountRounds;
+    return (nw + kPerItem - 1) / kPerItem;
 }
 
 void launch_count(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
