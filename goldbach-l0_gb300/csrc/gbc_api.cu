@@ -253,6 +253,10 @@ static size_t tb_capacity(double marks_per_bit, uint32_t tile_log2)
 
 constexpr uint32_t kOverflowCap = 1u << 22;  // overflow marks a binned batch may leave
 
+// words past the end of the primes and their reciprocals: the tile kernel
+// reads them four at a time
+constexpr size_t kPrimePad = 4;
+
 static int slot_alloc(gbc_ctx *ctx, Slot &s)
 {
     const auto &cfg = ctx->cfg;
@@ -521,9 +525,9 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     gbh::tile_attributes(cfg.tile_log2, ctx->gi);
     gbh::query_check_grids(ctx->grids);
     gbh::query_count_grids(ctx->grids);
-    CK(dev_alloc(ctx, &ctx->d_primes, std::max<size_t>(pr.size(), 1) * 4));
+    CK(dev_alloc(ctx, &ctx->d_primes, (pr.size() + kPrimePad) * 4));
     CK(cudaMemcpy(ctx->d_primes, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
-    CK(dev_alloc(ctx, &ctx->d_magic, std::max<size_t>(magic.size(), 1) * 4));
+    CK(dev_alloc(ctx, &ctx->d_magic, (magic.size() + kPrimePad) * 4));
     if (!magic.empty()) CK(cudaMemcpy(ctx->d_magic, magic.data(), magic.size() * 4, cudaMemcpyHostToDevice));
     CK(dev_alloc(ctx, &ctx->d_pat, pat.size() * 4));
     CK(cudaMemcpy(ctx->d_pat, pat.data(), pat.size() * 4, cudaMemcpyHostToDevice));

@@ -141,6 +141,9 @@ __device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_
 // Sieves bits [t0, t0 + tl) of class array k of a run in shared memory s
 // (the group patterns already in pat) and stores them. tl is a multiple of
 // 128 bits. Ends with the CTA synchronized, s free for the next tile.
+// kVec4: the context's own prime and reciprocal arrays (16-byte aligned,
+// padded by 4 words), read four at a time; otherwise any arrays.
+template <bool kVec4>
 __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo &gi, const uint32_t *pat,
                                           uint32_t *s, uint32_t k, uint32_t t0, uint32_t tl)
 {
@@ -198,9 +201,30 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
         if (l >= tl) continue;
         for (uint32_t b = l + lane * p; b < tl; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
     }
-    // the rest: a thread per prime, the next prime's three loads issued
-    // before the current prime's marks
-    {
+    if constexpr (kVec4) {
+        // the rest: four consecutive primes per thread and round, their
+        // primes and reciprocals as one 16-byte load each and their first
+        // bits as four loads, all issued before any of their marks (one L2
+        // round trip per four primes)
+        const uint32_t n = bp.n_mid, i_lo = bp.i_warp, c_lo = i_lo & ~3u;
+        for (uint32_t i = c_lo + 4 * tid; i < n; i += 4 * bs) {
+            const uint4 p4 = __ldg(reinterpret_cast<const uint4 *>(bp.primes + i));
+            const uint4 m4 = __ldg(reinterpret_cast<const uint4 *>(bp.magic + i));
+            uint32_t x4[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) x4[u] = i + u < n ? __ldg(xk + i + u) : kNone;
+            const uint32_t pv[4] = {p4.x, p4.y, p4.z, p4.w}, mv[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u) {
+                if (i + u < i_lo) continue;
+                const uint32_t p = pv[u];
+                const uint32_t l = local_start(x4[u], t0, p, mv[u], tl);
+                for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+            }
+        }
+    } else {
+        // the rest: a thread per prime, the next prime's three loads issued
+        // before the current prime's marks
         const uint32_t *pr = bp.primes, *mg = bp.magic;
         const uint32_t n = bp.n_mid;
         uint32_t i = bp.i_warp + tid;
@@ -277,7 +301,7 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uin
         const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
         const uint32_t k = local / tpc, t0 = (local - k * tpc) << tile_log2;
         const uint32_t tl = min(tb, bp.wpc * 32 - t0);
-        tile_body(bp, gi, pat, s, k, t0, tl);
+        tile_body<true>(bp, gi, pat, s, k, t0, tl);
     }
 }
 
@@ -289,7 +313,7 @@ __global__ void __launch_bounds__(1024, 1) k_tile1(BatchParams bp, GroupInfo gi)
     uint32_t *pat = sm + (tb >> 5);
     for (uint32_t i = threadIdx.x; i < gi.words; i += blockDim.x) pat[i] = bp.pat[i];
     __syncthreads();
-    tile_body(bp, gi, pat, sm, blockIdx.y, blockIdx.x << bp.tile_log2, tb);
+    tile_body<false>(bp, gi, pat, sm, blockIdx.y, blockIdx.x << bp.tile_log2, tb);
 }
 
 // Marks class k's multiples p m of the run, m coprime to 30 and to 7..23,
