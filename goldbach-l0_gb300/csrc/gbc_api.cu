@@ -284,7 +284,7 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         const uint64_t nblk = uint64_t(ctx->wpc_cap) * 32;
         uint32_t rlog, nreg;
         hl_regions(nblk, rlog, nreg);
-        const uint32_t ctas = uint32_t(ctx->grids.sm) * gbh::kHitlistCtasPerSm;
+        const uint32_t ctas = uint32_t(ctx->grids.sm) * uint32_t(ctx->grids.hitlist);
         const double marks = 8.0 * double(nblk) *
                              hl_density(double(cfg.limit) + 3, double(ctx->p_hl), double(ctx->primes.back()));
         s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks, ctas, 8 * nreg);
@@ -525,6 +525,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     gbh::tile_attributes(cfg.tile_log2, ctx->gi);
     gbh::query_check_grids(ctx->grids);
     gbh::query_count_grids(ctx->grids);
+    gbh::query_sieve_grids(ctx->grids);
     CK(dev_alloc(ctx, &ctx->d_primes, (pr.size() + kPrimePad) * 4));
     CK(cudaMemcpy(ctx->d_primes, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice));
     CK(dev_alloc(ctx, &ctx->d_magic, (magic.size() + kPrimePad) * 4));
@@ -769,7 +770,7 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
         gbk::BatchParams &bp = img.runs[0];
         uint32_t rlog, nreg;
         hl_regions(bp.nblk, rlog, nreg);
-        const uint32_t ctas = uint32_t(ctx->grids.sm) * gbh::kHitlistCtasPerSm, nbin = 8 * nreg;
+        const uint32_t ctas = uint32_t(ctx->grids.sm) * uint32_t(ctx->grids.hitlist), nbin = 8 * nreg;
         const double marks = 8.0 * double(bp.nblk) *
                              hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
                                         double(ctx->primes[bp.n_all - 1]));

@@ -373,6 +373,7 @@ namespace gbh {
 struct Grids {
     int sm = 1;                  // multiprocessors
     int check = 1, verify = 1, count = 1;  // resident CTAs of those kernels
+    int hitlist = 1;             // resident CTAs of k_hitlist (its grid: one wave)
     int max_seg = 1;             // segments a batch can hold
 };
 void launch_init(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
@@ -385,7 +386,7 @@ void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_hitlist(const gbk::BatchDesc &d, bool direct, const Grids &g, cudaStream_t st);
 void launch_binsort(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_hl_overflow(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
-constexpr int kHitlistCtasPerSm = 8;  // k_hitlist's grid: SMs x this
+void query_sieve_grids(Grids &g);
 void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st);
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st);
 void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st);

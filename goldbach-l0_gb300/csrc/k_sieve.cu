@@ -762,7 +762,16 @@ void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 
 void launch_hitlist(const gbk::BatchDesc &d, bool direct, const Grids &g, cudaStream_t st)
 {
-    gbk::k_hitlist<<<g.sm * kHitlistCtasPerSm, 256, 0, st>>>(d, direct ? 1u : 0u);
+    gbk::k_hitlist<<<g.sm * g.hitlist, 256, 0, st>>>(d, direct ? 1u : 0u);
+}
+
+// the harvest's grid is one wave of resident CTAs: its primes are dealt out
+// by CTA, so a second partial wave would run at a fraction of the occupancy
+void query_sieve_grids(Grids &g)
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_hitlist, 256, 0);
+    g.hitlist = n > 0 ? n : 1;
 }
 
 void launch_binsort(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
