@@ -360,6 +360,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!cfg.launch_mode) cfg.launch_mode = 1;
     if (cfg.plan_funnels > gbk::kVerifyMaxFun) cfg.plan_funnels = gbk::kVerifyMaxFun;
     if (!cfg.verify_funnels) cfg.verify_funnels = 3;
+    if (!cfg.hl_cap_pct || cfg.hl_cap_pct > 100) cfg.hl_cap_pct = 100;
     if (cfg.verify_funnels > cfg.plan_funnels) cfg.verify_funnels = cfg.plan_funnels;
     int rc = GBC_OK;
     if (cfg.limit > GBC_MAX_LIMIT || cfg.limit < 6) rc = fail(ctx, GBC_E_ARG, "limit outside [6, 2^64 - 2^40]");
@@ -545,10 +546,48 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->ct.ridge_min = cfg.ridge_min;
     CK(dev_alloc(ctx, &ctx->d_fun, std::max<size_t>(fun.size(), 1) * sizeof(uint2)));
     if (!fun.empty()) CK(cudaMemcpy(ctx->d_fun, fun.data(), fun.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    // member pairs of each funnel: in shift space (member p0 + 30 d at shift
+    // dm - d below the top member), pairs {a, a + delta} inside the members,
+    // each tested by one shift of the window ORed with itself shifted by
+    // delta; the delta with the fewest shifts (+ 4 for the OR) or none
+    {
+        std::vector<uint2> pairs(std::max<size_t>(fun.size(), 1), make_uint2(0u, 0u));
+        for (size_t f = 0; f < fun.size(); ++f) {
+            const uint32_t y = fun[f].y;
+            const int dm = 31 - __builtin_clz(y);
+            uint32_t S = 0;
+            for (int d = 0; d <= dm; ++d)
+                if (y >> d & 1u) S |= 1u << (dm - d);
+            // costs in half ALU operations: a member 3 (a funnel shift and
+            // half a three-input OR), the OR of the window with its shift 8
+            int best_cost = 3 * __builtin_popcount(S), best_delta = 0;
+            uint32_t best_a = 0;
+            for (int delta = 1; delta < 32; ++delta) {
+                uint32_t used = 0, A = 0;
+                for (int a = 0; a + delta < 32; ++a)
+                    if ((S >> a & 1u) && (S >> (a + delta) & 1u) && !(used >> a & 1u) && !(used >> (a + delta) & 1u)) {
+                        A |= 1u << a;
+                        used |= (1u << a) | (1u << (a + delta));
+                    }
+                const uint32_t R = S & ~used;
+                const int cost = 8 + 3 * (__builtin_popcount(A) + __builtin_popcount(R));
+                const int groups = (__builtin_popcount(A) + 3) / 4 + (__builtin_popcount(R) + 3) / 4;
+                if (A && cost < best_cost && groups <= int(gbk::kVerifyMaxGroups)) {
+                    best_cost = cost;
+                    best_delta = delta;
+                    best_a = A;
+                }
+            }
+            pairs[f] = make_uint2(uint32_t(best_delta), best_a);
+        }
+        CK(dev_alloc(ctx, &ctx->d_fpair, pairs.size() * sizeof(uint2)));
+        CK(cudaMemcpy(ctx->d_fpair, pairs.data(), pairs.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    }
     CK(dev_alloc(ctx, &ctx->d_rest, std::max<size_t>(rest.size(), 1) * 2));
     if (!rest.empty()) CK(cudaMemcpy(ctx->d_rest, rest.data(), rest.size() * 2, cudaMemcpyHostToDevice));
     ctx->vt.cand = ctx->d_cand;
     ctx->vt.fun = ctx->d_fun;
+    ctx->vt.fpair = ctx->d_fpair;
     ctx->vt.rest = ctx->d_rest;
     ctx->vt.ridge_min = cfg.ridge_min;
     ctx->vt.f1 = cfg.verify_funnels;
@@ -565,6 +604,7 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
     if (ctx->outputs && ctx->outputs_del) ctx->outputs_del(ctx->outputs);
     for (auto &s : ctx->slot) slot_free(s);
     cudaFree(ctx->d_fun);
+    cudaFree(ctx->d_fpair);
     cudaFree(ctx->d_rest);
     cudaFree(ctx->mtab);
     cudaFree(ctx->d_primes);
@@ -628,7 +668,7 @@ extern "C" int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out)
     out->device_bytes = ctx->device_bytes;
     out->p_hl = ctx->hl_on ? ctx->p_hl : 0;
     out->sm_count = uint32_t(ctx->grids.sm);
-    out->pad = 0;
+    out->hl_overflow = ctx->hl_overflow;
     return GBC_OK;
 }
 
@@ -774,9 +814,11 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
         const double marks = 8.0 * double(bp.nblk) *
                              hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
                                         double(ctx->primes[bp.n_all - 1]));
-        const uint32_t quota = hl_quota(marks, ctas, nbin);
+        const uint32_t pct = ctx->cfg.hl_cap_pct;
+        const uint32_t quota = uint32_t(std::max<size_t>(32, align_up(size_t(hl_quota(marks, ctas, nbin)) * pct / 100, 32)));
         const uint32_t tl2 = ctx->cfg.tile_log2;
-        const size_t tiles = size_t(8) * bp.tiles_pc, tcap = tb_capacity(marks / (8.0 * double(bp.nblk)), tl2);
+        const size_t tiles = size_t(8) * bp.tiles_pc,
+                     tcap = std::max<size_t>(32, align_up(tb_capacity(marks / (8.0 * double(bp.nblk)), tl2) * pct / 100, 32));
         const bool tb_fit = rlog >= tl2 && (uint64_t(1) << (rlog - tl2)) <= gbk::kSortMaxTiles &&
                             tiles <= s.tb_cnt_words && tiles * tcap <= s.tb_buf_words && tcap < (1ull << 31);
         if (size_t(ctas) * nbin * quota <= s.hl_buf_words && tb_fit) {
@@ -1121,6 +1163,11 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
     uint32_t berr = 0, bad_words = 0;
     CK(cudaMemcpy(&berr, s.err, 4, cudaMemcpyDeviceToHost));
     if (s.did_selfcheck) CK(cudaMemcpy(&bad_words, s.chk_count, 4, cudaMemcpyDeviceToHost));
+    if (ctx->cfg.hl_cap_pct < 100 && gbk::hl_binned(s.img.runs[0], s.img.h->nrun)) {
+        uint32_t ov = 0;
+        CK(cudaMemcpy(&ov, s.ovf_cnt, 4, cudaMemcpyDeviceToHost));
+        ctx->hl_overflow += ov;
+    }
     s.pending = false;
     if (berr) {
         char m[128];

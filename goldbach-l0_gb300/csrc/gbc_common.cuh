@@ -215,6 +215,7 @@ struct CheckTables {
 struct VerifyTables {
     const uint16_t *cand;
     const uint2 *fun;       // funnel: candidate index of its smallest member p, members (bit d: p + 30 d, d < 32)
+    const uint2 *fpair;     // per funnel: delta, pair starts a (bit a: shifts a and a + delta), or 0, 0
     const uint16_t *rest;   // candidates no funnel tests, ascending
     uint32_t fun_off[GBC_NCLASS], fun_cnt[GBC_NCLASS];
     uint32_t rest_off[GBC_NCLASS], rest_cnt[GBC_NCLASS];
@@ -237,6 +238,8 @@ constexpr uint32_t kErrHlOverflow = 1u << 10; // more hit-list overflow marks th
 
 // funnels per class the verify kernel holds (the plan has at most this many)
 constexpr uint32_t kVerifyMaxFun = 32;
+// shift groups (four shifts each) per funnel: pair starts, then single members
+constexpr uint32_t kVerifyMaxGroups = 9;
 
 // tiles per hit-list region k_binsort handles
 constexpr uint32_t kSortMaxTiles = 1024;

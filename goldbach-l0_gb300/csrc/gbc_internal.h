@@ -86,7 +86,7 @@ struct gbc_ctx {
     DescLayout layout;
     uint32_t *d_primes = nullptr, *d_magic = nullptr, *d_pat = nullptr, *d_skip = nullptr;
     uint16_t *d_inv = nullptr, *d_cand = nullptr, *d_list = nullptr;
-    uint2 *d_fun = nullptr;
+    uint2 *d_fun = nullptr, *d_fpair = nullptr;
     uint16_t *d_rest = nullptr;
     gbk::GroupInfo gi{};
     gbk::CheckTables ct{};
@@ -97,6 +97,7 @@ struct gbc_ctx {
     void *outputs = nullptr;
     void (*outputs_del)(void *) = nullptr;
     uint64_t launches = 0, batches = 0, graph_replays = 0, selfchecks = 0, hl_batches = 0;
+    uint32_t hl_overflow = 0;  // overflow-list marks seen by collect (hl_cap_pct < 100 only)
     uint64_t device_bytes = 0;
     // prime-multiplier table (hit lists for the primes >= p_hl)
     bool hl_on = false;

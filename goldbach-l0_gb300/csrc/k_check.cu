@@ -337,20 +337,38 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k)
     return pos;
 }
 
+// Funnel entry in shared memory: staged word offset (10 bits) | shift << 10
+// | pair groups << 15 | single groups << 19 | delta << 23.
+__device__ __forceinline__ uint32_t fent_off(uint32_t e) { return e & 0x3FFu; }
+__device__ __forceinline__ uint32_t fent_sh(uint32_t e) { return (e >> 10) & 31u; }
+__device__ __forceinline__ uint32_t fent_nga(uint32_t e) { return (e >> 15) & 15u; }
+__device__ __forceinline__ uint32_t fent_ngr(uint32_t e) { return (e >> 19) & 15u; }
+__device__ __forceinline__ uint32_t fent_delta(uint32_t e) { return e >> 23; }
+
+// ORs into wa the four shifted windows of one group (a funnel shift uses the
+// low 5 bits of its operand)
+__device__ __forceinline__ uint32_t group_hits(uint32_t lo, uint32_t hi, uint4 q)
+{
+    return __funnelshift_r(lo, hi, q.x) | __funnelshift_r(lo, hi, q.y) | __funnelshift_r(lo, hi, q.z) |
+           __funnelshift_r(lo, hi, q.w);
+}
+
 // The OR over one funnel's members of the 32 candidates' bits of word
 // window w (three staged words from w): the top member's 64-bit window at
-// bit sh, every other member's the same shifted down by its distance, four
-// shifts per uint4 (a funnel shift uses the low 5 bits of its operand).
-__device__ __forceinline__ uint32_t funnel_hits(const uint32_t *w, uint32_t sh, const uint4 *fsh, uint32_t ng)
+// bit sh, every other member's the same shifted down by its distance. A
+// pair of members a, a + delta is one shift of the window ORed with itself
+// shifted by delta (the bits a pair reads stay below 63).
+__device__ __forceinline__ uint32_t funnel_hits(const uint32_t *w, uint32_t e, const uint4 *fsh)
 {
-    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2];
+    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2], sh = fent_sh(e), nga = fent_nga(e), ngr = fent_ngr(e);
     const uint32_t al = __funnelshift_r(x0, x1, sh), ah = __funnelshift_r(x1, x2, sh);
-    uint32_t wa = al;
-    for (uint32_t g = 0; g < ng; ++g) {
-        const uint4 q = fsh[g];
-        wa |= __funnelshift_r(al, ah, q.x) | __funnelshift_r(al, ah, q.y) | __funnelshift_r(al, ah, q.z) |
-              __funnelshift_r(al, ah, q.w);
+    uint32_t wa = 0;
+    if (nga) {
+        const uint32_t dl = fent_delta(e);
+        const uint32_t bl = al | __funnelshift_r(al, ah, dl), bh = ah | (ah >> dl);
+        for (uint32_t g = 0; g < nga; ++g) wa |= group_hits(bl, bh, fsh[g]);
     }
+    for (uint32_t g = 0; g < ngr; ++g) wa |= group_hits(al, ah, fsh[nga + g]);
     return wa;
 }
 
@@ -376,10 +394,10 @@ __device__ __forceinline__ uint32_t funnel_hits(const uint32_t *w, uint32_t sh, 
 // for the slowest even of 4096.
 __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
 {
-    __shared__ uint32_t s_fent[kMaxFun];  // word offset | shift << 16 | member groups << 21
-    // per funnel and group of four other members: their window offsets
-    // above the top member's, padded with 0 (the top member again)
-    __shared__ uint4 s_fsh[kMaxFun][8];
+    __shared__ uint32_t s_fent[kMaxFun];  // see fent_off .. fent_delta
+    // per funnel: groups of four window offsets above the top member's, the
+    // pair starts first, then the single members, each padded with its first
+    __shared__ uint4 s_fsh[kMaxFun][kVerifyMaxGroups];
     __shared__ __align__(16) uint32_t s_win[kVerifyWarps][2][8 * kVWin];
     __shared__ __align__(8) uint64_t s_bar[kVerifyWarps][2];
     __shared__ uint32_t s_dmin, s_dmax;
@@ -450,19 +468,30 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
             const uint32_t p0 = vt.cand[e.x], dm = 31 - __clz(e.y);
             const uint32_t u = (r + 30 - p0 % 30) % 30;
             const uint32_t dd = uint32_t((n0 - base - p0 - u) / 30) - dm - dlo;
-            // member p0 + 30 d's window starts dm - d bits above the top member's
-            uint32_t sm = (__brev(e.y) >> (31 - dm)) & ~1u, ng = 0;
-            while (sm) {
-                uint32_t q[4] = {0u, 0u, 0u, 0u};
+            // member p0 + 30 d's window starts dm - d bits above the top
+            // member's (shift space, bit 0: the top member); the host's
+            // pairs {a, a + delta} take their members out of the singles
+            const uint2 pr = vt.fpair[vt.fun_off[cr] + f];
+            const uint32_t S = __brev(e.y) >> (31 - dm), dl = pr.x, A = pr.y;
+            const uint32_t R = S & ~(A | (dl ? A << dl : 0u));
+            uint32_t ng = 0, nga = 0;
+            for (uint32_t sel = 0; sel < 2; ++sel) {
+                uint32_t sm = sel ? R : A;
+                const uint32_t first = sm ? uint32_t(__ffs(sm) - 1) : 0u;
+                while (sm) {
+                    uint32_t q[4] = {first, first, first, first};
 #pragma unroll
-                for (uint32_t j = 0; j < 4; ++j)
-                    if (sm) {
-                        q[j] = uint32_t(__ffs(sm) - 1);
-                        sm &= sm - 1u;
-                    }
-                s_fsh[f][ng++] = make_uint4(q[0], q[1], q[2], q[3]);
+                    for (uint32_t j = 0; j < 4; ++j)
+                        if (sm) {
+                            q[j] = uint32_t(__ffs(sm) - 1);
+                            sm &= sm - 1u;
+                        }
+                    s_fsh[f][ng++] = make_uint4(q[0], q[1], q[2], q[3]);
+                }
+                if (!sel) nga = ng;
             }
-            s_fent[f] = (class_of(u) * kVWin + o + (dd >> 5)) | ((dd & 31) << 16) | (ng << 21);
+            s_fent[f] = (class_of(u) * kVWin + o + (dd >> 5)) | ((dd & 31) << 10) | (nga << 15) | ((ng - nga) << 19) |
+                        (dl << 23);
         }
         __syncthreads();
 
@@ -499,22 +528,33 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
                 for (uint32_t f = 0; f < f1; ++f) {
                     if (!__any_sync(~0u, u[0] | u[1] | u[2] | u[3])) break;
                     const uint32_t e = s_fent[f];
-                    const uint32_t *wl = win + lane + (e & 0xFFFF);
-                    const uint32_t sh = (e >> 16) & 31, ng = e >> 21;
+                    const uint32_t *wl = win + lane + fent_off(e);
+                    const uint32_t sh = fent_sh(e), nga = fent_nga(e), ngr = fent_ngr(e), dl = fent_delta(e);
                     uint32_t al[kVW], ah[kVW], wa[kVW];
 #pragma unroll
                     for (uint32_t w = 0; w < kVW; ++w) {
                         const uint32_t x0 = wl[32 * w], x1 = wl[32 * w + 1], x2 = wl[32 * w + 2];
                         al[w] = __funnelshift_r(x0, x1, sh);
                         ah[w] = __funnelshift_r(x1, x2, sh);
-                        wa[w] = al[w];
+                        wa[w] = 0;
                     }
-                    for (uint32_t g = 0; g < ng; ++g) {
-                        const uint4 q = s_fsh[f][g];
+                    if (nga) {
+                        uint32_t bl[kVW], bh[kVW];
 #pragma unroll
-                        for (uint32_t w = 0; w < kVW; ++w)
-                            wa[w] |= __funnelshift_r(al[w], ah[w], q.x) | __funnelshift_r(al[w], ah[w], q.y) |
-                                     __funnelshift_r(al[w], ah[w], q.z) | __funnelshift_r(al[w], ah[w], q.w);
+                        for (uint32_t w = 0; w < kVW; ++w) {
+                            bl[w] = al[w] | __funnelshift_r(al[w], ah[w], dl);
+                            bh[w] = ah[w] | (ah[w] >> dl);
+                        }
+                        for (uint32_t g = 0; g < nga; ++g) {
+                            const uint4 q = s_fsh[f][g];
+#pragma unroll
+                            for (uint32_t w = 0; w < kVW; ++w) wa[w] |= group_hits(bl[w], bh[w], q);
+                        }
+                    }
+                    for (uint32_t g = 0; g < ngr; ++g) {
+                        const uint4 q = s_fsh[f][nga + g];
+#pragma unroll
+                        for (uint32_t w = 0; w < kVW; ++w) wa[w] |= group_hits(al[w], ah[w], q);
                     }
 #pragma unroll
                     for (uint32_t w = 0; w < kVW; ++w) u[w] &= ~wa[w];
@@ -547,7 +587,7 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
                     for (uint32_t f = f1; f < nfun; ++f) {
                         if (!__any_sync(~0u, uu)) break;
                         const uint32_t e = s_fent[f];
-                        uu &= ~funnel_hits(win + jl + (e & 0xFFFF), (e >> 16) & 31, s_fsh[f], e >> 21);
+                        uu &= ~funnel_hits(win + jl + fent_off(e), e, s_fsh[f]);
                     }
                     if (uu) {  // every funnel tried: pending (rare)
                         const uint32_t at = atomicAdd(&res->npend, 1u);

@@ -89,7 +89,10 @@ typedef struct gbc_config {
     uint32_t verify_funnels; /* funnels of the plan every word of a chunk takes before the verify
                                 kernel gathers the words still without a witness, one per lane, for
                                 the plan's other funnels (default 3; at most plan_funnels) */
-    uint32_t reserved[3];
+    uint32_t hl_cap_pct;     /* the hit-list bins' quotas and capacities in percent of their sizing
+                                (default 100; lower values make marks take the overflow list, which
+                                is cleared after the tiles: for tests of that path) */
+    uint32_t reserved[2];
 } gbc_config;
 
 #define GBC_MAX_SLOTS 8
@@ -226,7 +229,7 @@ typedef struct gbc_ctx_stats {
     uint64_t device_bytes;
     uint64_t p_hl;            /* first hit-listed prime (0: hit lists off) */
     uint32_t sm_count;        /* multiprocessors of the context's device */
-    uint32_t pad;
+    uint32_t hl_overflow;     /* hit-list marks that took the overflow list (counted when hl_cap_pct < 100) */
 } gbc_ctx_stats;
 int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out);
 

@@ -241,3 +241,35 @@ def test_run_outputs_ridges_live_records(tmp_path):
     assert (j["primes"], j["twins"]) == (res.primes, res.twins)
     assert (j["pmax"], j["pmax_n"]) == (max(pn), a + 2 * pn.index(max(pn)))
     assert j["events"] == [] and (not rec.exists() or rec.read_text() == "")
+
+
+def test_hitlist_overflow_path_bit_exact():
+    """Hit-list bins at 80% of their sizing: marks beyond a region quota or a
+    tile bin's capacity take the overflow list (cleared after the tiles); the
+    maps (self-check against the rebuild without hit lists) and every
+    statistic equal those of the bins at full size."""
+    seg = 467_500_000
+    a = 4000008233142500000
+    segs = [(a, a + seg - 2), (a + seg, a + 2 * seg - 2)]
+    limit = segs[-1][1]
+    flags = [0, gbc.SEG_VERIFY]
+    out = {}
+    for pct in (100, 80):
+        with gbc.Context(limit=limit, segment_even=seg, max_batch=2, p_mid=1 << 21, mtab_max_gb=96, hl_mode=1,
+                         hl_cap_pct=pct, selfcheck_every=1) as c:
+            c.enqueue_batch(0, segs, limit, flags)
+            res, _ = c.collect(0, 2)
+            st = c.stats()
+            assert st.selfchecks >= 1
+            out[pct] = (res, st.hl_overflow)
+    assert out[100][1] == 0 and out[80][1] > 0  # the overflow list was used at 80%
+    for r1, r2 in zip(out[100][0], out[80][0]):
+        for f in ("primes30", "twins", "ghist"):
+            assert list(getattr(r1, f)) == list(getattr(r2, f)), f
+        for f in ("map_hash", "map_primes", "gmax_key", "first_prime", "last_prime", "nleft", "pending", "npend",
+                  "ntail", "nridge"):
+            assert getattr(r1, f) == getattr(r2, f), f
+        assert [list(h) for h in r1.hist] == [list(h) for h in r2.hist]
+        assert list(r1.first) == list(r2.first)
+        assert sorted(zip(r1.tail_g[:r1.ntail], r1.tail_lo[:r1.ntail])) == \
+            sorted(zip(r2.tail_g[:r2.ntail], r2.tail_lo[:r2.ntail]))
