@@ -526,7 +526,10 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
                 for (uint32_t w = 0; w < kVW; ++w) u[w] = word_mask(J + lane + 32 * w, ecount);
                 // the first f1 funnels on all four words of every lane
                 for (uint32_t f = 0; f < f1; ++f) {
-                    if (!__any_sync(~0u, u[0] | u[1] | u[2] | u[3])) break;
+                    uint32_t any = 0;
+#pragma unroll
+                    for (uint32_t w = 0; w < kVW; ++w) any |= u[w];
+                    if (!__any_sync(~0u, any)) break;
                     const uint32_t e = s_fent[f];
                     const uint32_t *wl = win + lane + fent_off(e);
                     const uint32_t sh = fent_sh(e), nga = fent_nga(e), ngr = fent_ngr(e), dl = fent_delta(e);
@@ -561,20 +564,23 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
                 }
                 // the words still unresolved, gathered one per lane (word
                 // order: w-major, then lane) for the other funnels
-                uint32_t bal[kVW], c1 = 0, c2 = 0, c3 = 0, nun = 0;
+                uint32_t bal[kVW], cpre[kVW], nun = 0;  // cpre[w]: unresolved words in w' <= w
 #pragma unroll
                 for (uint32_t w = 0; w < kVW; ++w) {
                     bal[w] = __ballot_sync(~0u, u[w] != 0u);
                     nun += __popc(bal[w]);
-                    if (w == 0) c1 = nun;
-                    if (w == 1) c2 = nun;
-                    if (w == 2) c3 = nun;
+                    cpre[w] = nun;
                 }
                 for (uint32_t r0 = 0; r0 < nun; r0 += 32) {
                     const uint32_t t = r0 + lane;
-                    const uint32_t wt = t < c1 ? 0u : t < c2 ? 1u : t < c3 ? 2u : 3u;
-                    const uint32_t before = wt == 0 ? 0u : wt == 1 ? c1 : wt == 2 ? c2 : c3;
-                    const uint32_t bm = wt == 0 ? bal[0] : wt == 1 ? bal[1] : wt == 2 ? bal[2] : bal[3];
+                    uint32_t wt = 0, before = 0, bm = bal[0];
+#pragma unroll
+                    for (uint32_t w = 0; w + 1 < kVW; ++w)
+                        if (t >= cpre[w]) {
+                            wt = w + 1;
+                            before = cpre[w];
+                            bm = bal[w + 1];
+                        }
                     const uint32_t srcl = t < nun ? nth_set_bit(bm, t - before) : 0u;
                     uint32_t uu = 0;
 #pragma unroll
