@@ -306,10 +306,11 @@ __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
 
 constexpr int kVerifyThreads = 128;
 constexpr uint32_t kVerifyWarps = kVerifyThreads / 32;
-constexpr uint32_t kVW = 4;                // words per lane in a chunk
+constexpr uint32_t kVW = 6;                // words per lane in a chunk
 constexpr uint32_t kVChunk = 32 * kVW;     // words per warp chunk
 constexpr uint32_t kVWin = kVChunk + 12;   // staged words per class array and buffer: chunk + funnel span (<= 5) + 3 + alignment (<= 3), a multiple of 4
 constexpr uint32_t kMaxFun = kVerifyMaxFun;
+constexpr size_t kVerifySmem = size_t(kVerifyWarps) * 2 * 8 * kVWin * 4;  // k_verify's dynamic shared memory
 
 // one chunk's eight class-array windows into a staging buffer: 8 bulk
 // copies of `bytes` each, completing on bar (issued by one lane)
@@ -337,13 +338,18 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k)
     return pos;
 }
 
-// Funnel entry in shared memory: staged word offset (10 bits) | shift << 10
-// | pair groups << 15 | single groups << 19 | delta << 23.
-__device__ __forceinline__ uint32_t fent_off(uint32_t e) { return e & 0x3FFu; }
-__device__ __forceinline__ uint32_t fent_sh(uint32_t e) { return (e >> 10) & 31u; }
-__device__ __forceinline__ uint32_t fent_nga(uint32_t e) { return (e >> 15) & 15u; }
-__device__ __forceinline__ uint32_t fent_ngr(uint32_t e) { return (e >> 19) & 15u; }
-__device__ __forceinline__ uint32_t fent_delta(uint32_t e) { return e >> 23; }
+// Funnel entry in shared memory: staged word offset (12 bits) | shift << 12
+// | pair groups << 17 | single groups << 21 | delta << 25.
+static_assert(7 * kVWin + 7 < 4096, "staged word offsets must fit the funnel entry's 12 bits");
+__device__ __forceinline__ uint32_t fent_make(uint32_t off, uint32_t sh, uint32_t nga, uint32_t ngr, uint32_t delta)
+{
+    return off | (sh << 12) | (nga << 17) | (ngr << 21) | (delta << 25);
+}
+__device__ __forceinline__ uint32_t fent_off(uint32_t e) { return e & 0xFFFu; }
+__device__ __forceinline__ uint32_t fent_sh(uint32_t e) { return (e >> 12) & 31u; }
+__device__ __forceinline__ uint32_t fent_nga(uint32_t e) { return (e >> 17) & 15u; }
+__device__ __forceinline__ uint32_t fent_ngr(uint32_t e) { return (e >> 21) & 15u; }
+__device__ __forceinline__ uint32_t fent_delta(uint32_t e) { return e >> 25; }
 
 // ORs into wa the four shifted windows of one group (a funnel shift uses the
 // low 5 bits of its operand)
@@ -392,13 +398,16 @@ __device__ __forceinline__ uint32_t funnel_hits(const uint32_t *w, uint32_t e, c
 // words, one per lane (in rounds of 32), for the plan's other funnels, so
 // the last funnels cost one word per lane instead of four and no lane waits
 // for the slowest even of 4096.
-__global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, VerifyTables vt)
+__global__ void __launch_bounds__(kVerifyThreads, 3) k_verify(BatchDesc d, VerifyTables vt)
 {
     __shared__ uint32_t s_fent[kMaxFun];  // see fent_off .. fent_delta
     // per funnel: groups of four window offsets above the top member's, the
     // pair starts first, then the single members, each padded with its first
     __shared__ uint4 s_fsh[kMaxFun][kVerifyMaxGroups];
-    __shared__ __align__(16) uint32_t s_win[kVerifyWarps][2][8 * kVWin];
+    // per warp: two staging buffers of eight class-array windows (dynamic
+    // shared memory: kVerifySmem bytes)
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    uint32_t (*s_win)[2][8 * kVWin] = reinterpret_cast<uint32_t (*)[2][8 * kVWin]>(s_dyn);
     __shared__ __align__(8) uint64_t s_bar[kVerifyWarps][2];
     __shared__ uint32_t s_dmin, s_dmax;
     __shared__ unsigned long long s_pend;
@@ -490,8 +499,7 @@ __global__ void __launch_bounds__(kVerifyThreads, 5) k_verify(BatchDesc d, Verif
                 }
                 if (!sel) nga = ng;
             }
-            s_fent[f] = (class_of(u) * kVWin + o + (dd >> 5)) | ((dd & 31) << 10) | (nga << 15) | ((ng - nga) << 19) |
-                        (dl << 23);
+            s_fent[f] = fent_make(class_of(u) * kVWin + o + (dd >> 5), dd & 31, nga, ng - nga, dl);
         }
         __syncthreads();
 
@@ -755,7 +763,7 @@ void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Gri
 
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st)
 {
-    gbk::k_verify<<<g.sm * g.verify, gbk::kVerifyThreads, 0, st>>>(d, vt);
+    gbk::k_verify<<<g.sm * g.verify, gbk::kVerifyThreads, gbk::kVerifySmem, st>>>(d, vt);
     gbk::k_tail<<<g.sm * 2, gbk::kTailThreads, 0, st>>>(d, vt);
 }
 
@@ -770,7 +778,8 @@ void query_check_grids(Grids &g)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_check, gbk::kCheckThreads, 0);
     g.check = n > 0 ? n : 1;
     n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_verify, gbk::kVerifyThreads, 0);
+    cudaFuncSetAttribute(gbk::k_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, int(gbk::kVerifySmem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_verify, gbk::kVerifyThreads, gbk::kVerifySmem);
     g.verify = n > 0 ? n : 1;
 }
 
