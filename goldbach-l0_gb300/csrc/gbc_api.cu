@@ -238,10 +238,15 @@ static void hl_regions(uint64_t nblk, uint32_t &rlog, uint32_t &nreg)
     nreg = uint32_t((nblk + (uint64_t(1) << rlog) - 1) >> rlog);
 }
 
-// Offsets per (harvest CTA, bin): the expected marks + 25%, + 64, whole lines.
-static uint32_t hl_quota(double marks, uint32_t ctas, uint32_t nbin)
+// Offsets per (harvest CTA, bin): the expected marks of a whole region (not
+// the batch's average over bins: its last region is cut short) + 45%, + 64,
+// whole lines. marks_per_bit: marks per class bit. The margin covers the
+// harvest CTAs' uneven shares: CTA c takes primes in blocks of 256, and the
+// first blocks (the smallest primes, with the most marks) weigh most.
+static uint32_t hl_quota(double marks_per_bit, uint64_t nblk, uint32_t rlog, uint32_t ctas)
 {
-    return uint32_t(align_up(size_t(1.25 * marks / (double(ctas) * nbin)) + 64, 32));
+    const double region = double(std::min<uint64_t>(nblk, uint64_t(1) << rlog));
+    return uint32_t(align_up(size_t(1.45 * marks_per_bit * region / double(ctas)) + 64, 32));
 }
 
 // Offsets per tile bin: the expected marks of a tile + 15%, + 2048, whole
@@ -251,7 +256,11 @@ static size_t tb_capacity(double marks_per_bit, uint32_t tile_log2)
     return align_up(size_t(1.15 * marks_per_bit * double(1u << tile_log2)) + 2048, 32);
 }
 
-constexpr uint32_t kOverflowCap = 1u << 22;  // overflow marks a binned batch may leave
+// overflow marks a binned batch may leave: 2% of a full batch's, at least 2^22
+static uint32_t overflow_cap(double marks)
+{
+    return uint32_t(std::min(double(1u << 30), std::max(double(1u << 22), 0.02 * marks)));
+}
 
 // words past the end of the primes and their reciprocals: the tile kernel
 // reads them four at a time
@@ -287,7 +296,7 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         const uint32_t ctas = uint32_t(ctx->grids.sm) * uint32_t(ctx->grids.hitlist);
         const double marks = 8.0 * double(nblk) *
                              hl_density(double(cfg.limit) + 3, double(ctx->p_hl), double(ctx->primes.back()));
-        s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks, ctas, 8 * nreg);
+        s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks / (8.0 * double(nblk)), nblk, rlog, ctas);
         CK(dev_alloc(ctx, &s.hl_buf, std::max<size_t>(s.hl_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.hl_cnt, size_t(ctas) * gbk::kHlMaxBins * 4));
         // tile bins: wpc_cap is a whole number of tiles
@@ -296,7 +305,7 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         s.tb_buf_words = s.tb_cnt_words * tb_capacity(marks / (8.0 * double(nblk)), tl2);
         CK(dev_alloc(ctx, &s.tb_buf, std::max<size_t>(s.tb_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.tb_cnt, std::max<size_t>(s.tb_cnt_words, 1) * 4));
-        s.ovf_cap = kOverflowCap;
+        s.ovf_cap = overflow_cap(marks);
         CK(dev_alloc(ctx, &s.ovf_buf, size_t(s.ovf_cap) * sizeof(uint2)));
         CK(dev_alloc(ctx, &s.ovf_cnt, 4));
     }
@@ -815,7 +824,8 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
                              hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
                                         double(ctx->primes[bp.n_all - 1]));
         const uint32_t pct = ctx->cfg.hl_cap_pct;
-        const uint32_t quota = uint32_t(std::max<size_t>(32, align_up(size_t(hl_quota(marks, ctas, nbin)) * pct / 100, 32)));
+        const uint32_t quota = uint32_t(std::max<size_t>(
+            32, align_up(size_t(hl_quota(marks / (8.0 * double(bp.nblk)), bp.nblk, rlog, ctas)) * pct / 100, 32)));
         const uint32_t tl2 = ctx->cfg.tile_log2;
         const size_t tiles = size_t(8) * bp.tiles_pc,
                      tcap = std::max<size_t>(32, align_up(tb_capacity(marks / (8.0 * double(bp.nblk)), tl2) * pct / 100, 32));
