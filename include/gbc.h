@@ -77,7 +77,9 @@ typedef struct gbc_config {
                                 gets p(n) of every even, the others the funnel verify + exact tail
                                 (GB_STATS_SAMPLE, include/gstats.hpp:62); 0 or 1: every segment
                                 (default) */
-    uint32_t plan_funnels;   /* funnels per class of the verify plan (default 8, at most 32) */
+    uint32_t plan_funnels;   /* funnels per class of the verify plan (default 8, at most 32; below 6
+                                the evens a production segment leaves to the exact continuation can
+                                overflow its pending list, and the batch fails closed) */
     uint32_t ridge_min;      /* evens with p(n) >= ridge_min are listed (default 3000,
                                 include/config.hpp:104 RIDGE_MIN_DEFAULT) */
     uint32_t launch_mode;    /* 0 or 1: a batch is one replay of the slot's CUDA graph of the whole

@@ -273,3 +273,33 @@ def test_hitlist_overflow_path_bit_exact():
         assert list(r1.first) == list(r2.first)
         assert sorted(zip(r1.tail_g[:r1.ntail], r1.tail_lo[:r1.ntail])) == \
             sorted(zip(r2.tail_g[:r2.ntail], r2.tail_lo[:r2.ntail]))
+
+
+@pytest.mark.parametrize("plan,first", [(8, 8), (6, 1), (32, 3), (16, 2)])
+def test_verify_plan_knobs_same_statistics(plan, first):
+    """The verify plan's funnel count and how many funnels every word takes
+    before the unresolved words are gathered change only which evens reach
+    the exact continuation: primes, twins, gaps, the map hash and the p(n) >=
+    3000 tail (counts and first occurrences) stay those of the default plan."""
+    seg = 467_500_000
+    a = 4000008233142500000
+    segs = [(a, a + seg - 2), (a + seg, a + 2 * seg - 2)]
+    limit = segs[-1][1]
+    flags = [gbc.SEG_VERIFY, gbc.SEG_VERIFY]
+    out = []
+    for pf, vf in ((0, 0), (plan, first)):
+        with gbc.Context(limit=limit, segment_even=seg, max_batch=2, p_mid=1 << 21, mtab_max_gb=96, hl_mode=1,
+                         plan_funnels=pf, verify_funnels=vf) as c:
+            c.enqueue_batch(0, segs, limit, flags)
+            res, _ = c.collect(0, 2)
+            out.append(res)
+    cand = gbc.candidates()
+    tail = [i for i, p in enumerate(cand) if p >= 3000]
+    for r1, r2 in zip(*out):
+        for f in ("primes30", "twins", "ghist"):
+            assert list(getattr(r1, f)) == list(getattr(r2, f)), f
+        for f in ("map_hash", "map_primes", "gmax_key", "nleft"):
+            assert getattr(r1, f) == getattr(r2, f), f
+        assert [sum(r1.hist[cr][i] for cr in range(15)) for i in tail] == \
+            [sum(r2.hist[cr][i] for cr in range(15)) for i in tail]
+        assert [r1.first[i] for i in tail] == [r2.first[i] for i in tail]
