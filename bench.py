@@ -540,6 +540,20 @@ def run_gb300(args, rep):
         "check": (["k_verify", "k_tail"], maps),                                 # the maps, read once
         "count": (["k_count"], maps),                                            # the maps, read once
     }
+    # Shared-memory atomics per launch (algorithmic): the tile sieve clears
+    # every multiple of its shared-atomic primes 71 <= p < p_mid in each of
+    # the 8 class arrays (W / 30 bits each) and every hit-list mark; the
+    # harvest counts each mark into its bin and the sort counts and ranks it;
+    # the count kernel adds each prime's gap to the histogram.
+    import numpy as np
+    sieve_to = int(cfg.p_mid)
+    flags_ = np.ones(sieve_to, dtype=bool)
+    flags_[:2] = False
+    for q_ in range(2, int(sieve_to ** 0.5) + 1):
+        if flags_[q_]:
+            flags_[q_ * q_::q_] = False
+    inv_sum = float((1.0 / np.nonzero(flags_[71:])[0].__add__(71)).sum())
+    smem_atomics = {"tile": 8 * W / 30 * inv_sum + marks, "large": 3 * marks, "check": 0.0, "count": W / L}
     counters = ncu_counters()
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = cst.sm_count * 4 * sm_mhz * 1e6                    # warp instructions per second
@@ -548,7 +562,11 @@ def run_gb300(args, rep):
         ms = stage[s_] / args.steps
         row = {"kernel": "+".join(kerns), "ms_per_launch": ms, "alg_bytes_per_launch": b,
                "achieved_gbs": b / (ms / 1e3) / 1e9 if ms > 0 else None,
-               "frac_hbm": b / (ms / 1e3) / 1e9 / hbm if ms > 0 else None}
+               "frac_hbm": b / (ms / 1e3) / 1e9 / hbm if ms > 0 else None,
+               "smem_atomics_per_launch": smem_atomics[s_],
+               "smem_atomic_rate_g_per_s": smem_atomics[s_] / (ms / 1e3) / 1e9 if ms > 0 else None,
+               "smem_atomics_per_clock_per_sm": smem_atomics[s_] / (ms / 1e3) / (cst.sm_count * sm_mhz * 1e6)
+               if ms > 0 else None}
         have = [counters[k] for k in kerns if k in counters]
         if have:
             row["ncu_dram_bytes_per_launch"] = sum(c[0] for c in have)
