@@ -282,6 +282,13 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
                  : "memory");
 }
 
+// the TMA unit's L2 prefetch of a global range (16-byte aligned start, size
+// a multiple of 16 bytes); no completion to wait for
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;

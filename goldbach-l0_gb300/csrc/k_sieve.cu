@@ -138,14 +138,43 @@ __device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_
     return rem ? p - rem : 0;
 }
 
+// Tile-bin staging of the persistent tile kernel: the first kTbStage
+// offsets of an item's tile bin go into shared memory by bulk copies issued
+// at the item's start (they land while the CTA sieves), the rest is
+// prefetched into L2 by the TMA unit and read from there.
+constexpr uint32_t kTbStage = 20480;       // offsets (80 KB), a multiple of kTbPiece
+constexpr uint32_t kTbPiece = 4096;        // offsets per bulk copy (16 KB)
+
+// thread 0 at an item's start: stages the first min(n, kTbStage) offsets of
+// the tile bin e (n offsets; the copy rounded up to 16 bytes, which stays in
+// the bin: capacities are multiples of 32 offsets) into stg, completing on
+// bar, and prefetches the rest into L2. Returns the offsets staged.
+__device__ __forceinline__ uint32_t stage_tile_bin(uint32_t *stg, uint64_t *bar, const uint32_t *e, uint32_t n)
+{
+    const uint32_t staged = min(n, kTbStage);
+    if (n > kTbStage) bulk_prefetch_l2(e + kTbStage, ((n - kTbStage + 3u) & ~3u) * 4u);
+    if (!staged) return 0;
+    const uint32_t words = (staged + 3u) & ~3u;
+    fence_proxy_async();  // the CTA's earlier reads of stg before the copies
+    mbar_arrive_expect_tx(bar, words * 4u);
+    for (uint32_t w0 = 0; w0 < words; w0 += kTbPiece)
+        bulk_copy_g2s(stg + w0, e + w0, min(kTbPiece, words - w0) * 4u, bar);
+    return staged;
+}
+
 // Sieves bits [t0, t0 + tl) of class array k of a run in shared memory s
 // (the group patterns already in pat) and stores them. tl is a multiple of
 // 128 bits. Ends with the CTA synchronized, s free for the next tile.
 // kVec4: the context's own prime and reciprocal arrays (16-byte aligned,
-// padded by 4 words), read four at a time; otherwise any arrays.
+// padded by 4 words), read four at a time, and the tile bin staged by
+// stage_tile_bin (*nb offsets, the first min(*nb, kTbStage) in stg once bar
+// completes the phase of parity bit 0 of phase); otherwise any arrays and
+// the tile bin read from global memory.
 template <bool kVec4>
 __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo &gi, const uint32_t *pat,
-                                          uint32_t *s, uint32_t k, uint32_t t0, uint32_t tl)
+                                          uint32_t *s, uint32_t k, uint32_t t0, uint32_t tl,
+                                          const uint32_t *stg = nullptr, uint64_t *bar = nullptr,
+                                          uint32_t *phase = nullptr, const uint32_t *nb = nullptr)
 {
     const uint32_t tid = threadIdx.x, bs = blockDim.x;
     const uint32_t tw = tl >> 5;
@@ -251,7 +280,50 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
         }
     }
     // a binned batch: the hit-list marks of this tile (offsets within it)
-    if (bp.tb_cap && bp.hl_quota) {
+    if constexpr (kVec4) {
+        const uint32_t n = *nb, staged = min(n, kTbStage);
+        if (staged) {
+            bool ok = mbar_wait(bar, *phase & 1u);
+            if (!ok) {
+                atomicOr(bp.err, kErrStaging);
+                ok = mbar_wait(bar, *phase & 1u);
+            }
+            *phase ^= 1u;
+            // offsets masked to the tile: a copy that missed its wait can
+            // leave stale words, never an access outside s
+            const uint32_t msk = (1u << bp.tile_log2) - 1u;
+            const uint4 *v4 = reinterpret_cast<const uint4 *>(stg);
+            for (uint32_t i = tid; ok && 4 * i < staged; i += bs) {
+                const uint4 v = v4[i];
+                const uint32_t at = 4 * i;
+                atomicAnd(&s[(v.x & msk) >> 5], ~(1u << (v.x & 31)));
+                if (at + 1 < staged) atomicAnd(&s[(v.y & msk) >> 5], ~(1u << (v.y & 31)));
+                if (at + 2 < staged) atomicAnd(&s[(v.z & msk) >> 5], ~(1u << (v.z & 31)));
+                if (at + 3 < staged) atomicAnd(&s[(v.w & msk) >> 5], ~(1u << (v.w & 31)));
+            }
+        }
+        if (n > kTbStage) {
+            // the rest from L2, four groups of four per thread in flight
+            const uint32_t tile = k * bp.tiles_pc + (t0 >> bp.tile_log2), m = n - kTbStage;
+            const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap + kTbStage);
+            for (uint32_t i = tid; 4 * i < m; i += 4 * bs) {
+                uint4 v[4];
+#pragma unroll
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const uint32_t g = i + u * bs;
+                    v[u] = 4 * g < m ? __ldcs(e + g) : make_uint4(0u, 0u, 0u, 0u);
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < 4; ++u) {
+                    const uint32_t at = 4 * (i + u * bs);
+                    if (at < m) atomicAnd(&s[v[u].x >> 5], ~(1u << (v[u].x & 31)));
+                    if (at + 1 < m) atomicAnd(&s[v[u].y >> 5], ~(1u << (v[u].y & 31)));
+                    if (at + 2 < m) atomicAnd(&s[v[u].z >> 5], ~(1u << (v[u].z & 31)));
+                    if (at + 3 < m) atomicAnd(&s[v[u].w >> 5], ~(1u << (v[u].w & 31)));
+                }
+            }
+        }
+    } else if (bp.tb_cap && bp.hl_quota) {
         const uint32_t tile = k * bp.tiles_pc + (t0 >> bp.tile_log2);
         const uint32_t n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
         const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap);
@@ -285,23 +357,40 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 // array's end.
 __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tile_log2)
 {
-    extern __shared__ uint32_t sm[];
+    // shared memory: the tile, the tile-bin staging buffer, the patterns
+    extern __shared__ __align__(16) uint32_t sm_tile[];
     const uint32_t tb = 1u << tile_log2;
-    uint32_t *s = sm;
-    uint32_t *pat = sm + (tb >> 5);
+    uint32_t *s = sm_tile;
+    uint32_t *stg = sm_tile + (tb >> 5);
+    uint32_t *pat = stg + kTbStage;
     const uint32_t nrun = d.h->nrun, items = d.h->tile_items;
     if (!nrun) return;
-    __shared__ uint32_t s_j;
+    __shared__ uint32_t s_j, s_nb;
+    __shared__ uint64_t s_bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_init_fence();
+    }
+    uint32_t phase = 0;
     for (uint32_t i = threadIdx.x; i < gi.words; i += blockDim.x) pat[i] = d.runs[0].pat[i];
     for (;;) {
-        const uint32_t j = next_item(d.work + kWorkTile, &s_j);
+        const uint32_t j = next_item(d.work + kWorkTile, &s_j);  // synchronizes the CTA
         if (j >= items) break;
         const uint32_t r = find_prefix(d.tile_pref, nrun, j);
         const BatchParams &bp = d.runs[r];
         const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
         const uint32_t k = local / tpc, t0 = (local - k * tpc) << tile_log2;
         const uint32_t tl = min(tb, bp.wpc * 32 - t0);
-        tile_body<true>(bp, gi, pat, s, k, t0, tl);
+        if (threadIdx.x == 0) {
+            uint32_t n = 0;
+            if (bp.tb_cap && bp.hl_quota) {
+                const uint32_t tile = k * tpc + (t0 >> bp.tile_log2);
+                n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
+                stage_tile_bin(stg, &s_bar, bp.tb_buf + size_t(tile) * bp.tb_cap, n);
+            }
+            s_nb = n;
+        }
+        tile_body<true>(bp, gi, pat, s, k, t0, tl, stg, &s_bar, &phase, &s_nb);
     }
 }
 
@@ -737,11 +826,17 @@ static size_t tile_smem(uint32_t tile_log2, const gbk::GroupInfo &gi)
     return size_t(((1u << tile_log2) >> 5) + gi.words) * 4;
 }
 
+// the persistent tile kernel adds the tile-bin staging buffer
+static size_t tile_smem_staged(uint32_t tile_log2, const gbk::GroupInfo &gi)
+{
+    return tile_smem(tile_log2, gi) + size_t(gbk::kTbStage) * 4;
+}
+
 void tile_attributes(uint32_t tile_log2, const gbk::GroupInfo &gi)
 {
-    const int smem = int(tile_smem(tile_log2, gi));
-    cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(tile_smem_staged(tile_log2, gi)));
+    cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tile_smem(tile_log2, gi)));
 }
 
 void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
@@ -752,7 +847,7 @@ void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
                  cudaStream_t st)
 {
-    gbk::k_tile<<<g.sm, 1024, tile_smem(tile_log2, gi), st>>>(d, gi, tile_log2);
+    gbk::k_tile<<<g.sm, 1024, tile_smem_staged(tile_log2, gi), st>>>(d, gi, tile_log2);
 }
 
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
