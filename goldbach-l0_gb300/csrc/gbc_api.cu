@@ -159,7 +159,7 @@ std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n)
 
 // The odd primes <= n, shared by the contexts of a process: the last list
 // sieved is kept and a smaller bound takes a prefix of it.
-static std::vector<uint32_t> cached_primes(uint64_t n)
+std::vector<uint32_t> gbh_cached_primes(uint64_t n)
 {
     static std::mutex mu;
     static std::shared_ptr<const std::vector<uint32_t>> last;
@@ -403,7 +403,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     // (the reference's base_prime_bound, include/primes.hpp:222-225)
     const double rt = std::sqrt(double(cfg.limit + 3)) + 16.0;
     const uint64_t bound = rt >= 4294967295.0 ? 0xFFFFFFFFull : uint64_t(rt);
-    ctx->primes = cached_primes(std::max<uint64_t>(bound, 127));
+    ctx->primes = gbh_cached_primes(std::max<uint64_t>(bound, 127));
     const auto &pr = ctx->primes;
     ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
     ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());

@@ -110,3 +110,6 @@ struct gbc_ctx {
 };
 
 std::vector<uint32_t> gbh_odd_primes_upto(uint64_t n);
+// the same, shared by the contexts of a process (the last list sieved is
+// kept; a smaller bound takes a prefix of it)
+std::vector<uint32_t> gbh_cached_primes(uint64_t n);

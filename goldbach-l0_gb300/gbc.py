@@ -88,6 +88,17 @@ class ServerStats(C.Structure):
                 ("device_bytes", C.c_uint64), ("hbm_budget", C.c_uint64)]
 
 
+class SparseConfig(C.Structure):
+    _fields_ = [("limit", C.c_uint64), ("dlt_log2", C.c_uint32), ("pmax", C.c_uint32), ("group_cap", C.c_uint32),
+                ("device", C.c_int32), ("host_only", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+class SparseResult(C.Structure):
+    _fields_ = [("evens", C.c_uint64), ("pending", C.c_uint64), ("map_primes", C.c_uint64), ("groups", C.c_uint64),
+                ("segments", C.c_uint64), ("ms_sieve", C.c_double), ("ms_large", C.c_double),
+                ("ms_check", C.c_double), ("ms_total", C.c_double)]
+
+
 # every entry point of include/gbc.h: name -> (restype, argtypes)
 SIGNATURES = {
     "gbc_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
@@ -134,6 +145,17 @@ SIGNATURES = {
     "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),
+    "gbc_sparse_create": (C.c_int, [C.POINTER(SparseConfig), C.POINTER(C.c_void_p)]),
+    "gbc_sparse_destroy": (None, [C.c_void_p]),
+    "gbc_sparse_last_error": (C.c_char_p, [C.c_void_p]),
+    "gbc_sparse_geometry": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
+    "gbc_sparse_verify": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(SparseResult)]),
+    "gbc_sparse_pending": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gbc_sparse_map": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint64]),
+    "gbc_sparse_witness": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "gbc_sparse_plan": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int]),
 }
 
 _lib = None
@@ -399,3 +421,79 @@ def segments_of(start, limit, segment_even):
             break
         s = e + 2
     return segs
+
+
+class Sparse:
+    """One gbc_sparse: the sparse class map cross-check (include/gbc.h; the
+    reference's --sparse path, src/sparse.cpp:840-973). `limit` sizes the
+    sieving primes; evens per class and segment 2^dlt_log2; candidates up to
+    pmax; group_cap limits the candidate groups the GPU tests per even class
+    (0: all); host_only builds the residues and the plan without a device."""
+
+    def __init__(self, limit, dlt_log2=0, pmax=0, group_cap=0, device=0, host_only=False):
+        self.lib = load()
+        cfg = SparseConfig(limit=limit, dlt_log2=dlt_log2, pmax=pmax, group_cap=group_cap, device=device,
+                           host_only=1 if host_only else 0)
+        h = C.c_void_p()
+        rc = self.lib.gbc_sparse_create(C.byref(cfg), C.byref(h))
+        self.h = h
+        if rc:
+            msg = self.lib.gbc_sparse_last_error(h).decode() if h else "no context"
+            self.close()
+            raise GbcError(rc, msg)
+        M, K, tb, dlt, pm = (C.c_uint32() for _ in range(5))
+        res = (C.c_uint32 * 16)()
+        self._check(self.lib.gbc_sparse_geometry(self.h, C.byref(M), C.byref(K), res, C.byref(tb), C.byref(dlt),
+                                                 C.byref(pm)))
+        self.M, self.K, self.tb, self.dlt, self.pmax = M.value, K.value, tb.value, dlt.value, pm.value
+        self.residues = list(res[:self.K])
+
+    def _check(self, rc):
+        if rc:
+            raise GbcError(rc, self.lib.gbc_sparse_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbc_sparse_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def verify(self, start, limit):
+        r = SparseResult()
+        self._check(self.lib.gbc_sparse_verify(self.h, start, limit, C.byref(r)))
+        return r
+
+    def pending(self):
+        n = C.c_uint64()
+        self._check(self.lib.gbc_sparse_pending(self.h, None, 0, C.byref(n)))
+        buf = (C.c_uint64 * max(1, n.value))()
+        self._check(self.lib.gbc_sparse_pending(self.h, buf, n.value, None))
+        return list(buf[:n.value])
+
+    def map(self, n0, dl):
+        """The K rows of the segment at n0 (a multiple of M), dl evens per
+        class: a list of K lists of row words."""
+        rows = (dl + self.tb + 31) // 32
+        buf = (C.c_uint32 * (self.K * rows))()
+        self._check(self.lib.gbc_sparse_map(self.h, n0, dl, buf, self.K * rows))
+        return [list(buf[k * rows:(k + 1) * rows]) for k in range(self.K)]
+
+    def witness(self, start, count):
+        buf = (C.c_uint32 * count)()
+        self._check(self.lib.gbc_sparse_witness(self.h, start, count, buf))
+        return list(buf)
+
+    def plan(self, r):
+        """Even class r's candidates in plan order: [(p, group index)]."""
+        n = self.lib.gbc_sparse_plan(self.h, r, None, None, 0)
+        if n < 0:
+            self._check(n)
+        p = (C.c_uint32 * max(1, n))()
+        g = (C.c_uint32 * max(1, n))()
+        self.lib.gbc_sparse_plan(self.h, r, p, g, n)
+        return list(zip(p[:n], g[:n]))

@@ -438,6 +438,92 @@ int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_t *d_primes
                           uint32_t max_prime, uint32_t *d_map, uint64_t map_words, uint64_t *base_out,
                           uint32_t *nblk_out, uint32_t *wpc_out, void *stream, char *err, size_t err_cap);
 
+/* ---- sparse class map: an independent verify-only cross-check ---------------
+ * The reference's opt-in sparse path (`--sparse`; include/sparse.hpp:1-33
+ * geometry, src/sparse.cpp:840-973 run_gpu_sparse, kernels/sparse.cl).
+ * Every even n needs one certified prime q = n - p, so the map holds only
+ * the q of K = 12 residue classes c_k mod M = 30030 (0.04% of the integers),
+ * chosen so that every even class r = n mod M reaches at least one of them
+ * (r - c_k a unit mod M); the candidates p <= pmax of those residues then
+ * verify an even through a set map bit. It shares no map, sieve or checker
+ * with the dense path and keeps no statistics: it verifies. Evens the GPU
+ * leaves are resolved by an ascending Miller-Rabin scan on the CPU.
+ *
+ * Geometry (all integers): segment s verifies n in [N_s, N_s + M dlt),
+ * N_s = N_0 + s M dlt, N_0 = start rounded down to a multiple of M; class
+ * k's bit t <-> q = N_s - M TB + c_k + M t, t < dl + TB (dl <= dlt: the
+ * segment's evens per class); even n = N_s + r + M i; a candidate
+ * p = ((r - c_k) mod M) + M a tests bit t = i + TB - a - [r < c_k].
+ * Valid for start - M (TB + 1) > sqrt(limit) and start > pmax (the map's q
+ * above every sieving prime); lower starts are GBC_E_ARG ("use the dense
+ * path"). */
+typedef struct gbc_sparse gbc_sparse;
+
+typedef struct gbc_sparse_config {
+    uint64_t limit;     /* largest even any call verifies (sizes the sieving primes) */
+    uint32_t dlt_log2;  /* evens per even class and segment = 2^dlt_log2, 12..26; 0 = 26 (1.0e12 evens) */
+    uint32_t pmax;      /* candidate bound, 1e5..2e8; 0 = 40,000,000 (about 413 primes per residue) */
+    uint32_t group_cap; /* candidate groups the GPU tests per even class (0 = all); fewer leaves evens to the CPU */
+    int device;
+    uint32_t host_only; /* 1: residues and plan only, no device (geometry and plan queries; the rest GBC_E_STATE) */
+    uint32_t reserved[3];
+} gbc_sparse_config;
+
+typedef struct gbc_sparse_result {
+    uint64_t evens;      /* evens in [start, limit] */
+    uint64_t pending;    /* evens the GPU left, each resolved on the CPU (the reference's leftovers) */
+    uint64_t map_primes; /* set map bits summed over the segments */
+    uint64_t groups;     /* candidate groups tested, summed over the checker's warps */
+    uint64_t segments;
+    double ms_sieve;     /* GPU time: first bits and tiles (primes below 2^20) */
+    double ms_large;     /* GPU time: primes from 2^20 */
+    double ms_check;     /* GPU time: the checker */
+    double ms_total;     /* wall time of the segment loop, CPU resolution included */
+} gbc_sparse_result;
+
+/* Builds the residues (checked to reach every even class), the sieving
+ * primes up to sqrt(limit), the inverse table mod M and the checker plan:
+ * per even class, candidate groups (class k, window word o, a 32-bit mask
+ * of the candidates whose offset is 32 o + bit), the fullest first; every
+ * candidate is decoded back to p and proved prime, <= pmax and in a usable
+ * class before the plan is uploaded (the reference's validate_plan_scm). */
+int gbc_sparse_create(const gbc_sparse_config *cfg, gbc_sparse **out);
+void gbc_sparse_destroy(gbc_sparse *sp);
+const char *gbc_sparse_last_error(const gbc_sparse *sp);
+
+/* M, K, the K residues (res: K entries), TB, dlt and pmax; any may be NULL. */
+int gbc_sparse_geometry(const gbc_sparse *sp, uint32_t *M, uint32_t *K, uint32_t *res, uint32_t *tb, uint32_t *dlt,
+                        uint32_t *pmax);
+
+/* Verifies every even of [start, limit] (start rounded up, limit down to
+ * even): per segment the map (tiles, then large primes), the checker, and
+ * the CPU for the evens it left. Fails closed: GBC_E_DEVICE on a device
+ * error flag or when the checker's even count differs from the range's,
+ * GBC_E_OVERFLOW when a segment leaves more than 2^20 words pending, and
+ * GBC_E_STATE for an even with no Goldbach pair (a counterexample). */
+int gbc_sparse_verify(gbc_sparse *sp, uint64_t start, uint64_t limit, gbc_sparse_result *res);
+
+/* The evens the last gbc_sparse_verify left to the CPU, ascending: up to
+ * cap into out, *count (may be NULL) = all of them. */
+int gbc_sparse_pending(const gbc_sparse *sp, uint64_t *out, uint64_t cap, uint64_t *count);
+
+/* The map of the segment at n0 (a multiple of M, n0 - M (TB + 1) above
+ * sqrt(limit)) with dl (1..dlt) evens per class: K rows of row_words =
+ * (dl + TB + 31) / 32 words, row k at out + k * row_words, bits at and
+ * above dl + TB zero. out_words < K * row_words: GBC_E_ARG. */
+int gbc_sparse_map(gbc_sparse *sp, uint64_t n0, uint32_t dl, uint32_t *out, uint64_t out_words);
+
+/* For each even n = start + 2 j, j < count (all in one segment's reach:
+ * n - (start rounded down to a multiple of M) < M dlt), the first candidate
+ * p in plan order (gbc_sparse_plan) whose q = n - p has its map bit set,
+ * within the first group_cap groups; 0 = none. */
+int gbc_sparse_witness(gbc_sparse *sp, uint64_t start, uint32_t count, uint32_t *p_out);
+
+/* Even class r's (r even, < M) candidates p in plan order (groups in order,
+ * within a group ascending offset) with their group index; returns how many
+ * there are, writing at most cap. */
+int gbc_sparse_plan(const gbc_sparse *sp, uint32_t r, uint32_t *p_out, uint32_t *group_out, int cap);
+
 #ifdef __cplusplus
 }
 #endif
