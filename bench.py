@@ -34,6 +34,11 @@ serving = Poisson arrivals at 50 windows/s for 60 s (seed 11), widths
          by the continuous-batching loop under a 150 GB HBM budget: p50 / p99
          latency from submission to completion, sustained evens/s, and a
          sample of windows compared with their runs alone.
+sparse = the sparse class map cross-check (12 residue classes mod 30030,
+         candidates to 4e7): --sparse-segments full segments of 30030 *
+         2^--sparse-dlt-log2 integers from 4e18, a warm pass then a timed
+         one; value from CUDA events, e2e the wall time of the call.
+         --sparse-only runs this leg alone.
 --slice runs the full 5e13-wide slice at 4e18 batched and plain, and checks
 3 seeded segments against the CPU oracle.
 --impl reference times the reference's CPU algorithm (the oracle's
@@ -377,6 +382,29 @@ def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64):
                       f"latency from submission to the window's merged statistics"}
 
 
+def sparse_leg(gbc, nseg=2, dlt_log2=26):
+    """The sparse class map cross-check (the reference's --sparse path):
+    nseg full segments of M 2^dlt_log2 integers from 4e18 (rounded down to a
+    multiple of M), one warm pass, then one timed pass; value from the
+    stages' CUDA events, e2e the wall time of gbc_sparse_verify (map, checker,
+    CPU resolution of the evens the GPU left)."""
+    a = 4 * 10**18 - 4 * 10**18 % 30030
+    span = 30030 * (1 << dlt_log2) * nseg
+    t0 = time.perf_counter()
+    with gbc.Sparse(limit=a + span + 10**9, dlt_log2=dlt_log2) as sp:
+        init_s = time.perf_counter() - t0
+        sp.verify(a, a + span - 2)
+        r = sp.verify(a, a + span - 2)
+    gpu_ms = r.ms_sieve + r.ms_large + r.ms_check
+    return {"metric": "sparse cross-check evens verified per second", "value": r.evens / gpu_ms / 1e6,
+            "unit": "G evens/s", "e2e": {"value": r.evens / r.ms_total / 1e6, "unit": "G evens/s"},
+            "evens": r.evens, "segments": r.segments, "pending": r.pending, "map_primes": r.map_primes,
+            "groups_per_warp_task": r.groups / (r.evens / 4096), "init_s": init_s,
+            "stage_ms": {"sieve": r.ms_sieve, "large": r.ms_large, "check": r.ms_check, "wall": r.ms_total},
+            "config": {"workload": f"[{a}, {a + span - 2}]", "M": 30030, "K": 12, "pmax": 40_000_000,
+                       "evens_per_class_per_segment": 1 << dlt_log2}}
+
+
 def slice_mode(args):
     """The full 5e13 slice at 4e18, batched and plain, 3 seeded segments
     against the CPU oracle."""
@@ -442,12 +470,19 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--slice", action="store_true")
+    ap.add_argument("--sparse-segments", type=int, default=2, help="segments of the sparse leg (0: none)")
+    ap.add_argument("--sparse-dlt-log2", type=int, default=26)
+    ap.add_argument("--sparse-only", action="store_true", help="run the sparse leg alone and print its line")
     ap.add_argument("--tuning", default="", help="autotuner record (default: the committed one); 'none': defaults")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.slice:
         return slice_mode(args)
+    if args.sparse_only:
+        import gbc
+        print(json.dumps(sparse_leg(gbc, args.sparse_segments, args.sparse_dlt_log2)))
+        return 0
     rep = Replicas()
     try:
         return run_gb300(args, rep)
@@ -624,6 +659,8 @@ def run_gb300(args, rep):
         out["windows"] = windows_leg(gbc, args.windows)
     if args.serve_seconds > 0:
         out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate)
+    if args.sparse_segments:
+        out["sparse"] = sparse_leg(gbc, args.sparse_segments, args.sparse_dlt_log2)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.cpu_evens, start)
     print(json.dumps(out))

@@ -104,6 +104,8 @@ int usage()
     std::fprintf(stderr,
                  "usage: goldbach_gb300 [--start N] --limit N [--segment N] [--batch N] [--stats-sample N] [--csv] "
                  "[--stats] [--verbose]\n"
+                 "       goldbach_gb300 --start N --limit N --sparse [--csv] [--verbose]   (the sparse class map "
+                 "cross-check; start well above sqrt(limit))\n"
                  "       goldbach_gb300 --start N --limit N --slice N --journal FILE [--release ID] [--stop-file F]\n"
                  "                      [--segment N] [--batch N] [--stats-sample N]   (journaled slices; exit 3 "
                  "on the stop file)\n");
@@ -115,7 +117,7 @@ int usage()
 int main(int argc, char **argv)
 {
     uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8, sample = 1, slice = 0;
-    bool csv = false, stats = false, verbose = false;
+    bool csv = false, stats = false, verbose = false, sparse = false;
     std::string journal, release = "gb300-1.0", stop_file;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
@@ -142,6 +144,7 @@ int main(int argc, char **argv)
         } else if (a == "--csv") csv = true;
         else if (a == "--stats") stats = true;
         else if (a == "--verbose") verbose = true;
+        else if (a == "--sparse") sparse = true;
         else return usage();
     }
     if (!limit) return usage();
@@ -154,6 +157,26 @@ int main(int argc, char **argv)
         return 1;
     }
     if ((slice != 0) != !journal.empty()) return usage();
+    if (sparse) {
+        if (slice || stats) return usage();
+        try {
+            const gb::RunStats st = gb::run_gpu_sparse(limit, verbose, start);
+            const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
+            if (csv)
+                std::printf("result=PASS,path=sparse,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64
+                            ",segments=%" PRIu64 ",leftovers=%" PRIu64 ",gpu_s=%.6f,wall_s=%.6f,evens_per_s=%.6g\n",
+                            st.start, st.limit, st.evens, st.segments, st.leftovers, st.gpu_seconds, st.wall_seconds,
+                            eps);
+            else
+                std::printf("PASS (sparse): every even n in [%" PRIu64 ", %" PRIu64 "] is a sum of two primes "
+                            "(%" PRIu64 " evens, %" PRIu64 " segments, %" PRIu64 " leftovers, %.3f G evens/s)\n",
+                            st.start, st.limit, st.evens, st.segments, st.leftovers, eps / 1e9);
+            return 0;
+        } catch (const gb::GbcError &e) {
+            std::fprintf(stderr, "FAIL: %s\n", e.what());
+            return e.code == GBC_E_ARG ? 2 : 1;
+        }
+    }
     gbc_config cfg{};
     cfg.limit = limit & ~uint64_t(1);
     cfg.segment_even = segment;

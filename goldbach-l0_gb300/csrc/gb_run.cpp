@@ -510,6 +510,46 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t s
     return st;
 }
 
+RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2)
+{
+    if (start_even < 4) start_even = 4;
+    if (start_even & 1) ++start_even;
+    if (limit & 1) --limit;
+    if (start_even > limit) throw GbcError(GBC_E_ARG, "sparse: start > limit");
+    gbc_sparse_config cfg{};
+    cfg.limit = limit;
+    cfg.dlt_log2 = dlt_log2;
+    gbc_sparse *sp = nullptr;
+    int rc = gbc_sparse_create(&cfg, &sp);
+    const auto done = [&](int code, const char *what) {
+        const std::string msg = std::string(what) + ": " + gbc_sparse_last_error(sp);
+        gbc_sparse_destroy(sp);
+        throw GbcError(code, msg);
+    };
+    if (rc != GBC_OK) done(rc, "gbc_sparse_create");
+    gbc_sparse_result r{};
+    rc = gbc_sparse_verify(sp, start_even, limit, &r);
+    if (rc != GBC_OK) done(rc, "gbc_sparse_verify");
+    gbc_sparse_destroy(sp);
+    RunStats st;
+    st.start = start_even;
+    st.limit = limit;
+    st.evens = r.evens;
+    st.segments = r.segments;
+    st.batches = r.segments;
+    st.leftovers = r.pending;
+    st.gpu_seconds = (r.ms_sieve + r.ms_large + r.ms_check) / 1e3;
+    st.wall_seconds = r.ms_total / 1e3;
+    st.tile_ms = r.ms_sieve;
+    st.large_ms = r.ms_large;
+    st.check_ms = r.ms_check;
+    if (verbose)
+        std::fprintf(stderr, "sparse [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, sieve %.3f large %.3f check "
+                     "%.3f ms, %" PRIu64 " evens left to the CPU\n",
+                     st.start, st.limit, st.segments, r.ms_sieve, r.ms_large, r.ms_check, r.pending);
+    return st;
+}
+
 }  // namespace gb
 
 extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gbc_run_result *res, char *line,

@@ -171,4 +171,10 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
 RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even = 4,
                  uint32_t max_batch = 8, uint16_t *pn = nullptr, uint32_t sample_every = 1);
 
+// gb::run_gpu_sparse (src/sparse.cpp:840-973): the sparse class map
+// cross-check of [start_even, limit] on one gbc_sparse context; evens,
+// segments, leftovers (evens the GPU left, proved on the CPU) and the
+// stage times. No statistics. Throws GbcError.
+RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
+
 }  // namespace gb

@@ -237,57 +237,98 @@ __global__ void __launch_bounds__(kCheckThreads, 4) k_sp_check(SpSeg s, const ui
         const uint32_t c = j / kClassBlocks, cb = j - c * kClassBlocks;
         const uint32_t *w0 = win + buf * kK * s.rw;
         const uint32_t cr1 = min(kHalfM, (cb + 1) * kClassBlock);
-        for (uint32_t cr = cb * kClassBlock + warp; ok && cr < cr1; cr += kCheckWarps) {
-            // the class's valid evens: i in [ilo, ihi)
-            const uint64_t base = s.N + 2 * cr;
-            uint64_t ilo = 0, ihi = 0;
-            if (s.limit >= base) {
-                ihi = min(uint64_t(s.dl), (s.limit - base) / kM + 1);
-                ilo = s.start > base ? (s.start - base + kM - 1) / kM : 0;
+        // a chunk inside [start, limit] for every even class needs no
+        // per-class range: the latest first even is class 0's, the earliest
+        // last even class M - 2's
+        const uint64_t ci0 = uint64_t(c) * kChunkEvens;
+        const uint64_t ilo_max = s.start > s.N ? (s.start - s.N + kM - 1) / kM : 0;
+        const uint64_t top = s.N + kM - 2;
+        const uint64_t ihi_min = s.limit >= top ? min(uint64_t(s.dl), (s.limit - top) / kM + 1) : 0;
+        const bool interior = ilo_max <= ci0 && ihi_min >= ci0 + kChunkEvens;
+        for (uint32_t q0 = cb * kClassBlock + warp; ok && q0 < cr1; q0 += 32 * kCheckWarps) {
+            // the group ranges of the warp's next 32 classes, one per lane
+            const uint32_t mine = q0 + lane * kCheckWarps;
+            uint32_t lg0 = 0, lg1 = 0;
+            if (mine < cr1) {
+                lg0 = __ldg(goff + mine);
+                lg1 = lg0 + min(__ldg(goff + mine + 1) - lg0, s.group_cap);
             }
-            uint32_t f[kV], all = ~0u;
+            const uint32_t nt = min(32u, (cr1 - q0 + kCheckWarps - 1) / kCheckWarps);
+            for (uint32_t tj = 0; tj < nt; ++tj) {
+                const uint32_t cr = q0 + tj * kCheckWarps;
+                const uint32_t g0 = __shfl_sync(~0u, lg0, tj), g1 = __shfl_sync(~0u, lg1, tj);
+                uint32_t f[kV];
+                if (interior) {
 #pragma unroll
-            for (uint32_t v = 0; v < kV; ++v) {
-                const uint64_t i0 = 32ull * (uint64_t(c) * kChunkWords + 32 * v + lane);
-                const uint32_t lo = ilo > i0 ? uint32_t(min(ilo - i0, uint64_t(32))) : 0u;
-                const uint32_t hi = ihi > i0 ? uint32_t(min(ihi - i0, uint64_t(32))) : 0u;
-                const uint32_t valid = hi > lo ? low_bits(hi) & ~low_bits(lo) : 0u;
-                nevens += __popc(valid);
-                f[v] = ~valid;
-                all &= f[v];
+                    for (uint32_t v = 0; v < kV; ++v) f[v] = 0u;
+                    nevens += 32 * kV;
+                } else {
+                    // the class's valid evens: i in [ilo, ihi)
+                    const uint64_t base = s.N + 2 * cr;
+                    uint64_t ilo = 0, ihi = 0;
+                    if (s.limit >= base) {
+                        ihi = min(uint64_t(s.dl), (s.limit - base) / kM + 1);
+                        ilo = s.start > base ? (s.start - base + kM - 1) / kM : 0;
+                    }
+                    uint32_t all = ~0u;
+#pragma unroll
+                    for (uint32_t v = 0; v < kV; ++v) {
+                        const uint64_t i0 = 32ull * (uint64_t(c) * kChunkWords + 32 * v + lane);
+                        const uint32_t lo = ilo > i0 ? uint32_t(min(ilo - i0, uint64_t(32))) : 0u;
+                        const uint32_t hi = ihi > i0 ? uint32_t(min(ihi - i0, uint64_t(32))) : 0u;
+                        const uint32_t valid = hi > lo ? low_bits(hi) & ~low_bits(lo) : 0u;
+                        nevens += __popc(valid);
+                        f[v] = ~valid;
+                        all &= f[v];
+                    }
+                    if (__all_sync(~0u, all == ~0u)) continue;
+                }
+                // the groups in plan order, 32 entries per coalesced load
+                uint32_t g = g0;
+                bool done = false;
+                while (!done && g < g1) {
+                    const uint32_t ng = min(32u, g1 - g);
+                    uint2 le = make_uint2(0u, 0u);
+                    if (lane < ng) le = __ldg(groups + g + lane);
+                    uint32_t u = 0;
+                    while (u < ng) {
+                        const uint32_t ex = __shfl_sync(~0u, le.x, u), ey = __shfl_sync(~0u, le.y, u);
+                        ++u;
+                        const uint32_t *row = w0 + (ex & 15u) * s.rw + (ex >> 4) + lane;
+                        uint32_t a[kV], b[kV];
+#pragma unroll
+                        for (uint32_t v = 0; v < kV; ++v) {
+                            a[v] = row[32 * v];
+                            b[v] = row[32 * v + 1];
+                        }
+                        // two candidates per step (an odd last one twice)
+                        for (uint32_t m = ey; m;) {
+                            const uint32_t s1 = __ffs(m) - 1;
+                            m &= m - 1;
+                            const uint32_t s2 = m ? __ffs(m) - 1 : s1;
+                            m &= m - 1;
+#pragma unroll
+                            for (uint32_t v = 0; v < kV; ++v)
+                                f[v] |= __funnelshift_r(a[v], b[v], s1) | __funnelshift_r(a[v], b[v], s2);
+                        }
+                        uint32_t all = f[0];
+#pragma unroll
+                        for (uint32_t v = 1; v < kV; ++v) all &= f[v];
+                        if (__all_sync(~0u, all == ~0u)) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    g += u;
+                }
+                ngroups += g - g0;
+#pragma unroll
+                for (uint32_t v = 0; v < kV; ++v)
+                    if (f[v] != ~0u) {
+                        const uint32_t slot = atomicAdd(&s.ctr->npend, 1u);
+                        if (slot < kPendCap) pend[slot] = make_uint4(cr, c * kChunkWords + 32 * v + lane, ~f[v], 0u);
+                    }
             }
-            if (__all_sync(~0u, all == ~0u)) continue;
-            const uint32_t g0 = __ldg(goff + cr), g1 = g0 + min(__ldg(goff + cr + 1) - g0, s.group_cap);
-            uint32_t g = g0;
-            while (g < g1) {
-                const uint2 e = __ldg(groups + g);
-                ++g;
-                const uint32_t *row = w0 + (e.x & 15u) * s.rw + (e.x >> 4) + lane;
-                uint32_t a[kV], b[kV];
-#pragma unroll
-                for (uint32_t v = 0; v < kV; ++v) {
-                    a[v] = row[32 * v];
-                    b[v] = row[32 * v + 1];
-                }
-                uint32_t m = e.y;
-                while (m) {
-                    const uint32_t sh = __ffs(m) - 1;
-                    m &= m - 1;
-#pragma unroll
-                    for (uint32_t v = 0; v < kV; ++v) f[v] |= __funnelshift_r(a[v], b[v], sh);
-                }
-                all = f[0];
-#pragma unroll
-                for (uint32_t v = 1; v < kV; ++v) all &= f[v];
-                if (__all_sync(~0u, all == ~0u)) break;
-            }
-            ngroups += g - g0;
-#pragma unroll
-            for (uint32_t v = 0; v < kV; ++v)
-                if (f[v] != ~0u) {
-                    const uint32_t slot = atomicAdd(&s.ctr->npend, 1u);
-                    if (slot < kPendCap) pend[slot] = make_uint4(cr, c * kChunkWords + 32 * v + lane, ~f[v], 0u);
-                }
         }
         j = jn;
         buf ^= 1u;

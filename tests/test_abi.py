@@ -95,3 +95,8 @@ def test_cli_usage_errors():
     assert subprocess.run([exe, "--start", "100", "--limit", "50"], capture_output=True).returncode == 2
     assert subprocess.run([exe, "--limit", "1.9e19"], capture_output=True).returncode == 2   # above 2^64
     assert subprocess.run([exe, "--limit", "18446743e12"], capture_output=True).returncode == 1  # > 2^64 - 2^40
+    # the sparse path: the same limit check before any GPU work; no statistics
+    r = subprocess.run([exe, "--start", "18446742974197000000", "--limit", "18446744073709551614", "--sparse"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "supported maximum" in r.stderr and "PASS" not in r.stdout
+    assert subprocess.run([exe, "--limit", "1e12", "--sparse", "--stats"], capture_output=True).returncode == 2

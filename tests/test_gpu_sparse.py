@@ -115,3 +115,16 @@ def test_rejects_low_start_and_high_limit():
         assert e.value.code == -1
         r = sp.verify(10**12 - 2 * 10**6, 10**12)
         assert r.evens == 10**6 + 1
+
+
+def test_cli_sparse_run():
+    import os
+    import subprocess
+    from conftest import ROOT
+    exe = os.path.join(ROOT, "goldbach-l0_gb300", "bin", "goldbach_gb300")
+    r = subprocess.run([exe, "--start", "4e18", "--limit", "4000000002000000001", "--sparse", "--csv"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    kv = dict(x.split("=", 1) for x in r.stdout.strip().split(","))
+    assert kv["result"] == "PASS" and kv["path"] == "sparse"
+    assert int(kv["evens"]) == 10**9 + 1 and int(kv["start"]) == 4 * 10**18
