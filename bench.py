@@ -399,7 +399,7 @@ def sparse_leg(gbc, nseg=2, dlt_log2=26):
     return {"metric": "sparse cross-check evens verified per second", "value": r.evens / gpu_ms / 1e6,
             "unit": "G evens/s", "e2e": {"value": r.evens / r.ms_total / 1e6, "unit": "G evens/s"},
             "evens": r.evens, "segments": r.segments, "pending": r.pending, "map_primes": r.map_primes,
-            "groups_per_warp_task": r.groups / (r.evens / 4096), "init_s": init_s,
+            "entries_per_warp_task": r.groups / (r.evens / 4096), "init_s": init_s,
             "stage_ms": {"sieve": r.ms_sieve, "large": r.ms_large, "check": r.ms_check, "wall": r.ms_total},
             "config": {"workload": f"[{a}, {a + span - 2}]", "M": 30030, "K": 12, "pmax": 40_000_000,
                        "evens_per_class_per_segment": 1 << dlt_log2}}

@@ -25,7 +25,7 @@
 //               staged in shared memory by bulk copies (two buffers: the next
 //               item's copies land while this one is checked); a warp takes an
 //               even class, each lane four words of its evens, and ORs in the
-//               candidate groups (class, window word, 32-bit offset mask) in
+//               plan entries (class, window word, up to six packed offsets) in
 //               plan order until every even of the warp is verified; words left
 //               unverified go to the pending list, which the host resolves by
 //               an ascending Miller-Rabin scan.
@@ -58,6 +58,16 @@ constexpr uint32_t kClassBlock = 128 * kCheckWarps;  // even classes per checker
 constexpr uint32_t kClassBlocks = (kHalfM + kClassBlock - 1) / kClassBlock;
 constexpr uint32_t kPendCap = 1u << 20;      // pending words per segment
 constexpr uint32_t kErrStaging = 1u << 0;    // a bulk copy missed its wait limit
+constexpr uint32_t kEntryMax = 6;            // candidates per plan entry
+
+// A plan entry: up to six candidates of one class k and one window word o,
+// as x = k | o << 4 | count << 12 and y = their offsets within the word, 5
+// bits each, ascending (an odd count repeats the last offset, so entries
+// are taken two offsets at a time; a funnel shift reads only an offset's
+// low five bits, so y >> 5 j needs no mask).
+__host__ __device__ __forceinline__ uint32_t entry_k(uint32_t x) { return x & 15u; }
+__host__ __device__ __forceinline__ uint32_t entry_o(uint32_t x) { return (x >> 4) & 255u; }
+__host__ __device__ __forceinline__ uint32_t entry_n(uint32_t x) { return (x >> 12) & 7u; }
 
 // inverse of a odd mod 2^64 (Newton: each step doubles the correct bits)
 constexpr uint64_t inv64(uint64_t a)
@@ -294,23 +304,25 @@ __global__ void __launch_bounds__(kCheckThreads, 4) k_sp_check(SpSeg s, const ui
                     while (u < ng) {
                         const uint32_t ex = __shfl_sync(~0u, le.x, u), ey = __shfl_sync(~0u, le.y, u);
                         ++u;
-                        const uint32_t *row = w0 + (ex & 15u) * s.rw + (ex >> 4) + lane;
+                        const uint32_t *row = w0 + entry_k(ex) * s.rw + entry_o(ex) + lane;
                         uint32_t a[kV], b[kV];
 #pragma unroll
                         for (uint32_t v = 0; v < kV; ++v) {
                             a[v] = row[32 * v];
                             b[v] = row[32 * v + 1];
                         }
-                        // two candidates per step (an odd last one twice)
-                        for (uint32_t m = ey; m;) {
-                            const uint32_t s1 = __ffs(m) - 1;
-                            m &= m - 1;
-                            const uint32_t s2 = m ? __ffs(m) - 1 : s1;
-                            m &= m - 1;
+                        // two candidates per step
+                        const uint32_t np = (entry_n(ex) + 1) >> 1;
+                        uint32_t y = ey;
 #pragma unroll
-                            for (uint32_t v = 0; v < kV; ++v)
-                                f[v] |= __funnelshift_r(a[v], b[v], s1) | __funnelshift_r(a[v], b[v], s2);
-                        }
+                        for (uint32_t jp = 0; jp < (kEntryMax + 1) / 2; ++jp)
+                            if (jp < np) {
+                                const uint32_t y2 = y >> 5;
+#pragma unroll
+                                for (uint32_t v = 0; v < kV; ++v)
+                                    f[v] |= __funnelshift_r(a[v], b[v], y) | __funnelshift_r(a[v], b[v], y2);
+                                y >>= 10;
+                            }
                         uint32_t all = f[0];
 #pragma unroll
                         for (uint32_t v = 1; v < kV; ++v) all &= f[v];
@@ -355,12 +367,9 @@ __global__ void __launch_bounds__(256) k_sp_witness(SpSeg s, uint64_t start, uin
     uint32_t p = 0;
     for (uint32_t g = g0; g < g1 && !p; ++g) {
         const uint2 e = groups[g];
-        const uint32_t k = e.x & 15u, o = e.x >> 4;
-        uint32_t m = e.y;
-        while (m) {
-            const uint32_t sh = __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t U = 32 * o + sh;
+        const uint32_t k = entry_k(e.x), o = entry_o(e.x), n = entry_n(e.x);
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint32_t U = 32 * o + ((e.y >> (5 * q)) & 31u);
             const uint64_t t = i + U;
             if ((s.map[size_t(k) * s.stride + (t >> 5)] >> (t & 31)) & 1u) {
                 const uint32_t ck = s.c[k];
@@ -383,7 +392,7 @@ struct gbc_sparse {
     uint32_t tb = 0, dlt = 0, rw = 0, stride = 0, tiles_max = 0, pmax = 0;
     uint32_t c[kK] = {};
     uint64_t qbound = 0;                   // sieving primes up to isqrt(limit + M)
-    std::vector<uint2> groups;             // plan: (k | o << 4, offset mask)
+    std::vector<uint2> groups;             // plan entries (entry_k / entry_o / entry_n, packed offsets)
     std::vector<uint32_t> goff;            // kHalfM + 1 group offsets
     uint32_t *d_primes = nullptr;          // sieving primes >= 17
     uint32_t nprimes = 0, nsmall = 0, nwarp = 0;
@@ -514,8 +523,9 @@ uint32_t decode(uint32_t r, uint32_t ck, uint32_t tb, uint32_t U)
 }
 
 // The checker plan: per even class r, the candidates p <= pmax of every
-// usable class k grouped by (k, window word o = U / 32) as 32-bit offset
-// masks, the fullest groups first (ties: k, then o). Classes in parallel.
+// usable class k grouped by (k, window word o = U / 32), the fullest groups
+// first (ties: k, then o), each group stored as entries of up to six
+// offsets in ascending order. Classes in parallel.
 void build_plan(gbc_sparse *sp, const std::vector<uint8_t> &isp)
 {
     const uint32_t tb = sp->tb, ow = tb / 32 + 1;
@@ -541,12 +551,24 @@ void build_plan(gbc_sparse *sp, const std::vector<uint8_t> &isp)
                             mask[size_t(k) * ow + U / 32] |= 1u << (U % 32);
                         }
                     }
-                    std::vector<uint2> &g = per[x];
+                    std::vector<uint2> g;
                     for (uint32_t k = 0; k < kK; ++k)
                         for (uint32_t o = 0; o < ow; ++o)
                             if (mask[size_t(k) * ow + o]) g.push_back(make_uint2(k | o << 4, mask[size_t(k) * ow + o]));
                     std::stable_sort(g.begin(), g.end(),
                                      [](uint2 u, uint2 v) { return __builtin_popcount(u.y) > __builtin_popcount(v.y); });
+                    // each group as entries of up to kEntryMax offsets, ascending
+                    for (const uint2 &e : g) {
+                        uint32_t sh[32], n = 0;
+                        for (uint32_t m = e.y; m; m &= m - 1) sh[n++] = uint32_t(__builtin_ctz(m));
+                        for (uint32_t i = 0; i < n; i += kEntryMax) {
+                            const uint32_t c = std::min(kEntryMax, n - i);
+                            uint32_t y = 0;
+                            for (uint32_t q = 0; q < c; ++q) y |= sh[i + q] << (5 * q);
+                            if (c & 1) y |= sh[i + c - 1] << (5 * c);
+                            per[x].push_back(make_uint2(e.x | c << 12, y));
+                        }
+                    }
                 }
             }
         });
@@ -568,13 +590,14 @@ bool validate_plan(const gbc_sparse *sp, const std::vector<uint8_t> &isp, std::s
         const uint32_t r = 2 * x;
         for (uint32_t g = sp->goff[x]; g < sp->goff[x + 1]; ++g) {
             const uint2 e = sp->groups[g];
-            const uint32_t k = e.x & 15u, o = e.x >> 4;
-            if (k >= kK) {
-                *why = "class index";
+            const uint32_t k = entry_k(e.x), o = entry_o(e.x), n = entry_n(e.x);
+            if (k >= kK || n == 0 || n > kEntryMax || (e.x >> 15) ||
+                ((n & 1) && ((e.y >> (5 * n)) & 31u) != ((e.y >> (5 * (n - 1))) & 31u))) {
+                *why = "entry layout";
                 return false;
             }
-            for (uint32_t m = e.y; m; m &= m - 1) {
-                const uint32_t U = 32 * o + uint32_t(__builtin_ctz(m));
+            for (uint32_t q = 0; q < n; ++q) {
+                const uint32_t U = 32 * o + ((e.y >> (5 * q)) & 31u);
                 const uint32_t ck = sp->c[k];
                 if (U > sp->tb || U + (r < ck ? 1u : 0u) > sp->tb) {
                     *why = "offset outside the window";
@@ -896,10 +919,10 @@ extern "C" int gbc_sparse_plan(const gbc_sparse *sp, uint32_t r, uint32_t *p_out
     int n = 0;
     for (uint32_t g = sp->goff[x]; g < sp->goff[x + 1]; ++g) {
         const uint2 e = sp->groups[g];
-        const uint32_t k = e.x & 15u, o = e.x >> 4;
-        for (uint32_t m = e.y; m; m &= m - 1, ++n) {
+        const uint32_t k = entry_k(e.x), o = entry_o(e.x), c = entry_n(e.x);
+        for (uint32_t q = 0; q < c; ++q, ++n) {
             if (n >= cap) continue;
-            const uint32_t U = 32 * o + uint32_t(__builtin_ctz(m));
+            const uint32_t U = 32 * o + ((e.y >> (5 * q)) & 31u);
             if (p_out) p_out[n] = decode(r, sp->c[k], sp->tb, U);
             if (group_out) group_out[n] = g - sp->goff[x];
         }

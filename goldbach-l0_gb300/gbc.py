@@ -427,7 +427,7 @@ class Sparse:
     """One gbc_sparse: the sparse class map cross-check (include/gbc.h; the
     reference's --sparse path, src/sparse.cpp:840-973). `limit` sizes the
     sieving primes; evens per class and segment 2^dlt_log2; candidates up to
-    pmax; group_cap limits the candidate groups the GPU tests per even class
+    pmax; group_cap limits the plan entries the GPU tests per even class
     (0: all); host_only builds the residues and the plan without a device."""
 
     def __init__(self, limit, dlt_log2=0, pmax=0, group_cap=0, device=0, host_only=False):
@@ -489,7 +489,7 @@ class Sparse:
         return list(buf)
 
     def plan(self, r):
-        """Even class r's candidates in plan order: [(p, group index)]."""
+        """Even class r's candidates in plan order: [(p, entry index)]."""
         n = self.lib.gbc_sparse_plan(self.h, r, None, None, 0)
         if n < 0:
             self._check(n)

@@ -463,7 +463,7 @@ typedef struct gbc_sparse_config {
     uint64_t limit;     /* largest even any call verifies (sizes the sieving primes) */
     uint32_t dlt_log2;  /* evens per even class and segment = 2^dlt_log2, 12..26; 0 = 26 (1.0e12 evens) */
     uint32_t pmax;      /* candidate bound, 1e5..2e8; 0 = 40,000,000 (about 413 primes per residue) */
-    uint32_t group_cap; /* candidate groups the GPU tests per even class (0 = all); fewer leaves evens to the CPU */
+    uint32_t group_cap; /* plan entries the GPU tests per even class (0 = all); fewer leaves evens to the CPU */
     int device;
     uint32_t host_only; /* 1: residues and plan only, no device (geometry and plan queries; the rest GBC_E_STATE) */
     uint32_t reserved[3];
@@ -473,7 +473,7 @@ typedef struct gbc_sparse_result {
     uint64_t evens;      /* evens in [start, limit] */
     uint64_t pending;    /* evens the GPU left, each resolved on the CPU (the reference's leftovers) */
     uint64_t map_primes; /* set map bits summed over the segments */
-    uint64_t groups;     /* candidate groups tested, summed over the checker's warps */
+    uint64_t groups;     /* plan entries tested, summed over the checker's warps */
     uint64_t segments;
     double ms_sieve;     /* GPU time: first bits and tiles (primes below 2^20) */
     double ms_large;     /* GPU time: primes from 2^20 */
@@ -483,10 +483,12 @@ typedef struct gbc_sparse_result {
 
 /* Builds the residues (checked to reach every even class), the sieving
  * primes up to sqrt(limit), the inverse table mod M and the checker plan:
- * per even class, candidate groups (class k, window word o, a 32-bit mask
- * of the candidates whose offset is 32 o + bit), the fullest first; every
- * candidate is decoded back to p and proved prime, <= pmax and in a usable
- * class before the plan is uploaded (the reference's validate_plan_scm). */
+ * per even class, the candidates grouped by (class k, window word o: the
+ * candidates whose offset is 32 o + 0..31), the fullest groups first, each
+ * group stored as plan entries of up to six offsets in ascending order;
+ * every candidate is decoded back to p and proved prime, <= pmax and in a
+ * usable class before the plan is uploaded (the reference's
+ * validate_plan_scm). */
 int gbc_sparse_create(const gbc_sparse_config *cfg, gbc_sparse **out);
 void gbc_sparse_destroy(gbc_sparse *sp);
 const char *gbc_sparse_last_error(const gbc_sparse *sp);
@@ -516,12 +518,12 @@ int gbc_sparse_map(gbc_sparse *sp, uint64_t n0, uint32_t dl, uint32_t *out, uint
 /* For each even n = start + 2 j, j < count (all in one segment's reach:
  * n - (start rounded down to a multiple of M) < M dlt), the first candidate
  * p in plan order (gbc_sparse_plan) whose q = n - p has its map bit set,
- * within the first group_cap groups; 0 = none. */
+ * within the first group_cap entries; 0 = none. */
 int gbc_sparse_witness(gbc_sparse *sp, uint64_t start, uint32_t count, uint32_t *p_out);
 
-/* Even class r's (r even, < M) candidates p in plan order (groups in order,
- * within a group ascending offset) with their group index; returns how many
- * there are, writing at most cap. */
+/* Even class r's (r even, < M) candidates p in plan order (entries in
+ * order, within an entry ascending offset) with their entry index; returns
+ * how many there are, writing at most cap. */
 int gbc_sparse_plan(const gbc_sparse *sp, uint32_t r, uint32_t *p_out, uint32_t *group_out, int cap);
 
 #ifdef __cplusplus

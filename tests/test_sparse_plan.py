@@ -53,19 +53,32 @@ def check_plan(sp, r, isp):
     want = so.candidates(r, sp.residues, sp.pmax, isp)
     ps = [p for p, _ in got]
     assert sorted(ps) == sorted(p for p, _ in want), r  # every candidate, each once
-    groups = [g for _, g in got]
-    assert groups == sorted(groups)
-    # within a group one class k and one window word; groups fullest first
+    entries = [g for _, g in got]
+    assert entries == sorted(entries)
     ks = dict(want)
-    sizes = []
-    for g in sorted(set(groups)):
-        members = [p for p, gg in got if gg == g]
-        assert len({ks[p] for p in members}) == 1
-        c = sp.residues[ks[members[0]]]
-        offs = [sp.tb - (p - (r - c) % sp.M) // sp.M - (1 if r < c else 0) for p in members]
+
+    def offset(p):
+        c = sp.residues[ks[p]]
+        return sp.tb - (p - (r - c) % sp.M) // sp.M - (1 if r < c else 0)
+
+    # an entry: one class k and one window word, up to six offsets ascending;
+    # consecutive entries of one (k, word) form a group: all but its last
+    # entry full, groups fullest first, each (k, word) once
+    groups = []
+    for e in sorted(set(entries)):
+        members = [p for p, g in got if g == e]
+        offs = [offset(p) for p in members]
+        assert 1 <= len(members) <= 6 and offs == sorted(offs)
+        assert len({ks[p] for p in members}) == 1 and len({u // 32 for u in offs}) == 1
         assert all(0 <= u <= sp.tb for u in offs)
-        assert len({u // 32 for u in offs}) == 1 and offs == sorted(offs)
-        sizes.append(len(members))
+        key = (ks[members[0]], offs[0] // 32)
+        if groups and groups[-1][0] == key:
+            assert groups[-1][1][-1] == 6
+            groups[-1][1].append(len(members))
+        else:
+            groups.append((key, [len(members)]))
+    assert len({k for k, _ in groups}) == len(groups)
+    sizes = [sum(n) for _, n in groups]
     assert sizes == sorted(sizes, reverse=True)
 
 
