@@ -91,7 +91,7 @@ struct SpSeg {
     uint32_t dl, T, tb;       // evens per class; map bits per row (dl + TB); TB
     uint32_t tiles, chunks;   // tiles per row; checker chunks
     uint32_t stride, rw;      // words per map row; staged words per row and item
-    uint32_t group_cap;       // groups per class (all: ~0)
+    uint32_t group_cap;       // plan entries per class (all: ~0)
     uint32_t *map;
     SpCtr *ctr;
     uint32_t c[kK];           // residues
@@ -99,7 +99,8 @@ struct SpSeg {
 
 // First bit t of a multiple of p in each class row: q = p m, m = c_k p^-1
 // (mod M), the least such m with p m >= Q; then (p m - Q - c_k) / M, an
-// exact division (by 2, then by the inverse of M / 2 mod 2^64). t < p + 2.
+// exact division (by 2, then by the inverse of M / 2 mod 2^64). t < p:
+// p m - Q < p M, since the m one period lower gives a multiple below Q.
 __device__ __forceinline__ void sp_first(uint64_t Q, uint32_t p, uint32_t invp, const uint32_t *c, uint64_t *t)
 {
     const uint64_t qd = Q / p;
