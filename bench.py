@@ -397,7 +397,9 @@ def sparse_leg(gbc, nseg=2, dlt_log2=26):
         r = sp.verify(a, a + span - 2)
     gpu_ms = r.ms_sieve + r.ms_large + r.ms_check
     return {"metric": "sparse cross-check evens verified per second", "value": r.evens / gpu_ms / 1e6,
-            "unit": "G evens/s", "e2e": {"value": r.evens / r.ms_total / 1e6, "unit": "G evens/s"},
+            "unit": "G evens/s",
+            "e2e": {"value": r.evens / r.ms_total / 1e6, "unit": "G evens/s", "h2d_bytes_per_step": 16,
+                    "d2h_bytes_per_step": 32 * r.segments + 16 * r.pending},
             "evens": r.evens, "segments": r.segments, "pending": r.pending, "map_primes": r.map_primes,
             "entries_per_warp_task": r.groups / (r.evens / 4096), "init_s": init_s,
             "stage_ms": {"sieve": r.ms_sieve, "large": r.ms_large, "check": r.ms_check, "wall": r.ms_total},

@@ -457,7 +457,7 @@ int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_t *d_primes
  * Valid for start - M (TB + 1) > sqrt(limit) and start > pmax (the map's q
  * above every sieving prime); lower starts are GBC_E_ARG ("use the dense
  * path"). */
-typedef struct gbc_sparse gbc_sparse;
+typedef struct gbc_sparse gbc_sparse;   /* one call at a time per context */
 
 typedef struct gbc_sparse_config {
     uint64_t limit;     /* largest even any call verifies (sizes the sieving primes) */
