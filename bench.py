@@ -592,6 +592,12 @@ def run_gb300(args, rep):
     inv_sum = float((1.0 / np.nonzero(flags_[71:])[0].__add__(71)).sum())
     smem_atomics = {"tile": 8 * W / 30 * inv_sum + marks, "large": 3 * marks, "check": 0.0, "count": W / L}
     counters = ncu_counters()
+    # the shared-memory atomic roof: the device's conflict-free atomicAnd
+    # throughput, measured after the timed region
+    try:
+        smem_peak, smem_peak_clk = gbc.smem_atomic_peak()
+    except Exception:
+        smem_peak, smem_peak_clk = None, None
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = cst.sm_count * 4 * sm_mhz * 1e6                    # warp instructions per second
     stage_bw = {}
@@ -603,7 +609,8 @@ def run_gb300(args, rep):
                "smem_atomics_per_launch": smem_atomics[s_],
                "smem_atomic_rate_g_per_s": smem_atomics[s_] / (ms / 1e3) / 1e9 if ms > 0 else None,
                "smem_atomics_per_clock_per_sm": smem_atomics[s_] / (ms / 1e3) / (cst.sm_count * sm_mhz * 1e6)
-               if ms > 0 else None}
+               if ms > 0 else None,
+               "frac_smem_atomic": smem_atomics[s_] / (ms / 1e3) / smem_peak if ms > 0 and smem_peak else None}
         have = [counters[k] for k in kerns if k in counters]
         if have:
             row["ncu_dram_bytes_per_launch"] = sum(c[0] for c in have)
@@ -645,7 +652,11 @@ def run_gb300(args, rep):
                      "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic, "peak_kind": kind,
                      "alg_bytes_per_launch": stage_bw[dom]["alg_bytes_per_launch"],
                      "ms_per_launch": stage_bw[dom]["ms_per_launch"],
-                     "issue_peak_warp_inst_per_s": issue_peak, "stages": stage_bw},
+                     "issue_peak_warp_inst_per_s": issue_peak,
+                     "smem_atomic_peak": {"per_s": smem_peak, "per_clock_per_sm": smem_peak_clk,
+                                          "pattern": "conflict-free 32-bit atomicAnd, 1024 threads per SM "
+                                                     "(gbc_smem_atomic_peak)"},
+                     "stages": stage_bw},
         "clocks": clk.summary(),
     }
     if rep.world > 1:

@@ -156,6 +156,7 @@ SIGNATURES = {
     "gbc_sparse_map": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint64]),
     "gbc_sparse_witness": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
     "gbc_sparse_plan": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int]),
+    "gbc_smem_atomic_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -497,3 +498,14 @@ class Sparse:
         g = (C.c_uint32 * max(1, n))()
         self.lib.gbc_sparse_plan(self.h, r, p, g, n)
         return list(zip(p[:n], g[:n]))
+
+
+def smem_atomic_peak(device=0):
+    """(atomics per second, atomics per SM clock): the device's
+    conflict-free shared-memory atomicAnd throughput."""
+    lib = load()
+    a, b = C.c_double(), C.c_double()
+    rc = lib.gbc_smem_atomic_peak(device, C.byref(a), C.byref(b))
+    if rc:
+        raise GbcError(rc, "shared-memory atomic probe")
+    return a.value, b.value

@@ -526,6 +526,14 @@ int gbc_sparse_witness(gbc_sparse *sp, uint64_t start, uint32_t count, uint32_t 
  * how many there are, writing at most cap. */
 int gbc_sparse_plan(const gbc_sparse *sp, uint32_t r, uint32_t *p_out, uint32_t *group_out, int cap);
 
+/* ---- measurement -------------------------------------------------------------
+ * No counterpart in the reference: the shared-memory atomic roof the sieve
+ * stages are reported against. Conflict-free 32-bit atomicAnd throughput of
+ * the device (one CTA of 1024 threads per SM, the tile sieve's shape, every
+ * warp instruction on 32 banks): atomics per second over an event-timed launch and atomics per SM
+ * clock; either pointer may be NULL. GBC_E_CUDA without a device. */
+int gbc_smem_atomic_peak(int device, double *atomics_per_s, double *per_clock_per_sm);
+
 #ifdef __cplusplus
 }
 #endif

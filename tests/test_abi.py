@@ -100,3 +100,11 @@ def test_cli_usage_errors():
                        capture_output=True, text=True)
     assert r.returncode == 1 and "supported maximum" in r.stderr and "PASS" not in r.stdout
     assert subprocess.run([exe, "--limit", "1e12", "--sparse", "--stats"], capture_output=True).returncode == 2
+
+
+def test_smem_atomic_probe_fails_loudly_without_a_gpu(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(gbc.GbcError):
+        gbc.smem_atomic_peak()

@@ -128,3 +128,4 @@ def test_cli_sparse_run():
     kv = dict(x.split("=", 1) for x in r.stdout.strip().split(","))
     assert kv["result"] == "PASS" and kv["path"] == "sparse"
     assert int(kv["evens"]) == 10**9 + 1 and int(kv["start"]) == 4 * 10**18
+
