@@ -408,7 +408,10 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
     ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());
     const uint32_t tb = 1u << cfg.tile_log2;
-    ctx->i_warp = uint32_t(std::lower_bound(pr.begin(), pr.end(), std::max(tb / 64, 72u)) - pr.begin());
+    // primes with at least 128 marks per tile: a warp per prime; above, a
+    // thread per prime (measured on 128-segment batches at 4e18 with 2^20-bit
+    // tiles: tb / 64 13.37 ms, tb / 128 13.03, tb / 256 13.55 per tile stage)
+    ctx->i_warp = uint32_t(std::lower_bound(pr.begin(), pr.end(), std::max(tb / 128, 72u)) - pr.begin());
     if (ctx->i_warp > ctx->n_mid) ctx->i_warp = ctx->n_mid;
     std::vector<uint32_t> magic(ctx->n_mid);
     for (uint32_t i = 0; i < ctx->n_mid; ++i) magic[i] = uint32_t((1ull << 32) / pr[i]);
