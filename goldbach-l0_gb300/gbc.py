@@ -5,7 +5,10 @@ not load it. `load()` loads it and raises if it is missing (there is no CPU
 fallback). `Context` wraps one gbc_ctx: the per-segment contract
 (enqueue_batch / enqueue_segments / collect, the reference's
 enqueue/collect_slot, src/verifier.cpp:1741-2444) and the whole-range call
-verify_range (gb::run_gpu, include/verifier.hpp:71-110).
+verify_range (gb::run_gpu, include/verifier.hpp:71-110). `Sparse` wraps the
+sparse class map cross-check (gbc_sparse_*, the reference's --sparse path)
+and `smem_atomic_peak` the shared-memory atomic probe the bench reports the
+sieve stages against.
 """
 import ctypes as C
 import os

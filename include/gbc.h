@@ -1,5 +1,6 @@
 /*
- * gbc.h -- C ABI of the GB300 dense Goldbach verify path.
+ * gbc.h -- C ABI of the GB300 dense Goldbach verify path (and, at the end,
+ * the sparse class map cross-check and the shared-memory atomic probe).
  *
  * The reference (goldbach-l0) has no FFI: its boundary for this path is the
  * dense run driver's per-segment contract (src/verifier.cpp:1741-2444:
