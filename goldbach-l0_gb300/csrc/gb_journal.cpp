@@ -19,6 +19,7 @@
 #include <cstring>
 #include <ctime>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <sstream>
 #include <string>
@@ -92,19 +93,14 @@ uint64_t journal_resume(const std::string &path, uint64_t start)
     return next;
 }
 
-// Runs [start, limit] in journaled slices on ctx. Returns the number of
-// slices verified now; *stopped = 1 when the stop file ended the run early.
-// Throws GbcError when a slice fails twice (the journal then holds its RETRY
-// row and the resume point is that slice).
-uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
-                    const std::string &release, const char *stop_file, FILE *log, int *stopped)
+namespace {
+
+// The journaled slice loop over [start, limit]: verify(a, b) verifies one
+// slice and returns its csv line, or throws GbcError.
+uint64_t journal_loop(uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
+                      const std::string &release, const char *stop_file, FILE *log, int *stopped,
+                      const std::function<std::string(uint64_t, uint64_t)> &verify)
 {
-    if (slice < 4 || (slice & 1)) throw GbcError(GBC_E_ARG, "slice must be even and at least 4");
-    if (start & 1) ++start;
-    limit &= ~uint64_t(1);
-    gbc_config cfg{};
-    if (gbc_get_config(ctx, &cfg) != GBC_OK) throw GbcError(GBC_E_ARG, "no context");
-    if (limit > cfg.limit) throw GbcError(GBC_E_ARG, "limit above the context's limit");
     if (stopped) *stopped = 0;
     uint64_t next = journal_resume(journal, start), done = 0;
     if (log)
@@ -118,12 +114,12 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
             return done;
         }
         const uint64_t a = next, b = limit - a < slice - 2 ? limit : a + slice - 2;
-        RunStats st;
+        std::string csv;
         int attempts = 0;
         for (;;) {
             ++attempts;
             try {
-                st = run_range(ctx, a, b, cfg.segment_even, cfg.max_batch, nullptr, nullptr, cfg.sample_every);
+                csv = verify(a, b);
                 break;
             } catch (const GbcError &e) {
                 if (attempts == 1)
@@ -139,8 +135,8 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
         }
         {
             std::ofstream out(journal, std::ios::app);
-            out << "PASS " << a << ' ' << b << ' ' << utc_now() << ' ' << csv_line(st, cfg.segment_even)
-                << " release=" << release << (attempts == 2 ? " attempts=2" : "") << '\n';
+            out << "PASS " << a << ' ' << b << ' ' << utc_now() << ' ' << csv << " release=" << release
+                << (attempts == 2 ? " attempts=2" : "") << '\n';
             if (!out) throw GbcError(GBC_E_ARG, "cannot append to the journal " + journal);
         }
         ++done;
@@ -154,6 +150,70 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
     }
     if (log) std::fprintf(log, "%s COMPLETE [%" PRIu64 ", %" PRIu64 "]\n", utc_now().c_str(), start, limit);
     return done;
+}
+
+}  // namespace
+
+// Runs [start, limit] in journaled slices on ctx. Returns the number of
+// slices verified now; *stopped = 1 when the stop file ended the run early.
+// Throws GbcError when a slice fails twice (the journal then holds its RETRY
+// row and the resume point is that slice).
+uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
+                    const std::string &release, const char *stop_file, FILE *log, int *stopped)
+{
+    if (slice < 4 || (slice & 1)) throw GbcError(GBC_E_ARG, "slice must be even and at least 4");
+    if (start & 1) ++start;
+    limit &= ~uint64_t(1);
+    gbc_config cfg{};
+    if (gbc_get_config(ctx, &cfg) != GBC_OK) throw GbcError(GBC_E_ARG, "no context");
+    if (limit > cfg.limit) throw GbcError(GBC_E_ARG, "limit above the context's limit");
+    return journal_loop(start, limit, slice, journal, release, stop_file, log, stopped, [&](uint64_t a, uint64_t b) {
+        const RunStats st = run_range(ctx, a, b, cfg.segment_even, cfg.max_batch, nullptr, nullptr, cfg.sample_every);
+        return csv_line(st, cfg.segment_even);
+    });
+}
+
+// The sparse cross-check's csv line (the keys it shares with the dense
+// line; path=sparse, no statistics).
+std::string sparse_csv_line(const RunStats &st)
+{
+    const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
+    char b[512];
+    std::snprintf(b, sizeof b,
+                  "version=gb300-1.0 path=sparse limit=%" PRIu64 " start=%" PRIu64 " segments=%" PRIu64
+                  " leftovers=%" PRIu64 " result=PASS gpu_s=%.4f total_s=%.4f sieve_s=%.4f large_s=%.4f check_s=%.4f"
+                  " evens_per_sec=%.6g stats=0",
+                  st.limit, st.start, st.segments, st.leftovers, st.gpu_seconds, st.wall_seconds, st.tile_ms / 1e3,
+                  st.large_ms / 1e3, st.check_ms / 1e3, eps);
+    return b;
+}
+
+// The sparse cross-check of [start, limit] in journaled slices on sp
+// (ci/sparse_crosscheck.sh run: run_range with GB_SPARSE=1 and its own
+// journal): the same rows, resume rule and stop file as run_slices.
+uint64_t run_sparse_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
+                           const std::string &release, const char *stop_file, FILE *log, int *stopped)
+{
+    if (slice < 4 || (slice & 1)) throw GbcError(GBC_E_ARG, "slice must be even and at least 4");
+    if (start & 1) ++start;
+    limit &= ~uint64_t(1);
+    return journal_loop(start, limit, slice, journal, release, stop_file, log, stopped, [&](uint64_t a, uint64_t b) {
+        gbc_sparse_result r{};
+        const int rc = gbc_sparse_verify(sp, a, b, &r);
+        if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_sparse_verify: ") + gbc_sparse_last_error(sp));
+        RunStats st;
+        st.start = a;
+        st.limit = b;
+        st.evens = r.evens;
+        st.segments = r.segments;
+        st.leftovers = r.pending;
+        st.gpu_seconds = (r.ms_sieve + r.ms_large + r.ms_check) / 1e3;
+        st.wall_seconds = r.ms_total / 1e3;
+        st.tile_ms = r.ms_sieve;
+        st.large_ms = r.ms_large;
+        st.check_ms = r.ms_check;
+        return sparse_csv_line(st);
+    });
 }
 
 }  // namespace gb
@@ -179,6 +239,23 @@ extern "C" int gbc_run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint
         return e.code;
     } catch (const std::exception &e) {
         gbh_set_error(ctx, e.what());
+        return GBC_E_DEVICE;
+    }
+}
+
+extern "C" int gbc_sparse_run_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64_t slice,
+                                     const char *journal, const char *release, const char *stop_file,
+                                     uint64_t *slices_done, int *stopped)
+{
+    if (!sp || !journal) return GBC_E_ARG;
+    try {
+        const uint64_t n = gb::run_sparse_slices(sp, start, limit, slice, journal, release ? release : "gb300-1.0",
+                                                 stop_file, nullptr, stopped);
+        if (slices_done) *slices_done = n;
+        return GBC_OK;
+    } catch (const gb::GbcError &e) {
+        return e.code;
+    } catch (const std::exception &) {
         return GBC_E_DEVICE;
     }
 }

@@ -106,6 +106,9 @@ int usage()
                  "[--stats] [--verbose]\n"
                  "       goldbach_gb300 --start N --limit N --sparse [--csv] [--verbose]   (the sparse class map "
                  "cross-check; start well above sqrt(limit))\n"
+                 "       goldbach_gb300 --start N --limit N --sparse --slice N --journal FILE [--release ID] "
+                 "[--stop-file F]   (journaled cross-check)\n"
+                 "       goldbach_gb300 --start N --limit N --crosscheck-status DENSE_JOURNAL SPARSE_JOURNAL\n"
                  "       goldbach_gb300 --start N --limit N --slice N --journal FILE [--release ID] [--stop-file F]\n"
                  "                      [--segment N] [--batch N] [--stats-sample N]   (journaled slices; exit 3 "
                  "on the stop file)\n");
@@ -118,7 +121,7 @@ int main(int argc, char **argv)
 {
     uint64_t start = 4, limit = 0, segment = GBC_DEFAULT_SEGMENT, batch = 8, sample = 1, slice = 0;
     bool csv = false, stats = false, verbose = false, sparse = false;
-    std::string journal, release = "gb300-1.0", stop_file;
+    std::string journal, release = "gb300-1.0", stop_file, status_dense, status_sparse;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto val = [&](uint64_t &dst) {
@@ -145,7 +148,11 @@ int main(int argc, char **argv)
         else if (a == "--stats") stats = true;
         else if (a == "--verbose") verbose = true;
         else if (a == "--sparse") sparse = true;
-        else return usage();
+        else if (a == "--crosscheck-status") {
+            if (i + 2 >= argc) return usage();
+            status_dense = argv[++i];
+            status_sparse = argv[++i];
+        } else return usage();
     }
     if (!limit) return usage();
     if (start > limit) {
@@ -157,8 +164,47 @@ int main(int argc, char **argv)
         return 1;
     }
     if ((slice != 0) != !journal.empty()) return usage();
+    if (!status_dense.empty()) {
+        // ci/sparse_crosscheck.sh status: the contiguous coverage of both
+        // journals from start and the evens both have verified
+        start += start & 1;
+        const uint64_t d = gb::journal_resume(status_dense, start) - 2, s = gb::journal_resume(status_sparse, start) - 2;
+        const uint64_t both = d < s ? d : s;
+        std::printf("dense  (%s): verified [%" PRIu64 ", %" PRIu64 "]\n", status_dense.c_str(), start, d);
+        std::printf("sparse (%s): verified [%" PRIu64 ", %" PRIu64 "]\n", status_sparse.c_str(), start, s);
+        if (both + 2 > start)
+            std::printf("both:   [%" PRIu64 ", %" PRIu64 "] = %" PRIu64 " evens, %.3f%% of [%" PRIu64 ", %" PRIu64 "]\n",
+                        start, both, (both - start) / 2 + 1, 100.0 * double(both - start + 2) / double(limit - start + 2),
+                        start, limit);
+        else
+            std::printf("both:   nothing yet\n");
+        return 0;
+    }
     if (sparse) {
-        if (slice || stats) return usage();
+        if (stats) return usage();
+        if (slice) {
+            gbc_sparse_config scfg{};
+            scfg.limit = limit & ~uint64_t(1);
+            gbc_sparse *sp = nullptr;
+            int rc = gbc_sparse_create(&scfg, &sp);
+            if (rc != GBC_OK) {
+                std::fprintf(stderr, "FAIL: gbc_sparse_create: %s\n", gbc_sparse_last_error(sp));
+                gbc_sparse_destroy(sp);
+                return rc == GBC_E_ARG ? 2 : 1;
+            }
+            int code = 0;
+            try {
+                int stopped = 0;
+                gb::run_sparse_slices(sp, start, limit, slice, journal, release,
+                                      stop_file.empty() ? nullptr : stop_file.c_str(), stdout, &stopped);
+                code = stopped ? 3 : 0;
+            } catch (const gb::GbcError &e) {
+                std::fprintf(stderr, "FAIL: %s\n", e.what());
+                code = e.code == GBC_E_ARG ? 2 : 1;
+            }
+            gbc_sparse_destroy(sp);
+            return code;
+        }
         try {
             const gb::RunStats st = gb::run_gpu_sparse(limit, verbose, start);
             const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;

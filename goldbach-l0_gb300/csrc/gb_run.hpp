@@ -177,4 +177,11 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t s
 // stage times. No statistics. Throws GbcError.
 RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
 
+// The sparse cross-check in journaled slices (ci/sparse_crosscheck.sh run):
+// run_slices' rows, resume rule and stop file, each slice through
+// gbc_sparse_verify; its csv line carries path=sparse and no statistics.
+uint64_t run_sparse_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
+                           const std::string &release, const char *stop_file, FILE *log, int *stopped);
+std::string sparse_csv_line(const RunStats &st);
+
 }  // namespace gb

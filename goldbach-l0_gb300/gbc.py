@@ -160,6 +160,8 @@ SIGNATURES = {
     "gbc_sparse_witness": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
     "gbc_sparse_plan": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int]),
     "gbc_smem_atomic_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gbc_sparse_run_slices": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_char_p, C.c_char_p,
+                                        C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
 }
 
 _lib = None
@@ -491,6 +493,14 @@ class Sparse:
         buf = (C.c_uint32 * count)()
         self._check(self.lib.gbc_sparse_witness(self.h, start, count, buf))
         return list(buf)
+
+    def run_slices(self, start, limit, slice_, journal, release="gb300-1.0", stop_file=None):
+        """The cross-check in journaled slices: (slices verified now, stopped)."""
+        done, stopped = C.c_uint64(), C.c_int()
+        self._check(self.lib.gbc_sparse_run_slices(self.h, start, limit, slice_, str(journal).encode(),
+                                                   release.encode(), str(stop_file).encode() if stop_file else None,
+                                                   C.byref(done), C.byref(stopped)))
+        return done.value, bool(stopped.value)
 
     def plan(self, r):
         """Even class r's candidates in plan order: [(p, entry index)]."""

@@ -522,6 +522,15 @@ int gbc_sparse_map(gbc_sparse *sp, uint64_t n0, uint32_t dl, uint32_t *out, uint
  * within the first group_cap entries; 0 = none. */
 int gbc_sparse_witness(gbc_sparse *sp, uint64_t start, uint32_t count, uint32_t *p_out);
 
+/* The cross-check in journaled slices (ci/sparse_crosscheck.sh run: the
+ * reference's run_range with GB_SPARSE=1 and its own journal): the rows,
+ * resume rule, retry and stop file of gbc_run_slices, each row's csv part
+ * "version=gb300-1.0 path=sparse limit= start= segments= leftovers=
+ * result=PASS ... stats=0". Coverage of both journals from a start is
+ * gbc_journal_resume on each (ci/sparse_crosscheck.sh status). */
+int gbc_sparse_run_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64_t slice, const char *journal,
+                          const char *release, const char *stop_file, uint64_t *slices_done, int *stopped);
+
 /* Even class r's (r even, < M) candidates p in plan order (entries in
  * order, within an entry ascending offset) with their entry index; returns
  * how many there are, writing at most cap. */

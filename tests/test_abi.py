@@ -108,3 +108,19 @@ def test_smem_atomic_probe_fails_loudly_without_a_gpu(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(gbc.GbcError):
         gbc.smem_atomic_peak()
+
+
+def test_cli_crosscheck_status(tmp_path):
+    # ci/sparse_crosscheck.sh status: both journals' PASS chains from start
+    exe = os.path.join(ROOT, "goldbach-l0_gb300", "bin", "goldbach_gb300")
+    if not os.path.exists(exe):
+        pytest.skip("CLI not built")
+    d, s = tmp_path / "dense.journal", tmp_path / "sparse.journal"
+    d.write_text("PASS 1000 1998 t version=x\nPASS 2000 2998 t version=x\n")
+    s.write_text("PASS 1000 1998 t version=x path=sparse\nRETRY 2000 2998 t reason=-3\n")
+    r = subprocess.run([exe, "--start", "1000", "--limit", "9998", "--crosscheck-status", str(d), str(s)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0
+    lines = r.stdout.splitlines()
+    assert lines[0].endswith("verified [1000, 2998]") and lines[1].endswith("verified [1000, 1998]")
+    assert lines[2].startswith("both:   [1000, 1998] = 500 evens")

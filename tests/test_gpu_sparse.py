@@ -129,3 +129,26 @@ def test_cli_sparse_run():
     assert kv["result"] == "PASS" and kv["path"] == "sparse"
     assert int(kv["evens"]) == 10**9 + 1 and int(kv["start"]) == 4 * 10**18
 
+
+
+def test_sparse_journaled_slices(tmp_path, sp4e18):
+    # ci/sparse_crosscheck.sh run: the dense runner's rows, resume and stop file
+    sp = sp4e18
+    j = tmp_path / "range-sparse.journal"
+    a = 4 * 10**18 + 10**10
+    b = a + 3 * 10**9 - 2
+    assert sp.run_slices(a, b, 10**9, j) == (3, False)
+    rows = j.read_text().splitlines()
+    assert len(rows) == 3
+    for row, lo in zip(rows, (a, a + 10**9, a + 2 * 10**9)):
+        t = row.split()
+        kv = dict(x.split("=", 1) for x in t[4:] if "=" in x)
+        assert t[0] == "PASS" and int(t[1]) == lo and int(t[2]) == lo + 10**9 - 2
+        assert kv["path"] == "sparse" and kv["result"] == "PASS" and kv["release"] == "gb300-1.0"
+        assert int(kv["start"]) == lo and int(kv["limit"]) == lo + 10**9 - 2
+    assert gbc.journal_resume(j, a) == b + 2
+    assert sp.run_slices(a, b, 10**9, j) == (0, False)       # resumed past the chain
+    stop = tmp_path / "STOP"
+    stop.write_text("")
+    assert sp.run_slices(a, b + 10**9, 10**9, j, stop_file=stop) == (0, True)
+    assert len(j.read_text().splitlines()) == 3
