@@ -129,3 +129,24 @@ def test_device_context_fails_loudly_without_a_gpu():
     with pytest.raises(gbc.GbcError) as e:
         gbc.Sparse(limit=10**13)
     assert e.value.code == -2
+
+
+def test_oracle_sieve_matches_miller_rabin(plan_ctx):
+    # the oracle's progression sieve against primality by Miller-Rabin: every
+    # bit at 1e12, a random sample at 1e15 (where both sieve stages' prime
+    # ranges occur)
+    sp = plan_ctx
+    n0 = 10**12 - 10**12 % sp.M + 3 * sp.M
+    a = so.class_map(n0, 2000, sp.tb, sp.residues)
+    b = so.map_by_mr(n0, 2000, sp.tb, sp.residues)
+    assert all((x == y).all() for x, y in zip(a, b))
+    assert sum(int(x.sum()) for x in a) > 1000
+    n0 = 10**15 - 10**15 % sp.M
+    rows = so.class_map(n0, 50_000, sp.tb, sp.residues)
+    rnd = random.Random(11)
+    Q = n0 - sp.M * sp.tb
+    import oracle
+    for _ in range(4000):
+        k = rnd.randrange(sp.K)
+        t = rnd.randrange(len(rows[k]))
+        assert bool(rows[k][t]) == oracle.is_prime(Q + sp.residues[k] + sp.M * t), (k, t)
