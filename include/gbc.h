@@ -156,7 +156,9 @@ typedef struct gbc_batch_times {
  * sqrt(cfg->limit + 3), the pattern and wheel tables, and two slots.
  * Replaces DenseRun's construction (src/verifier.cpp:346-354) and
  * RunSetup::load_base_primes / upload_tables (src/verifier.cpp:633-692,
- * 1361-1440). Returns GBC_OK and *out, or an error (then *out = NULL). */
+ * 1361-1440). Returns GBC_OK and *out, or an error: then *out is NULL, or,
+ * for a failure past the argument checks (a CUDA call), a context that
+ * holds the error text for gbc_last_error and must be destroyed. */
 int gbc_create(const gbc_config *cfg, gbc_ctx **out);
 
 /* Frees every device and host buffer of the context (release_device_objects,
@@ -489,7 +491,8 @@ typedef struct gbc_sparse_result {
  * group stored as plan entries of up to six offsets in ascending order;
  * every candidate is decoded back to p and proved prime, <= pmax and in a
  * usable class before the plan is uploaded (the reference's
- * validate_plan_scm). */
+ * validate_plan_scm). On an error *out holds a context with the error text
+ * for gbc_sparse_last_error (destroy it), or NULL when cfg or out is NULL. */
 int gbc_sparse_create(const gbc_sparse_config *cfg, gbc_sparse **out);
 void gbc_sparse_destroy(gbc_sparse *sp);
 const char *gbc_sparse_last_error(const gbc_sparse *sp);
