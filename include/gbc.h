@@ -156,9 +156,9 @@ typedef struct gbc_batch_times {
  * sqrt(cfg->limit + 3), the pattern and wheel tables, and two slots.
  * Replaces DenseRun's construction (src/verifier.cpp:346-354) and
  * RunSetup::load_base_primes / upload_tables (src/verifier.cpp:633-692,
- * 1361-1440). Returns GBC_OK and *out, or an error: then *out is NULL, or,
- * for a failure past the argument checks (a CUDA call), a context that
- * holds the error text for gbc_last_error and must be destroyed. */
+ * 1361-1440). Returns GBC_OK and *out, or an error: *out is then a
+ * context holding the error text for gbc_last_error, which the caller
+ * destroys (NULL only when out is NULL or no context could be allocated). */
 int gbc_create(const gbc_config *cfg, gbc_ctx **out);
 
 /* Frees every device and host buffer of the context (release_device_objects,
