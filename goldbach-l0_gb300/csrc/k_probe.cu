@@ -8,9 +8,6 @@
 // event-timed launch and atomics per SM clock (clock64 of CTA 0).
 #include <cuda_runtime.h>
 
-#include <algorithm>
-#include <string>
-
 #include "../../include/gbc.h"
 
 namespace {
