@@ -3,12 +3,13 @@
 
 Headline workload: production segments of 467.5M integers at 4e18 + k *
 467.5e6, k drawn from seed 1 in [0, 1e5) (the reference's production
-segment shape). A step is one batch of --batch consecutive segments
-(default 16: one sieve pass over one HBM-resident class map of 250 MB,
-then per segment the checker, prime / twin / gap statistics and the
-class-map hash), replayed as the slot's captured CUDA graph. Successive
-steps take successive batches, so no step repeats work, and a step's map
-and sieving primes (393 MB) exceed L2.
+segment shape). A step is one batch of consecutive segments (128, the
+committed autotuner record's choice; --batch with --tuning none): one sieve
+pass over one HBM-resident class map of 2.0 GB, then per segment the
+checker, prime / twin / gap statistics and the class-map hash, replayed as
+the slot's captured CUDA graph. Successive steps take successive batches,
+so no step repeats work, and a step's map and sieving primes (393 MB)
+exceed L2.
 
 Statistics mode (--sample-every, default 256): the reference's production
 mode -- every 256th segment of the run gets p(n) of every even (its
