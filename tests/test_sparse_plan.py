@@ -150,3 +150,15 @@ def test_oracle_sieve_matches_miller_rabin(plan_ctx):
         k = rnd.randrange(sp.K)
         t = rnd.randrange(len(rows[k]))
         assert bool(rows[k][t]) == oracle.is_prime(Q + sp.residues[k] + sp.M * t), (k, t)
+
+
+def test_largest_pmax_plan():
+    # pmax 2e8: window words up to 208 in the entries' 8-bit field; creation
+    # validates every entry, and a few classes are checked here in full
+    with gbc.Sparse(limit=5 * 10**18, pmax=200_000_000, host_only=True) as sp:
+        assert sp.tb == -(-200_000_000 // sp.M) + 2 and sp.tb // 32 < 256
+        isp = bytearray(sp.pmax + 1)
+        for p in so.primes_upto(sp.pmax).tolist():
+            isp[p] = 1
+        for r in (0, 30028, 2 * 7001):
+            check_plan(sp, r, isp)
