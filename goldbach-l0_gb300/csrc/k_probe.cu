@@ -1,5 +1,6 @@
-// k_probe.cu -- the shared-memory atomic roof the sieve stages are measured
-// against: conflict-free 32-bit atomicAnd throughput of this GPU.
+// k_probe.cu -- measurement only (libgbc_probe.so, include/gbc_probe.h): the
+// shared-memory atomic roof the sieve stages are measured against,
+// conflict-free 32-bit atomicAnd throughput of this GPU.
 //
 // One CTA of 1024 threads per SM, the tile sieve's shape; each thread clears
 // bits of its own word column (warp w, lane l, round i: word
@@ -9,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gbc.h"
+#include "../../include/gbc_probe.h"
 
 namespace {
 
@@ -37,9 +39,9 @@ __global__ void __launch_bounds__(kProbeThreads, 1) k_smem_atomic_probe(uint32_t
     }
 }
 
-}  // namespace
-
-extern "C" int gbc_smem_atomic_peak(int device, double *atomics_per_s, double *per_clock_per_sm)
+// the probe on one device; the caller's current device is restored by
+// gbc_smem_atomic_peak
+int probe(int device, double *atomics_per_s, double *per_clock_per_sm)
 {
     if (cudaSetDevice(device) != cudaSuccess) return GBC_E_CUDA;
     cudaDeviceProp prop{};
@@ -50,34 +52,44 @@ extern "C" int gbc_smem_atomic_peak(int device, double *atomics_per_s, double *p
         return GBC_E_CUDA;
     uint32_t *sink = nullptr;
     long long *cyc = nullptr;
-    if (cudaMalloc(&sink, size_t(sms) * 4) != cudaSuccess) return GBC_E_CUDA;
-    if (cudaMalloc(&cyc, sizeof(long long)) != cudaSuccess) {
-        cudaFree(sink);
-        return GBC_E_CUDA;
-    }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = GBC_OK;
+    if (cudaMalloc(&sink, size_t(sms) * 4) != cudaSuccess || cudaMalloc(&cyc, sizeof(long long)) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        rc = GBC_E_CUDA;
     const uint32_t iters = 1u << 14;
-    k_smem_atomic_probe<<<sms, kProbeThreads, smem>>>(64, sink, cyc);  // warm-up
-    cudaEventRecord(e0);
-    k_smem_atomic_probe<<<sms, kProbeThreads, smem>>>(iters, sink, cyc);
-    cudaEventRecord(e1);
-    int rc = cudaEventSynchronize(e1) == cudaSuccess && cudaGetLastError() == cudaSuccess ? GBC_OK : GBC_E_CUDA;
     float ms = 0;
     long long cycles = 0;
     if (!rc) {
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (cudaMemcpy(&cycles, cyc, sizeof cycles, cudaMemcpyDeviceToHost) != cudaSuccess) rc = GBC_E_CUDA;
+        k_smem_atomic_probe<<<sms, kProbeThreads, smem>>>(64, sink, cyc);  // warm-up
+        if (cudaEventRecord(e0) != cudaSuccess) rc = GBC_E_CUDA;
+    }
+    if (!rc) {
+        k_smem_atomic_probe<<<sms, kProbeThreads, smem>>>(iters, sink, cyc);
+        if (cudaEventRecord(e1) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaGetLastError() != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess ||
+            cudaMemcpy(&cycles, cyc, sizeof cycles, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = GBC_E_CUDA;
     }
     const double total = double(iters) * kProbeThreads * sms;
     if (!rc && ms > 0 && cycles > 0) {
         if (atomics_per_s) *atomics_per_s = total / (ms * 1e-3);
         if (per_clock_per_sm) *per_clock_per_sm = double(iters) * kProbeThreads / double(cycles);
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     cudaFree(sink);
     cudaFree(cyc);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int gbc_smem_atomic_peak(int device, double *atomics_per_s, double *per_clock_per_sm)
+{
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess) return GBC_E_CUDA;
+    const int rc = probe(device, atomics_per_s, per_clock_per_sm);
+    if (cudaSetDevice(prev) != cudaSuccess) return GBC_E_CUDA;
     return rc;
 }

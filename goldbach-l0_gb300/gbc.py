@@ -6,15 +6,17 @@ fallback). `Context` wraps one gbc_ctx: the per-segment contract
 (enqueue_batch / enqueue_segments / collect, the reference's
 enqueue/collect_slot, src/verifier.cpp:1741-2444) and the whole-range call
 verify_range (gb::run_gpu, include/verifier.hpp:71-110). `Sparse` wraps the
-sparse class map cross-check (gbc_sparse_*, the reference's --sparse path)
-and `smem_atomic_peak` the shared-memory atomic probe the bench reports the
-sieve stages against.
+sparse class map cross-check (gbc_sparse_*, the reference's --sparse path).
+`smem_atomic_peak` calls the measurement library libgbc_probe.so (not part of
+the verify path): the shared-memory atomic roof the bench reports the sieve
+stages against.
 """
 import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgbc.so")
+PROBE_PATH = os.path.join(HERE, "libgbc_probe.so")
 
 NCAND = 1205
 NCLASS = 15
@@ -159,7 +161,6 @@ SIGNATURES = {
     "gbc_sparse_map": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint64]),
     "gbc_sparse_witness": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
     "gbc_sparse_plan": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int]),
-    "gbc_smem_atomic_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbc_sparse_run_slices": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_char_p, C.c_char_p,
                                         C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
 }
@@ -513,10 +514,26 @@ class Sparse:
         return list(zip(p[:n], g[:n]))
 
 
+_probe = None
+
+
+def load_probe():
+    """The measurement library (include/gbc_probe.h); raises if it is missing."""
+    global _probe
+    if _probe is None:
+        if not os.path.exists(PROBE_PATH):
+            raise OSError(f"{PROBE_PATH} is missing: build it with `make -C goldbach-l0_gb300`")
+        L = C.CDLL(PROBE_PATH)
+        L.gbc_smem_atomic_peak.restype = C.c_int
+        L.gbc_smem_atomic_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _probe = L
+    return _probe
+
+
 def smem_atomic_peak(device=0):
     """(atomics per second, atomics per SM clock): the device's
     conflict-free shared-memory atomicAnd throughput."""
-    lib = load()
+    lib = load_probe()
     a, b = C.c_double(), C.c_double()
     rc = lib.gbc_smem_atomic_peak(device, C.byref(a), C.byref(b))
     if rc:

@@ -1,6 +1,7 @@
 /*
  * gbc.h -- C ABI of the GB300 dense Goldbach verify path (and, at the end,
- * the sparse class map cross-check and the shared-memory atomic probe).
+ * the sparse class map cross-check). The measurement probe the bench reports
+ * the sieve stages against is a separate library (include/gbc_probe.h).
  *
  * The reference (goldbach-l0) has no FFI: its boundary for this path is the
  * dense run driver's per-segment contract (src/verifier.cpp:1741-2444:
@@ -406,35 +407,41 @@ uint64_t gbc_pn_exact(uint64_t n);
 /* ---- allocation-free class map ---------------------------------------------
  * This entry point has no counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc: code running while a CUDA stream
- * is being captured (an allocation there breaks or invalidates the capture),
- * code inside another framework's memory pool with a fixed device budget,
- * and latency-critical paths where cudaMalloc's implicit device-wide
- * synchronization is not acceptable. It needs no gbc_ctx.
+ * For callers that cannot call cudaMalloc: code inside another framework's
+ * memory pool with a fixed device budget (an allocation outside the pool is
+ * refused or breaks the pool's accounting), and latency-critical paths where
+ * cudaMalloc's implicit device-wide synchronization is not acceptable. It
+ * needs no gbc_ctx.
  *
  * Builds the exact mod-30 class map of q in [q_lo, q_hi] (the tile sieve's
  * output: bit t of class array k <-> q = base + 30 t + u_k, u = 1, 7, 11,
  * 13, 17, 19, 23, 29, class k at d_map + k * wpc) into d_map, a device
  * buffer of map_words u32 the caller owns, on the given CUDA stream (a
- * cudaStream_t; NULL = the default stream). d_primes (device, caller-owned)
- * holds the odd primes 3, 5, 7, ... ascending, nprimes of them, the last
- * one max_prime, and max_prime^2 >= q_hi. *base_out, *nblk_out and *wpc_out
- * (each may be NULL) receive the layout; the call returns them and
- * GBC_E_ARG without launching anything when map_words < 8 * wpc, so a
- * caller can size d_map first. err (may be NULL) receives a message on any
- * error.
+ * cudaStream_t; NULL = the default stream). Bits t < *nblk_out are exact;
+ * bits t >= *nblk_out (up to 32 * wpc) are zero. d_primes (device,
+ * caller-owned) holds every odd prime 3, 5, 7, ... up to max_prime,
+ * ascending (nprimes of them; a count that differs from the number of odd
+ * primes <= max_prime is rejected), and max_prime^2 >= q_hi. *base_out,
+ * *nblk_out and *wpc_out (each may be NULL) receive the layout; the call
+ * returns them and GBC_E_ARG without launching anything when map_words <
+ * 8 * wpc, so a caller can size d_map first. err (may be NULL) receives a
+ * message on any error.
  *
  * Limits: nprimes <= GBC_NOALLOC_MAX_PRIMES (131072 primes: q_hi up to
  * about 3e12) and q_hi - q_lo <= GBC_NOALLOC_MAX_SPAN (2^30); larger
- * requests are rejected with GBC_E_ARG. The sieve's scratch (pattern
- * words, a reciprocal and eight first class bits per prime: 4.5 MiB) is a
+ * requests are rejected with GBC_E_ARG before any CUDA call. The sieve's
+ * scratch (a reciprocal and eight first class bits per prime: 4.5 MiB) is a
  * fixed device array inside this library, which every GPU that loads the
- * library keeps until the process exits. The first call on a device looks
- * up that array's address and writes its constant part, so make the first
- * call on each device before any stream capture. Every call uses the same
- * array: calls whose kernels overlap on the GPU (two streams, or two
- * threads) race on it and must be ordered by the caller. This function
- * calls no cudaMalloc, cudaFree or other allocating routine. */
+ * library keeps until the process exits; the pattern words of the primes
+ * 7..67 are a constant device table of the library. Every call looks up
+ * the array's device address on the current device (cudaGetSymbolAddress);
+ * the first call on a device also loads this library's device code there,
+ * so make the first call on each device before any stream capture. Every
+ * call uses the same array and keeps nothing from the last call (each word
+ * a kernel reads is written earlier in the same call): calls whose kernels
+ * overlap on the GPU (two streams, or two threads) race on it and must be
+ * ordered by the caller. This function calls no cudaMalloc, cudaFree or
+ * other allocating routine. */
 #define GBC_NOALLOC_MAX_PRIMES 131072u
 #define GBC_NOALLOC_MAX_SPAN 1073741824ull
 int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_t *d_primes, uint32_t nprimes,
@@ -538,14 +545,6 @@ int gbc_sparse_run_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64
  * order, within an entry ascending offset) with their entry index; returns
  * how many there are, writing at most cap. */
 int gbc_sparse_plan(const gbc_sparse *sp, uint32_t r, uint32_t *p_out, uint32_t *group_out, int cap);
-
-/* ---- measurement -------------------------------------------------------------
- * No counterpart in the reference: the shared-memory atomic roof the sieve
- * stages are reported against. Conflict-free 32-bit atomicAnd throughput of
- * the device (one CTA of 1024 threads per SM, the tile sieve's shape, every
- * warp instruction on 32 banks): atomics per second over an event-timed launch and atomics per SM
- * clock; either pointer may be NULL. GBC_E_CUDA without a device. */
-int gbc_smem_atomic_peak(int device, double *atomics_per_s, double *per_clock_per_sm);
 
 #ifdef __cplusplus
 }

@@ -2,7 +2,7 @@
 """Regenerates the golden fixtures in this directory from the reference.
 
 Runs only where the goldbach-l0 source tree is present (its path is the
-first argument, default /root/reference) and after `make -C oracle ref` has
+first argument, or GB_REFERENCE) and after `make -C oracle ref REF=...` has
 compiled the reference's own CPU path into oracle/_ref/. Everything it writes
 is plain data; the tests read these files and never the reference itself.
 
@@ -71,7 +71,9 @@ def pn_list(start, count):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GB_REFERENCE", "")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py <goldbach-l0 tree> (or GB_REFERENCE=<tree>)")
     with open(os.path.join(HERE, "stats_ref_windows.txt"), "w") as f:
         for a, b in STATS_WINDOWS:
             line = run([os.path.join(REFBIN, "stats_ref"), str(a), str(b), "8"]).strip()

@@ -102,6 +102,18 @@ def test_cli_usage_errors():
     assert subprocess.run([exe, "--limit", "1e12", "--sparse", "--stats"], capture_output=True).returncode == 2
 
 
+def test_probe_library_is_separate_and_exports_its_header():
+    """The measurement probe lives in libgbc_probe.so, not in the product
+    library, and exports what include/gbc_probe.h declares."""
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gbc_probe.h")).read(), flags=re.S)
+    names = sorted(set(re.findall(r"\b(gbc_\w+)\s*\(", src)))
+    assert names == ["gbc_smem_atomic_peak"]
+    probe = gbc.load_probe()
+    assert all(hasattr(probe, n) for n in names)
+    out = subprocess.run(["nm", "-D", "--defined-only", gbc.LIB_PATH], capture_output=True, text=True).stdout
+    assert "gbc_smem_atomic_peak" not in out
+
+
 def test_smem_atomic_probe_fails_loudly_without_a_gpu(lib):
     import torch
     if torch.cuda.is_available():

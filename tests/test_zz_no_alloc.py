@@ -1,16 +1,18 @@
-"""The allocation-free class-map entry point against the existing path.
+"""The allocation-free class-map entry point (gbc_class_map_noalloc).
 
-gbc_class_map_noalloc serves callers that cannot call cudaMalloc -- code
-running while a CUDA stream is captured, code inside another framework's
-fixed memory pool, latency-critical paths that cannot take cudaMalloc's
-device-wide synchronization. It builds the class map of a q range in a
-buffer the caller owns and keeps its scratch in a fixed device array of the
-library. Here the test is that caller: it owns the primes and the map
-buffers (allocated with torch), calls the entry point twice in a row on two
-different windows, and compares each map bit for bit with the map the
-per-segment path (gbc_enqueue_batch) built for the same q range. The file is
-named so pytest collects it last: a failure here stops a -x run only after
-every other test has run.
+It serves callers that cannot call cudaMalloc: code inside another
+framework's memory pool with a fixed device budget, and latency-critical
+paths that cannot take cudaMalloc's device-wide synchronization. It builds
+the class map of a q range in a buffer the caller owns and keeps its scratch
+in a fixed device array of the library. Here the test is that caller: it owns
+the primes and the map buffers (allocated with torch), calls the entry point
+twice in a row on two different windows, and compares each map bit for bit
+with the map the per-segment path (gbc_enqueue_batch) built for the same q
+range, checks it against the oracle's hash of the primes in the range, and
+checks that every bit past the range is zero. The file is named so pytest
+collects it last: a failure here stops a -x run only after every other test
+has run. The argument checks run on the host before any CUDA call, so they
+are tested without a GPU.
 """
 import ctypes as C
 
@@ -18,8 +20,9 @@ import numpy as np
 import pytest
 
 import gbc
+import oracle
 
-pytestmark = pytest.mark.gpu
+U30 = (1, 7, 11, 13, 17, 19, 23, 29)
 
 
 def odd_primes_upto(n):
@@ -42,10 +45,31 @@ def existing_map(a, b, seg):
     return base, nblk, wpc, np.frombuffer(words, dtype=np.uint32).copy()
 
 
-def class_bits(words, wpc, nblk):
+def class_bits(words, wpc, nbits):
     w = words.reshape(8, -1)[:, :wpc]
     bits = np.unpackbits(np.ascontiguousarray(w).view(np.uint8), axis=1, bitorder="little")
-    return bits[:, :nblk]
+    return bits[:, :nbits]
+
+
+def splitmix64(q):
+    with np.errstate(over="ignore"):
+        z = q + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def map_hash(bits, base):
+    """Sum mod 2^64 of splitmix64(q) over the set bits, and their count (the
+    oracle's class-map hash, gbo_map_hash)."""
+    h, c = np.uint64(0), 0
+    for k in range(8):
+        t = np.nonzero(bits[k])[0].astype(np.uint64)
+        q = np.uint64(base) + np.uint64(30) * t + np.uint64(U30[k])
+        with np.errstate(over="ignore"):
+            h = h + np.sum(splitmix64(q), dtype=np.uint64)
+        c += len(t)
+    return int(h), c
 
 
 def noalloc_map(lib, torch, q_lo, q_hi, primes_dev, nprimes, max_prime, stream):
@@ -55,7 +79,8 @@ def noalloc_map(lib, torch, q_lo, q_hi, primes_dev, nprimes, max_prime, stream):
     rc = lib.gbc_class_map_noalloc(q_lo, q_hi, primes_dev, nprimes, max_prime, None, 0, C.byref(base),
                                    C.byref(nblk), C.byref(wpc), stream, err, len(err))
     assert rc == -1 and wpc.value > 0
-    out = torch.empty(8 * wpc.value, dtype=torch.int32, device="cuda")
+    # filled with ones first: every word past the range must come back zero
+    out = torch.full((8 * wpc.value,), -1, dtype=torch.int32, device="cuda")
     rc = lib.gbc_class_map_noalloc(q_lo, q_hi, primes_dev, nprimes, max_prime, C.c_void_p(out.data_ptr()),
                                    8 * wpc.value, C.byref(base), C.byref(nblk), C.byref(wpc), stream, err,
                                    len(err))
@@ -64,6 +89,7 @@ def noalloc_map(lib, torch, q_lo, q_hi, primes_dev, nprimes, max_prime, stream):
     return base.value, nblk.value, wpc.value, out.cpu().numpy().view(np.uint32)
 
 
+@pytest.mark.gpu
 def test_noalloc_map_matches_existing_path_twice():
     torch = pytest.importorskip("torch")
     lib = gbc.load()
@@ -78,7 +104,10 @@ def test_noalloc_map_matches_existing_path_twice():
         nb, nn, nw, got = noalloc_map(lib, torch, base, q_hi, C.c_void_p(pd.data_ptr()), len(primes),
                                       int(primes[-1]), stream)
         assert (nb, nn) == (base, nblk)
-        assert np.array_equal(class_bits(got, nw, nblk), class_bits(words, wpc, nblk))
+        mine = class_bits(got, nw, nblk)
+        assert np.array_equal(mine, class_bits(words, wpc, nblk))
+        assert map_hash(mine, base) == oracle.map_hash(base, q_hi)
+        assert not class_bits(got, nw, 32 * nw)[:, nblk:].any(), "bits past the range must be zero"
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits():
@@ -91,6 +120,11 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     rc = lib.gbc_class_map_noalloc(10**12, 10**12 + 1000, dummy, 200_000, 2_750_000, None, 0, None, None, None,
                                    None, err, len(err))
     assert rc == -1 and b"GBC_NOALLOC_MAX_PRIMES" in err.value
-    rc = lib.gbc_class_map_noalloc(10**12, 10**12 + 1000, dummy, 1000, 7919, None, 0, None, None, None, None, err,
+    # 999 odd primes end at 7919, whose square is below the range
+    rc = lib.gbc_class_map_noalloc(10**12, 10**12 + 1000, dummy, 999, 7919, None, 0, None, None, None, None, err,
                                    len(err))
     assert rc == -1 and b"sqrt" in err.value
+    # a list that does not start at 3 (or misses a prime) has the wrong count
+    rc = lib.gbc_class_map_noalloc(10**6, 10**6 + 1000, dummy, 1000, 7919, None, 0, None, None, None, None, err,
+                                   len(err))
+    assert rc == -1 and b"every odd prime from 3" in err.value
