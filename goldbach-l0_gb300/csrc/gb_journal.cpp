@@ -52,7 +52,7 @@ bool file_exists(const char *p)
 
 // The reference's --csv line for a run (src/main.cpp:191-215): key=value
 // pairs, the keys this path has in common with it.
-std::string csv_line(const RunStats &st, uint64_t segment)
+std::string csv_line(const RangeStats &st, uint64_t segment)
 {
     const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
     const uint64_t ridge_max = st.ridges.empty() ? 0 : st.ridges.front().p;
@@ -168,14 +168,14 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
     if (gbc_get_config(ctx, &cfg) != GBC_OK) throw GbcError(GBC_E_ARG, "no context");
     if (limit > cfg.limit) throw GbcError(GBC_E_ARG, "limit above the context's limit");
     return journal_loop(start, limit, slice, journal, release, stop_file, log, stopped, [&](uint64_t a, uint64_t b) {
-        const RunStats st = run_range(ctx, a, b, cfg.segment_even, cfg.max_batch, nullptr, nullptr, cfg.sample_every);
+        const RangeStats st = run_range(ctx, a, b, cfg.segment_even, cfg.max_batch, nullptr, nullptr, cfg.sample_every);
         return csv_line(st, cfg.segment_even);
     });
 }
 
 // The sparse cross-check's csv line (the keys it shares with the dense
 // line; path=sparse, no statistics).
-std::string sparse_csv_line(const RunStats &st)
+std::string sparse_csv_line(const RangeStats &st)
 {
     const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
     char b[512];
@@ -201,7 +201,7 @@ uint64_t run_sparse_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint6
         gbc_sparse_result r{};
         const int rc = gbc_sparse_verify(sp, a, b, &r);
         if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_sparse_verify: ") + gbc_sparse_last_error(sp));
-        RunStats st;
+        RangeStats st;
         st.start = a;
         st.limit = b;
         st.evens = r.evens;

@@ -206,7 +206,7 @@ int main(int argc, char **argv)
             return code;
         }
         try {
-            const gb::RunStats st = gb::run_gpu_sparse(limit, verbose, start);
+            const gb::RangeStats st = gb::run_gpu_sparse(limit, verbose, start);
             const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
             if (csv)
                 std::printf("result=PASS,path=sparse,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64
@@ -253,7 +253,7 @@ int main(int argc, char **argv)
     int code = 0;
     try {
         gbc_get_config(ctx, &cfg);
-        const gb::RunStats st = gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, nullptr, nullptr,
+        const gb::RangeStats st = gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, nullptr, nullptr,
                                               cfg.sample_every);
         if (verbose)
             std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",

@@ -25,13 +25,23 @@
 #include <string>
 #include <vector>
 
-void gbh_set_error(gbc_ctx *ctx, const char *msg);  // gbc_api.cu
+void gbh_set_error(gbc_ctx *ctx, const char *msg);                            // gbc_api.cu
+void gbh_set_stats(gbc_ctx *ctx, void *p, void (*del)(void *), bool gaps);    // gbc_api.cu
+void *gbh_stats(gbc_ctx *ctx, bool *gaps);                                    // gbc_api.cu
 
 namespace gb {
 
+StatsCampaign *campaign_of(gbc_ctx *ctx) { return static_cast<StatsCampaign *>(gbh_stats(ctx, nullptr)); }
+
+bool stats_gaps_of(gbc_ctx *ctx)
+{
+    bool g = true;
+    gbh_stats(ctx, &g);
+    return g;
+}
+
 namespace {
 
-using u128 = unsigned __int128;
 
 std::string u128_str(u128 v)
 {
@@ -73,6 +83,8 @@ RunAccumulator::RunAccumulator(uint64_t start, uint64_t limit, uint32_t tail_t)
     cand_ = candidates();
     samp_.assign(size_t(GBC_NCLASS) * GBC_NCAND, 0);
     tail_.assign(GBC_NCAND, 0);
+    tail_cls_.assign(size_t(GBC_NCLASS) * GBC_NCAND, 0);
+    tail_agg_.assign(GBC_NCAND, 0);
     first_all_.assign(GBC_NCAND, 0);
     first_tail_.assign(GBC_NCAND, 0);
     ghist_.assign(GBC_GBINS, 0);
@@ -154,7 +166,11 @@ void RunAccumulator::add_segment(const gbc_segment_result &r)
             const uint64_t c = r.hist[cr][i];
             if (!c) continue;
             if (r.sampled) samp_[size_t(cr) * GBC_NCAND + i] += c;
-            if (cand_[i] >= tail_t_) tail_[i] += c;
+            if (cand_[i] >= tail_t_) {
+                tail_[i] += c;
+                if (r.sampled) tail_cls_[size_t(cr) * GBC_NCAND + i] += c;
+                else tail_agg_[i] += c;
+            }
         }
     for (int i = 0; i < GBC_NCAND; ++i)
         if (r.first[i] != 0xFFFFFFFFu) {
@@ -164,13 +180,20 @@ void RunAccumulator::add_segment(const gbc_segment_result &r)
         }
     if (r.sampled) evens_sampled_ += r.evens;
     else pending_ += r.pending;
+    std::vector<std::pair<uint64_t, uint64_t>> left;
     for (uint32_t i = 0; i < r.nleft; ++i) {
         if (!r.left_p[i])
             throw std::runtime_error("no Goldbach partition found for n = " + std::to_string(r.left_n[i]) +
                                      " (reported, never passed)");
         add_beyond(r.left_n[i], r.left_p[i]);
+        left.push_back({r.left_n[i], r.left_p[i]});
         ++leftovers_;
     }
+    // the campaign keeps them in the order of the evens (the GPU lists them
+    // in no fixed order)
+    std::sort(left.begin(), left.end());
+    for (const auto &e : left)
+        if (e.second > GBC_MAX_CAND) beyond_list_.push_back(e);
     for (uint32_t i = 0; i < r.nridge; ++i) note_ridge(r.ridge_n[i], r.ridge_p[i]);
     static const int res[8] = {1, 7, 11, 13, 17, 19, 23, 29};
     for (int k = 0; k < 8; ++k) primes30_[res[k]] += r.primes30[k];
@@ -321,60 +344,55 @@ std::string RunAccumulator::stats_ref_line() const
 
 std::string RunAccumulator::gbstats_line(const char *version) const
 {
-    // the reference's run line without a campaign state: new_first lists the
-    // run's first occurrences of the tail bins
-    uint64_t pm = 0;
-    for (int i = 0; i < GBC_NCAND; ++i)
-        if (tail_[i]) pm = cand_[i];
-    for (auto &b : beyond_) pm = std::max(pm, b.first);
-    std::string o = "GBSTATS v2 version=" + std::string(version);
-    char b[512];
-    std::snprintf(b, sizeof b,
-                  " start=%" PRIu64 " limit=%" PRIu64 " evens=%" PRIu64 " evens_sampled=%" PRIu64 " tail_t=%u"
-                  " tail_evens=%" PRIu64 " pmax=%" PRIu64 " primes=%" PRIu64 " twins=%" PRIu64,
-                  start_, limit_, evens_, evens_sampled_, tail_t_, tail_evens(), pm, primes(), twins());
-    o += b;
+    // the reference's run line against an empty campaign: new_first lists
+    // every first occurrence of the run's tail bins
+    std::string l = gb::gbstats_line(record(true), std::vector<uint64_t>(GBC_NCAND, 0), version);
+    if (!l.empty() && l.back() == '\n') l.pop_back();
+    return l;
+}
+
+RunRecord RunAccumulator::record(bool gaps_on) const
+{
+    RunRecord r;
+    r.start = start_;
+    r.limit = limit_;
+    r.evens = evens_;
+    r.evens_sampled = evens_sampled_;
+    r.tail_t = tail_t_;
+    r.samp = samp_;
+    r.tail_cls = tail_cls_;
+    r.tail_agg = tail_agg_;
+    r.first = first_tail_;
+    r.beyond = beyond_list_;
     static const int u[8] = {1, 7, 11, 13, 17, 19, 23, 29};
-    o += " primes30=";
-    for (int i = 0; i < 8; ++i) o += (i ? "," : "") + std::to_string(primes30_[u[i]]);
-    o += " twins30=" + std::to_string(twins30_[11]) + "," + std::to_string(twins30_[17]) + "," +
-         std::to_string(twins30_[29]);
-    std::string nf;
-    for (int i = 0; i < GBC_NCAND; ++i)
-        if (cand_[i] >= tail_t_ && first_tail_[i])
-            nf += (nf.empty() ? "" : ";") + std::to_string(cand_[i]) + ":" + std::to_string(first_tail_[i]);
-    o += " new_first=" + (nf.empty() ? std::string("-") : nf);
-    std::string bey;
-    for (auto &e : beyond_)
-        bey += (bey.empty() ? "" : ";") + std::to_string(e.first) + ":" + std::to_string(e.second.second);
-    o += " beyond=" + (bey.empty() ? std::string("-") : bey);
-    // gaps: every segment is walked, so the walk totals are the run totals
-    u128 m[4] = {odd_gaps_, odd_gaps_, odd_gaps_, odd_gaps_};
-    const uint64_t n = gap_count();
-    for (size_t i = 0; i < ghist_.size(); ++i) {
-        const u128 c = ghist_[i], g = 2 * i, g2 = g * g;
-        m[0] += c * g;
-        m[1] += c * g2;
-        m[2] += c * g2 * g;
-        m[3] += c * g2 * g2;
+    for (int i = 0; i < 8; ++i) r.primes30[i] = primes30_[u[i]];
+    r.twins30[0] = twins30_[11];
+    r.twins30[1] = twins30_[17];
+    r.twins30[2] = twins30_[29];
+    r.gaps_on = gaps_on;
+    if (gaps_on) {
+        // every segment is walked: the walk totals are the run's gaps (one
+        // per prime of [start + 1, limit - 1], upper prime in that range)
+        GapTotals &g = r.gaps;
+        g.n = primes();
+        g.wn = gap_count();
+        g.wd[0] = g.wd[1] = g.wd[2] = g.wd[3] = odd_gaps_;
+        for (size_t i = 0; i < ghist_.size(); ++i) {
+            const u128 c = ghist_[i], gg = 2 * i, g2 = gg * gg;
+            g.wd[0] += c * gg;
+            g.wd[1] += c * g2;
+            g.wd[2] += c * g2 * gg;
+            g.wd[3] += c * g2 * g2;
+        }
+        g.d1 = g.wd[0];
+        g.samp = ghist_;
+        g.gmax = gmax_;
+        g.gmax_lo = gmax_lo_;
+        g.all_walked = true;
+        g.tail = tail_gaps_;
+        r.walk_evens = evens_;
     }
-    o += " gaps=" + std::to_string(n) + " gd1=" + u128_str(m[0]) + " gmax=" +
-         (gmax_ ? std::to_string(gmax_) + ":" + std::to_string(gmax_lo_) : std::string("-")) + " gtail=";
-    std::string t;
-    for (auto &e : tail_gaps_)
-        t += (t.empty() ? "" : ";") + std::to_string(e.first) + ":" + std::to_string(e.second.first) + ":" +
-             std::to_string(e.second.second);
-    o += t.empty() ? "-" : t;
-    o += " gwalk=" + std::to_string(evens_) + ":" + std::to_string(n) + " gsmom=";
-    for (int k = 0; k < 4; ++k) o += (k ? "," : "") + u128_str(m[k]);
-    const std::string h = dense_list(ghist_);
-    o += " gsamp=" + (h.empty() ? std::string("-") : h);
-    // tail: counts by consecutive candidates from the first p >= tail_t
-    size_t t0 = 0;
-    while (t0 < cand_.size() && cand_[t0] < tail_t_) ++t0;
-    const std::string tl = t0 < cand_.size() ? dense_list(tail_, t0) : std::string();
-    o += " tail=" + (tl.empty() ? std::string("-") : std::to_string(cand_[t0]) + ":" + tl);
-    return o;
+    return r;
 }
 
 std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_t limit, uint64_t segment_even)
@@ -407,10 +425,10 @@ void check(gbc_ctx *ctx, int rc, const char *what)
 
 }  // namespace
 
-RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
+RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
                    uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every)
 {
-    RunStats st;
+    RangeStats st;
     const auto t0 = std::chrono::steady_clock::now();
     if (start < 4) start = 4;
     if (start & 1) start += 1;
@@ -482,14 +500,20 @@ RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segmen
     st.gpu_seconds = gpu_ms / 1e3;
     st.wall_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     st.stats_line = acc.stats_ref_line();
-    st.gbstats_line = acc.gbstats_line("gb300-1.0");
+    st.gbstats_line = acc.gbstats_line(kVersion);
     st.ridges = acc.ridges();
+    // the passed run into the campaign state, once (GoldbachStats::commit)
+    if (StatsCampaign *camp = campaign_of(ctx); camp && start >= kStatsMinStart) {
+        std::string l = camp->commit(acc.record(stats_gaps_of(ctx)), &st.stats_committed);
+        if (!l.empty() && l.back() == '\n') l.pop_back();
+        st.gbstats_line = l;
+    }
     if (outs) outs->finish_run();
     if (acc_out) *acc_out = acc;
     return st;
 }
 
-RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even, uint32_t max_batch,
+RangeStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even, uint32_t max_batch,
                  uint16_t *pn, uint32_t sample_every)
 {
     gbc_config cfg{};
@@ -502,7 +526,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t s
     const int rc = gbc_create(&cfg, &raw);
     std::unique_ptr<gbc_ctx, CtxCloser> ctx(raw);
     if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_create: ") + gbc_last_error(raw));
-    RunStats st = run_range(ctx.get(), start_even, limit, segment_even ? segment_even : GBC_DEFAULT_SEGMENT,
+    RangeStats st = run_range(ctx.get(), start_even, limit, segment_even ? segment_even : GBC_DEFAULT_SEGMENT,
                             max_batch ? max_batch : 8, pn, nullptr, sample_every);
     if (verbose)
         std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",
@@ -510,7 +534,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t s
     return st;
 }
 
-RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2)
+RangeStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2)
 {
     if (start_even < 4) start_even = 4;
     if (start_even & 1) ++start_even;
@@ -531,7 +555,7 @@ RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint3
     rc = gbc_sparse_verify(sp, start_even, limit, &r);
     if (rc != GBC_OK) done(rc, "gbc_sparse_verify");
     gbc_sparse_destroy(sp);
-    RunStats st;
+    RangeStats st;
     st.start = start_even;
     st.limit = limit;
     st.evens = r.evens;
@@ -559,7 +583,7 @@ extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gb
     try {
         gbc_config cfg{};
         if (gbc_get_config(ctx, &cfg) != GBC_OK) return GBC_E_ARG;
-        gb::RunStats st =
+        gb::RangeStats st =
             gb::run_range(ctx, start, limit, cfg.segment_even, cfg.max_batch, pn, nullptr, cfg.sample_every);
         if (res) {
             res->start = st.start;
@@ -587,5 +611,69 @@ extern "C" int gbc_verify_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, gb
     } catch (const std::exception &e) {
         gbh_set_error(ctx, e.what());
         return GBC_E_DEVICE;
+    }
+}
+
+extern "C" int gbc_set_stats(gbc_ctx *ctx, const char *state, const char *log, const char *version, int gaps)
+{
+    if (!ctx) return GBC_E_ARG;
+    if (!state || !*state) {
+        gbh_set_stats(ctx, nullptr, nullptr, true);
+        return GBC_OK;
+    }
+    if (!log || !*log) {
+        gbh_set_error(ctx, "gbc_set_stats: a state file needs a log file");
+        return GBC_E_ARG;
+    }
+    try {
+        auto *c = new gb::StatsCampaign(state, log, version && *version ? version : gb::kVersion);
+        try {
+            c->check();
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        gbh_set_stats(ctx, c, [](void *p) { delete static_cast<gb::StatsCampaign *>(p); }, gaps != 0);
+        return GBC_OK;
+    } catch (const std::exception &e) {
+        gbh_set_error(ctx, e.what());
+        return GBC_E_STATE;
+    }
+}
+
+extern "C" int gbc_stats_commit(const char *state, const char *log, const char *version, int gaps, uint64_t start,
+                                uint64_t limit, const gbc_segment_result *segs, int nseg, char *line, uint64_t line_cap,
+                                int *merged, char *err, size_t err_cap)
+{
+    const auto fail = [&](int code, const std::string &m) {
+        if (err && err_cap) std::snprintf(err, err_cap, "%s", m.c_str());
+        return code;
+    };
+    if (!state || !*state || !log || !*log || !segs || nseg < 1 || start < gb::kStatsMinStart || (start & 1) ||
+        (limit & 1) || limit < start)
+        return fail(GBC_E_ARG, "need state and log paths, results, and even start >= 1e6 <= even limit");
+    uint64_t next = start;
+    for (int i = 0; i < nseg; ++i) {
+        if (segs[i].seg_start != next || segs[i].seg_end < segs[i].seg_start ||
+            segs[i].evens != (segs[i].seg_end - segs[i].seg_start) / 2 + 1)
+            return fail(GBC_E_ARG, "the segments must cover [start, limit] in order");
+        next = segs[i].seg_end + 2;
+    }
+    if (next != limit + 2) return fail(GBC_E_ARG, "the segments must cover [start, limit] in order");
+    try {
+        gb::RunAccumulator acc(start, limit);
+        for (int i = 0; i < nseg; ++i) acc.add_segment(segs[i]);
+        gb::StatsCampaign camp(state, log, version && *version ? version : gb::kVersion);
+        bool m = false;
+        std::string l = camp.commit(acc.record(gaps != 0), &m);
+        if (!l.empty() && l.back() == '\n') l.pop_back();
+        if (merged) *merged = m ? 1 : 0;
+        if (line && line_cap) {
+            if (l.size() + 1 > line_cap) return fail(GBC_E_OVERFLOW, "line buffer too small");
+            std::memcpy(line, l.c_str(), l.size() + 1);
+        }
+        return GBC_OK;
+    } catch (const std::exception &e) {
+        return fail(GBC_E_STATE, e.what());
     }
 }

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gbc.h"
+#include "gb_stats.hpp"
 
 namespace gb {
 
@@ -29,8 +30,10 @@ struct Ridge {
     uint64_t n = 0, p = 0;
 };
 
-// Totals and timings of one run (RunStats, include/verifier.hpp:30-69).
-struct RunStats {
+// Totals and timings of one run on a context (the counts of the reference's
+// RunStats, include/verifier.hpp:30-69; gb_verifier.cpp fills the
+// reference's own struct from it).
+struct RangeStats {
     uint64_t start = 0, limit = 0, evens = 0, segments = 0, batches = 0;
     uint64_t leftovers = 0;       // evens settled by the GPU retry beyond 9781
     uint64_t pmax = 0;            // largest p(n) of the run (exact: tail + sampled segments)
@@ -43,6 +46,8 @@ struct RunStats {
     std::string stats_line;       // tests/stats_ref.cpp's line (every segment sampled), else empty
     std::string gbstats_line;     // the GBSTATS v2 log line of the run (include/gstats.hpp:913-969)
     std::vector<Ridge> ridges;    // the run's top 30 ridges
+    bool stats_committed = false; // merged into the context's campaign state (gbc_set_stats)
+    uint64_t tile_items = 0;      // tile-sieve work items (run, class, tile) over the run's batches
 };
 
 // Run statistics merged from per-segment results (GoldbachStats::add_* and
@@ -66,6 +71,9 @@ public:
     bool fully_sampled() const { return evens_sampled_ == evens_; }
     std::string stats_ref_line() const;
     std::string gbstats_line(const char *version) const;
+    // the run in the campaign's form (gb_stats.hpp); gaps_on = false leaves
+    // the gap statistics out (the reference's GB_GAPS=0)
+    RunRecord record(bool gaps_on = true) const;
     const std::vector<Ridge> &ridges() const { return ridges_; }
 
 private:
@@ -81,6 +89,9 @@ private:
     std::vector<uint16_t> cand_;
     std::vector<uint64_t> samp_;                                  // [15][NCAND], sampled segments
     std::vector<uint64_t> tail_;                                  // [NCAND], p >= tail_t, every segment
+    std::vector<uint64_t> tail_cls_;                              // [15][NCAND], p >= tail_t, sampled segments
+    std::vector<uint64_t> tail_agg_;                              // [NCAND], p >= tail_t, other segments
+    std::vector<std::pair<uint64_t, uint64_t>> beyond_list_;      // (n, p) beyond 9781, in run order
     std::vector<uint64_t> first_all_;                             // first n per candidate, sampled segments
     std::vector<uint64_t> first_tail_;                            // first n per tail candidate, every segment
     std::map<uint64_t, std::pair<uint64_t, uint64_t>> beyond_;    // p -> (count, first n), GPU retry
@@ -148,6 +159,18 @@ private:
 // the outputs attached to a context by gbc_set_outputs, or nullptr
 Outputs *outputs_of(gbc_ctx *ctx);
 
+// the campaign statistics attached to a context by gbc_set_stats, or nullptr;
+// stats_gaps_of: whether its runs record their gaps
+StatsCampaign *campaign_of(gbc_ctx *ctx);
+bool stats_gaps_of(gbc_ctx *ctx);
+
+// the version= field of this build's statistics lines and journal rows
+constexpr const char *kVersion = "gb300-1.0";
+
+// runs that start below this keep no campaign statistics (STATS_MIN_START,
+// include/gstats.hpp:139)
+constexpr uint64_t kStatsMinStart = 1000000;
+
 // Segments of a run: segment_even integers each, the lowest one short
 // (it takes the generic checker), the last one ragged.
 std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_t limit, uint64_t segment_even);
@@ -155,11 +178,11 @@ std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_
 // Runs [start, limit] on an existing context. pn: p(n) of every even, or
 // nullptr. sample_every: every sample_every-th segment (segment 0 always)
 // gets p(n) of every even, the others the funnel verify + exact tail.
-RunStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
+RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
                    uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every = 1);
 
 // The reference's --csv key=value line of a run (src/main.cpp:191-215).
-std::string csv_line(const RunStats &st, uint64_t segment);
+std::string csv_line(const RangeStats &st, uint64_t segment);
 
 // Journaled slices (gb_journal.cpp): the resume point of a journal, and a
 // run of [start, limit] in slices that appends PASS / RETRY rows.
@@ -168,20 +191,20 @@ uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice
                     const std::string &release, const char *stop_file, FILE *log, int *stopped);
 
 // gb::run_gpu: creates a context, runs, destroys it.
-RunStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even = 4,
+RangeStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even = 4,
                  uint32_t max_batch = 8, uint16_t *pn = nullptr, uint32_t sample_every = 1);
 
 // gb::run_gpu_sparse (src/sparse.cpp:840-973): the sparse class map
 // cross-check of [start_even, limit] on one gbc_sparse context; evens,
 // segments, leftovers (evens the GPU left, proved on the CPU) and the
 // stage times. No statistics. Throws GbcError.
-RunStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
+RangeStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
 
 // The sparse cross-check in journaled slices (ci/sparse_crosscheck.sh run):
 // run_slices' rows, resume rule and stop file, each slice through
 // gbc_sparse_verify; its csv line carries path=sparse and no statistics.
 uint64_t run_sparse_slices(gbc_sparse *sp, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
                            const std::string &release, const char *stop_file, FILE *log, int *stopped);
-std::string sparse_csv_line(const RunStats &st);
+std::string sparse_csv_line(const RangeStats &st);
 
 }  // namespace gb

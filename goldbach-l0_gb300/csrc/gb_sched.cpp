@@ -33,9 +33,9 @@ Window::Window(uint64_t id_, uint64_t start_, uint64_t limit_, uint64_t segment_
     t_submit = Clock::now();
 }
 
-RunStats Window::stats() const
+RangeStats Window::stats() const
 {
-    RunStats st;
+    RangeStats st;
     st.start = start;
     st.limit = limit;
     st.evens = acc.evens();
@@ -152,7 +152,7 @@ std::vector<std::shared_ptr<Window>> Scheduler::collect(bool block)
     return done;
 }
 
-std::vector<RunStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint64_t, uint64_t>> &windows,
+std::vector<RangeStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint64_t, uint64_t>> &windows,
                                   SchedStats *out)
 {
     gbc_config cfg{};
@@ -173,7 +173,7 @@ std::vector<RunStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint
         sch.launch_ready();
         sch.collect(true);
     }
-    std::vector<RunStats> res;
+    std::vector<RangeStats> res;
     for (auto &w : ws) res.push_back(w->stats());
     if (out) *out = sch.stats();
     return res;
@@ -183,7 +183,7 @@ std::vector<RunStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint
 
 namespace {
 
-void fill_result(gbc_run_result *r, const gb::RunStats &st)
+void fill_result(gbc_run_result *r, const gb::RangeStats &st)
 {
     r->start = st.start;
     r->limit = st.limit;
@@ -199,7 +199,7 @@ void fill_result(gbc_run_result *r, const gb::RunStats &st)
 }
 
 // the stats_ref line when every segment was sampled, else the GBSTATS v2 line
-int put_line(const gb::RunStats &st, char *line, uint64_t cap)
+int put_line(const gb::RangeStats &st, char *line, uint64_t cap)
 {
     if (!line || !cap) return GBC_OK;
     const std::string &l = st.stats_line.empty() ? st.gbstats_line : st.stats_line;
@@ -219,7 +219,7 @@ extern "C" int gbc_verify_windows(gbc_ctx *ctx, const uint64_t *bounds, int nwin
         for (int i = 0; i < nwin; ++i) w.push_back({bounds[2 * i], bounds[2 * i + 1]});
         const auto t0 = gb::Clock::now();
         gb::SchedStats ss;
-        const std::vector<gb::RunStats> st = gb::run_windows(ctx, w, &ss);
+        const std::vector<gb::RangeStats> st = gb::run_windows(ctx, w, &ss);
         for (int i = 0; i < nwin; ++i) {
             if (res) fill_result(res + i, st[i]);
             if (lines)
@@ -371,7 +371,7 @@ extern "C" int gbc_server_wait(gbc_server *srv, uint64_t id, int timeout_ms, gbc
             auto w = it->second;
             srv->done.erase(it);
             lk.unlock();
-            const gb::RunStats st = w->stats();
+            const gb::RangeStats st = w->stats();
             if (res) fill_result(res, st);
             if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(w->t_done - w->t_submit).count();
             return put_line(st, line, line_cap);

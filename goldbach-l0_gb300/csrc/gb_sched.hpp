@@ -37,7 +37,7 @@ struct Window {
     Clock::time_point t_submit, t_done;
     Window(uint64_t id, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t sample_every);
     bool finished() const { return done == segs.size(); }
-    RunStats stats() const;        // the window's RunStats (lines, counts)
+    RangeStats stats() const;        // the window's RangeStats (lines, counts)
 };
 
 // Totals of a scheduler's life.
@@ -82,8 +82,8 @@ private:
 };
 
 // Verifies every window, segments packed across windows (the batched
-// uneven-window form); returns each window's RunStats in input order.
-std::vector<RunStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint64_t, uint64_t>> &windows,
+// uneven-window form); returns each window's RangeStats in input order.
+std::vector<RangeStats> run_windows(gbc_ctx *ctx, const std::vector<std::pair<uint64_t, uint64_t>> &windows,
                                   SchedStats *out = nullptr);
 
 }  // namespace gb

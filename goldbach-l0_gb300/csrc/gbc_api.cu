@@ -614,6 +614,7 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
 {
     if (!ctx) return;
     if (ctx->outputs && ctx->outputs_del) ctx->outputs_del(ctx->outputs);
+    if (ctx->stats && ctx->stats_del) ctx->stats_del(ctx->stats);
     for (auto &s : ctx->slot) slot_free(s);
     cudaFree(ctx->d_fun);
     cudaFree(ctx->d_fpair);
@@ -638,6 +639,21 @@ void gbh_set_outputs(gbc_ctx *ctx, void *p, void (*del)(void *))
 }
 
 void *gbh_outputs(gbc_ctx *ctx) { return ctx ? ctx->outputs : nullptr; }
+
+// the campaign statistics of runs on the context (gb_run.cpp)
+void gbh_set_stats(gbc_ctx *ctx, void *p, void (*del)(void *), bool gaps)
+{
+    if (ctx->stats && ctx->stats_del) ctx->stats_del(ctx->stats);
+    ctx->stats = p;
+    ctx->stats_del = del;
+    ctx->stats_gaps = gaps;
+}
+
+void *gbh_stats(gbc_ctx *ctx, bool *gaps)
+{
+    if (gaps) *gaps = ctx && ctx->stats_gaps;
+    return ctx ? ctx->stats : nullptr;
+}
 
 void gbh_set_error(gbc_ctx *ctx, const char *msg)
 {

@@ -96,6 +96,10 @@ struct gbc_ctx {
     // host outputs of runs on this context (gb_records.cpp), owned
     void *outputs = nullptr;
     void (*outputs_del)(void *) = nullptr;
+    // campaign statistics files of runs on this context (gb_stats.cpp), owned
+    void *stats = nullptr;
+    void (*stats_del)(void *) = nullptr;
+    bool stats_gaps = true;
     uint64_t launches = 0, batches = 0, graph_replays = 0, selfchecks = 0, hl_batches = 0;
     uint32_t hl_overflow = 0;  // overflow-list marks seen by collect (hl_cap_pct < 100 only)
     uint64_t device_bytes = 0;

@@ -147,6 +147,10 @@ SIGNATURES = {
                                    C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]),
     "gbc_record_event": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint64, C.c_uint64, C.c_int]),
     "gbc_pn_exact": (C.c_uint64, [C.c_uint64]),
+    "gbc_set_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]),
+    "gbc_stats_commit": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_uint64, C.c_uint64,
+                                   C.c_void_p, C.c_int, C.c_char_p, C.c_uint64, C.POINTER(C.c_int), C.c_char_p,
+                                   C.c_size_t]),
     "gbc_class_map_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                         C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_char_p, C.c_size_t]),

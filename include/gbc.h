@@ -404,6 +404,49 @@ int gbc_record_event(const char *records, const char *hook, uint64_t n, uint64_t
 /* p(n) by an ascending Miller-Rabin scan on the CPU (0: none <= n / 2). */
 uint64_t gbc_pn_exact(uint64_t n);
 
+/* ---- campaign statistics ------------------------------------------------------
+ * The reference's campaign statistics files (GoldbachStats, include/gstats.hpp:
+ * 507-1342), in its formats byte for byte:
+ *   state       "statistics state v2": tail_t, covered ranges, evens, primes and
+ *               twins by residue, first occurrences, evens beyond 9781, the
+ *               sampled p(n) histogram and the tail counts per class n mod 30,
+ *               the class-less tail of unsampled segments
+ *   state.gaps  "prime gap state v1" (GapStats): gap ranges, counts, sums of
+ *               g^1..g^4, the walk histogram, the largest gap, gaps >= 700
+ *   log         one GBSTATS v2 line per merged run (gstats.hpp:913-969); a
+ *               GBPSAMP row (the run's p(n) sample) for a covered range run
+ *               again and a GBGAPS row when that run's gaps were not in the
+ *               gap state yet (a backfill)
+ * A passed run is merged once (GoldbachStats::commit, gstats.hpp:715-772):
+ * under an exclusive lock on state.lock the state is re-read; a run that
+ * overlaps a covered range is not merged again; the gap state is written
+ * before the main state, each atomically and durably (temporary file, fsync,
+ * rename); a damaged, cut-off or incompatible state is refused and left
+ * unchanged. Runs that start below 1e6 keep no campaign statistics
+ * (STATS_MIN_START, gstats.hpp:139). */
+
+/* Attaches campaign statistics to ctx: every run of gbc_verify_range and of
+ * gbc_run_slices that passes and starts at >= 1e6 is merged into state and
+ * logged in log, and the run's line is its GBSTATS v2 line as logged.
+ * version: the lines' version= field (NULL: this build's); gaps = 0 keeps no
+ * gap statistics (the reference's GB_GAPS=0). The files are read now: a
+ * damaged or incompatible state is GBC_E_STATE, nothing attached. state =
+ * NULL detaches. */
+int gbc_set_stats(gbc_ctx *ctx, const char *state, const char *log, const char *version, int gaps);
+
+/* The statistics half of the per-segment contract without a context: the
+ * results of one run [start, limit] (nseg segments covering it in order, as
+ * gbc_collect returns them; start >= 1e6) merged into state and log as
+ * above (collect_stats + finish_run + commit, src/verifier.cpp:1012-1045,
+ * 2553-2563). line (may be NULL) gets the run's GBSTATS v2 line, *merged (may
+ * be NULL) 1 when the run was merged, 0 when it overlapped a covered range;
+ * err (may be NULL) the message of a failure: GBC_E_ARG for results that do
+ * not cover the run, GBC_E_STATE for a coverage failure in a segment or a
+ * damaged, unreadable or unwritable state (the files are then unchanged). */
+int gbc_stats_commit(const char *state, const char *log, const char *version, int gaps, uint64_t start,
+                     uint64_t limit, const gbc_segment_result *segs, int nseg, char *line, uint64_t line_cap,
+                     int *merged, char *err, size_t err_cap);
+
 /* ---- allocation-free class map ---------------------------------------------
  * This entry point has no counterpart in the reference.
  *

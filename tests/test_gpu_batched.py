@@ -181,20 +181,51 @@ def uneven_windows(n=256, seed=7):
 
 
 def test_uneven_windows_sampled_against_oracle_config_c4():
-    """All 256 windows in shared batches; 8 sampled windows (seed 8, among
-    those under 2e7 wide so the oracle finishes in seconds) against the
-    oracle's exact sieve, every window against its run alone."""
+    """All 256 windows in shared batches, plus one of 1e9 across 2^63;
+    against the oracle's exact sieve: 8 sampled windows (seed 8, among those
+    under 2e7 wide so the oracle finishes in seconds), the narrowest window
+    of at least 1e9 (several 467.5M segments in one run) and the window
+    across 2^63; every one of 16 sampled windows against its run alone."""
     wins = uneven_windows()
     small = [i for i, (a, b) in enumerate(wins) if b - a < 2 * 10**7]
     pick = random.Random(8).sample(small, 8)
+    wide = min((i for i, (a, b) in enumerate(wins) if b - a >= 10**9), key=lambda i: wins[i][1] - wins[i][0])
+    top = 2**63 - 400_000_000
+    wins.append((top, top + 10**9))
+    pick += [wide, len(wins) - 1]
     limit = max(b for _, b in wins)
     with gbc.Context(limit=limit, segment_even=gbc.DEFAULT_SEGMENT, max_batch=16, max_runs=16, nslots=3) as c:
         out, summ = c.verify_windows(wins)
-        assert summ.runs >= 256 and summ.batches < summ.segments
+        assert summ.runs >= 257 and summ.batches < summ.segments
         for i in pick:
             assert out[i][1] == oracle.stats_line(wins[i][0], wins[i][1], oracle.SIEVE), wins[i]
-        for i in random.Random(9).sample(range(len(wins)), 16):
+        for i in random.Random(9).sample(range(len(wins) - 1), 16):
             assert out[i][1] == c.verify_range(*wins[i])[1], wins[i]
+
+
+def test_slice_seeded_segments_config_c3():
+    """Three seeded segments of the full 5e13 slice [4e18, 4e18 + 5e13]
+    (random.Random(3), the segments bench.py --slice checks), each in a run
+    of three consecutive segments under the tuned knobs of the batched form
+    (tile-binned hit lists through the prime-multiplier table): the run's
+    stats_ref line (every p(n), primes, twins, gaps) and each segment's
+    class-map hash against the oracle's exact sieve."""
+    import autotune
+    a = 4 * 10**18
+    b = a + 5 * 10**13
+    segs = gbc.segments_of(a, b, gbc.DEFAULT_SEGMENT)
+    pick = sorted(random.Random(3).sample(range(len(segs)), 3))
+    knobs = autotune.load(autotune.DEFAULT_RECORD)
+    with gbc.Context(limit=b, segment_even=gbc.DEFAULT_SEGMENT, hl_mode=1, **knobs) as c:
+        for i in pick:
+            run = segs[max(0, i - 1):i + 2]
+            s, e = run[0][0], run[-1][1]
+            c.enqueue_batch(0, run, e)
+            res, _ = c.collect(0, len(run))
+            assert c.stats().p_hl > 0
+            for r in res:
+                assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi), (r.seg_start, r.seg_end)
+            assert c.verify_range(s, e)[1] == oracle.stats_line(s, e, oracle.SIEVE), (i, s, e)
 
 
 def test_journaled_slices_resume_and_stop(tmp_path):
