@@ -70,35 +70,6 @@ bool parse_count(const char *s, uint64_t &out)
     return true;
 }
 
-// The run's ridge store, records file and live snapshot at the reference's
-// paths (src/verifier.cpp:725-745, include/gstats.hpp:474-478):
-// GB_RIDGE_FILE (goldbach_ridges.csv; GB_RIDGE=0 turns ridges off),
-// GB_RECORDS_FILE (goldbach_records.txt), GB_STATS_LIVE (goldbach_live.json);
-// a variable set but empty turns its output off. The record hook is
-// GB_RECORD_HOOK (set but empty: none), else scripts/notify_record.sh when
-// present.
-void attach_outputs(gbc_ctx *ctx)
-{
-    auto path = [](const char *var, const char *def) -> std::string {
-        const char *v = std::getenv(var);
-        return v ? v : def;
-    };
-    const char *rg = std::getenv("GB_RIDGE");
-    const bool ridge_on = !(rg && (!std::strcmp(rg, "0") || !std::strcmp(rg, "off")));
-    const std::string ridge = ridge_on ? path("GB_RIDGE_FILE", "goldbach_ridges.csv") : "";
-    const std::string rec = path("GB_RECORDS_FILE", "goldbach_records.txt");
-    const std::string live = path("GB_STATS_LIVE", "goldbach_live.json");
-    const char *hk = std::getenv("GB_RECORD_HOOK");
-    std::string hook = hk ? hk : "";
-    if (!hk)
-        if (std::FILE *f = std::fopen("scripts/notify_record.sh", "rb")) {
-            std::fclose(f);
-            hook = "bash scripts/notify_record.sh";
-        }
-    if (gbc_set_outputs(ctx, ridge.c_str(), rec.c_str(), live.c_str(), hook.c_str()) != GBC_OK)
-        std::fprintf(stderr, "outputs: %s\n", gbc_last_error(ctx));
-}
-
 int usage()
 {
     std::fprintf(stderr,
@@ -206,7 +177,7 @@ int main(int argc, char **argv)
             return code;
         }
         try {
-            const gb::RangeStats st = gb::run_gpu_sparse(limit, verbose, start);
+            const gb::RangeStats st = gb::run_sparse(limit, verbose, start);
             const double eps = st.gpu_seconds > 0 ? double(st.evens) / st.gpu_seconds : 0.0;
             if (csv)
                 std::printf("result=PASS,path=sparse,start=%" PRIu64 ",limit=%" PRIu64 ",evens=%" PRIu64
@@ -235,7 +206,7 @@ int main(int argc, char **argv)
         gbc_destroy(ctx);
         return rc == GBC_E_ARG ? 2 : 1;
     }
-    attach_outputs(ctx);
+    gb::attach_env_outputs(ctx);
     if (slice) {
         int code = 0;
         try {

@@ -296,6 +296,36 @@ void *gbh_outputs(gbc_ctx *ctx);  // gbc_api.cu
 
 gb::Outputs *gb::outputs_of(gbc_ctx *ctx) { return static_cast<gb::Outputs *>(gbh_outputs(ctx)); }
 
+// The run's ridge store, records file and live snapshot at the reference's
+// paths (src/verifier.cpp:725-745, include/gstats.hpp:474-478):
+// GB_RIDGE_FILE (goldbach_ridges.csv; GB_RIDGE=0 turns ridges off),
+// GB_RECORDS_FILE (goldbach_records.txt), GB_STATS_LIVE (goldbach_live.json);
+// a variable set but empty turns its output off. The record hook is
+// GB_RECORD_HOOK (set but empty: none), else scripts/notify_record.sh when
+// present.
+void gb::attach_env_outputs(gbc_ctx *ctx)
+{
+    auto path = [](const char *var, const char *def) -> std::string {
+        const char *v = std::getenv(var);
+        return v ? v : def;
+    };
+    const char *rg = std::getenv("GB_RIDGE");
+    const bool ridge_on = !(rg && (!std::strcmp(rg, "0") || !std::strcmp(rg, "off")));
+    const std::string ridge = ridge_on ? path("GB_RIDGE_FILE", "goldbach_ridges.csv") : "";
+    const std::string rec = path("GB_RECORDS_FILE", "goldbach_records.txt");
+    const std::string live = path("GB_STATS_LIVE", "goldbach_live.json");
+    const char *hk = std::getenv("GB_RECORD_HOOK");
+    std::string hook = hk ? hk : "";
+    if (!hk)
+        if (std::FILE *f = std::fopen("scripts/notify_record.sh", "rb")) {
+            std::fclose(f);
+            hook = "bash scripts/notify_record.sh";
+        }
+    if (gbc_set_outputs(ctx, ridge.c_str(), rec.c_str(), live.c_str(), hook.c_str()) != GBC_OK)
+        std::fprintf(stderr, "outputs: %s\n", gbc_last_error(ctx));
+}
+
+
 // ---------------------------------------------------------------------------
 // C ABI
 

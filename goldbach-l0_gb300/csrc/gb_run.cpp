@@ -1,5 +1,5 @@
-// gb_run.cpp -- the run driver above the C ABI: gbc_verify_range and the
-// C++ gb::run_gpu of gb_run.hpp.
+// gb_run.cpp -- the run driver above the C ABI: gbc_verify_range, the
+// campaign statistics calls and gb::run_range of gb_run.hpp.
 //
 // Follows the reference's DenseRun (src/verifier.cpp:2487-2569): segments
 // of segment_even integers, two slots in flight (batch k + 1 is enqueued
@@ -426,7 +426,7 @@ void check(gbc_ctx *ctx, int rc, const char *what)
 }  // namespace
 
 RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
-                   uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every)
+                     uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every, bool per_segment)
 {
     RangeStats st;
     const auto t0 = std::chrono::steady_clock::now();
@@ -452,12 +452,26 @@ RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segm
     Outputs *outs = outputs_of(ctx);
     const std::vector<uint16_t> cand = outs ? candidates() : std::vector<uint16_t>();
     const uint64_t evens_total = (limit - start) / 2 + 1;
+    auto t_last = std::chrono::steady_clock::now();
     auto collect = [&](size_t b) {
         const int slot = int(b & 1);
         const int n = int(batches[b].size());
         out[slot].resize(n);
         gbc_batch_times tm{};
         check(ctx, gbc_collect(ctx, slot, out[slot].data(), n, &tm, 600000), "collect");
+        if (per_segment) {
+            const auto now = std::chrono::steady_clock::now();
+            const double wall = std::chrono::duration<double, std::milli>(now - t_last).count();
+            t_last = now;
+            uint64_t be = 0;
+            for (int i = 0; i < n; ++i) be += out[slot][i].evens;
+            for (int i = 0; i < n; ++i) {
+                const auto &r = out[slot][i];
+                const double f = double(r.evens) / double(be);
+                st.per_segment.push_back({r.seg_start, r.seg_end, r.evens, r.nleft, tm.ms_tile * f, tm.ms_large * f,
+                                          (tm.ms_check + tm.ms_count) * f, wall * f});
+            }
+        }
         gpu_ms += tm.ms_total;
         st.tile_ms += tm.ms_tile;
         st.large_ms += tm.ms_large;
@@ -513,28 +527,7 @@ RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segm
     return st;
 }
 
-RangeStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even, uint32_t max_batch,
-                 uint16_t *pn, uint32_t sample_every)
-{
-    gbc_config cfg{};
-    cfg.limit = limit & ~uint64_t(1);
-    cfg.segment_even = segment_even;
-    cfg.max_batch = max_batch;
-    cfg.want_pn = pn ? 1 : 0;
-    cfg.sample_every = sample_every;
-    gbc_ctx *raw = nullptr;
-    const int rc = gbc_create(&cfg, &raw);
-    std::unique_ptr<gbc_ctx, CtxCloser> ctx(raw);
-    if (rc != GBC_OK) throw GbcError(rc, std::string("gbc_create: ") + gbc_last_error(raw));
-    RangeStats st = run_range(ctx.get(), start_even, limit, segment_even ? segment_even : GBC_DEFAULT_SEGMENT,
-                            max_batch ? max_batch : 8, pn, nullptr, sample_every);
-    if (verbose)
-        std::fprintf(stderr, "run [%" PRIu64 ", %" PRIu64 "]: %" PRIu64 " segments, gpu %.3f s, wall %.3f s\n",
-                     st.start, st.limit, st.segments, st.gpu_seconds, st.wall_seconds);
-    return st;
-}
-
-RangeStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2)
+RangeStats run_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2)
 {
     if (start_even < 4) start_even = 4;
     if (start_even & 1) ++start_even;

@@ -1,9 +1,10 @@
 // gb_run.hpp -- C++ run driver over the C ABI of include/gbc.h.
 //
-// gb::run_gpu mirrors the reference's entry point (include/verifier.hpp:
-// 71-110): verify every even in [start_even, limit], return the run's
-// statistics, throw on any failure (GbcError carries the C ABI status), and
-// never report a PASS that did not happen.
+// run_range is the work of the reference's gb::run_gpu (include/verifier.hpp:
+// 71-110) on an existing context: verify every even in [start, limit],
+// return the run's statistics, throw on any failure (GbcError carries the C
+// ABI status), and never report a PASS that did not happen. gb_verifier.cpp
+// wraps it in the reference's own signature (include/gb_verifier.hpp).
 #pragma once
 #include <cstdint>
 #include <cstdio>
@@ -30,6 +31,13 @@ struct Ridge {
     uint64_t n = 0, p = 0;
 };
 
+// One segment's share of its batch (gb::run_gpu's per_segment records).
+struct SegRecord {
+    uint64_t start = 0, end = 0, evens = 0;
+    uint32_t leftovers = 0;
+    double tile_ms = 0, large_ms = 0, check_ms = 0, wall_ms = 0;  // the segment's share by evens
+};
+
 // Totals and timings of one run on a context (the counts of the reference's
 // RunStats, include/verifier.hpp:30-69; gb_verifier.cpp fills the
 // reference's own struct from it).
@@ -47,7 +55,7 @@ struct RangeStats {
     std::string gbstats_line;     // the GBSTATS v2 log line of the run (include/gstats.hpp:913-969)
     std::vector<Ridge> ridges;    // the run's top 30 ridges
     bool stats_committed = false; // merged into the context's campaign state (gbc_set_stats)
-    uint64_t tile_items = 0;      // tile-sieve work items (run, class, tile) over the run's batches
+    std::vector<SegRecord> per_segment;  // filled when run_range is asked for it
 };
 
 // Run statistics merged from per-segment results (GoldbachStats::add_* and
@@ -159,6 +167,10 @@ private:
 // the outputs attached to a context by gbc_set_outputs, or nullptr
 Outputs *outputs_of(gbc_ctx *ctx);
 
+// attaches the reference's ridge store, records file, live snapshot and
+// record hook to ctx from its GB_* environment (gb_records.cpp)
+void attach_env_outputs(gbc_ctx *ctx);
+
 // the campaign statistics attached to a context by gbc_set_stats, or nullptr;
 // stats_gaps_of: whether its runs record their gaps
 StatsCampaign *campaign_of(gbc_ctx *ctx);
@@ -179,7 +191,7 @@ std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_
 // nullptr. sample_every: every sample_every-th segment (segment 0 always)
 // gets p(n) of every even, the others the funnel verify + exact tail.
 RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segment_even, uint32_t max_batch,
-                   uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every = 1);
+                     uint16_t *pn, RunAccumulator *acc_out, uint32_t sample_every = 1, bool per_segment = false);
 
 // The reference's --csv key=value line of a run (src/main.cpp:191-215).
 std::string csv_line(const RangeStats &st, uint64_t segment);
@@ -190,15 +202,11 @@ uint64_t journal_resume(const std::string &path, uint64_t start);
 uint64_t run_slices(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t slice, const std::string &journal,
                     const std::string &release, const char *stop_file, FILE *log, int *stopped);
 
-// gb::run_gpu: creates a context, runs, destroys it.
-RangeStats run_gpu(uint64_t limit, uint64_t segment_even, bool verbose, uint64_t start_even = 4,
-                 uint32_t max_batch = 8, uint16_t *pn = nullptr, uint32_t sample_every = 1);
-
-// gb::run_gpu_sparse (src/sparse.cpp:840-973): the sparse class map
-// cross-check of [start_even, limit] on one gbc_sparse context; evens,
-// segments, leftovers (evens the GPU left, proved on the CPU) and the
-// stage times. No statistics. Throws GbcError.
-RangeStats run_gpu_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
+// The sparse class map cross-check of [start_even, limit] on one gbc_sparse
+// context (the work of gb::run_gpu_sparse, src/sparse.cpp:840-973); evens,
+// segments, leftovers (evens the GPU left, proved on the CPU) and the stage
+// times. No statistics. Throws GbcError.
+RangeStats run_sparse(uint64_t limit, bool verbose, uint64_t start_even, uint32_t dlt_log2 = 0);
 
 // The sparse cross-check in journaled slices (ci/sparse_crosscheck.sh run):
 // run_slices' rows, resume rule and stop file, each slice through
