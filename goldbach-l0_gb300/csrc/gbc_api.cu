@@ -481,6 +481,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
             if (gbk::class_of(u) < 8) list.push_back(uint16_t(i));
         }
         ctx->ct.cnt[cr] = uint32_t(list.size()) - ctx->ct.off[cr];
+        if (cfg.test_flags & GBC_TEST_RETRY_LIMIT) ctx->ct.cnt[cr] = std::min<uint32_t>(ctx->ct.cnt[cr], 1);
     }
     // verify plan (the reference's make_plan30, include/check30.hpp:88-174,
     // with our own greedy order): per class, the useful candidates below
@@ -603,6 +604,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->vt.rest = ctx->d_rest;
     ctx->vt.ridge_min = cfg.ridge_min;
     ctx->vt.f1 = cfg.verify_funnels;
+    ctx->vt.spin0 = (cfg.test_flags & GBC_TEST_STAGING_WAIT) ? 0u : gbk::kStageSpin;
     ctx->slot.resize(cfg.nslots);
     for (auto &s : ctx->slot)
         if (int r = slot_alloc(ctx, s)) return r;
@@ -802,6 +804,7 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
         bp.map = s.map + map_off;
         bp.xfirst = s.xfirst + xf_off;
         bp.err = s.err;
+        bp.spin0 = (ctx->cfg.test_flags & GBC_TEST_STAGING_WAIT) ? 0u : gbk::kStageSpin;
         map_off += words;
         xf_off += uint64_t(8) * bp.n_mid;
         for (int k = i; k < j; ++k) img.segs[k].run = nrun;
@@ -938,6 +941,7 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
         bb.skip_tab = ctx->d_skip;
         bb.inv_tab = ctx->d_inv;
         bb.err = ctx->slot[0].err;
+        bb.spin0 = gbk::kStageSpin;
         const uint64_t root = isqrt64(bb.qmax);
         bb.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
         bb.i0 = std::min(ctx->i0, bb.n_all);
@@ -1028,7 +1032,7 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     CK(cudaEventRecordWithFlags(s.ev[2], st, rec));
     gbh::launch_check(d, ctx->ct, g, st);
     gbh::launch_verify(d, ctx->vt, g, st);
-    gbh::launch_retry(d, ctx->cfg.ridge_min, g, st);
+    gbh::launch_retry(d, ctx->cfg.ridge_min, (ctx->cfg.test_flags & GBC_TEST_RETRY_LIMIT) ? 1u : (1u << 22), g, st);
     CK(cudaEventRecordWithFlags(s.ev[3], st, rec));
     gbh::launch_count(d, g, st);
     CK(cudaEventRecordWithFlags(s.ev[4], st, rec));

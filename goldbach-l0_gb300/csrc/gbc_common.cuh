@@ -101,6 +101,7 @@ struct BatchParams {
     uint32_t ovf_cap;
     uint2 *ovf_buf;           // (class, bit) of each overflow mark
     uint32_t *ovf_cnt;
+    uint32_t spin0;           // try_wait rounds of the first wait on a tile bin's bulk copies (kStageSpin)
 };
 
 // a one-run batch whose hit lists go through the tile bins
@@ -221,6 +222,7 @@ struct VerifyTables {
     uint32_t rest_off[GBC_NCLASS], rest_cnt[GBC_NCLASS];
     uint32_t ridge_min;     // evens with p(n) >= ridge_min are listed with their p(n)
     uint32_t f1;            // funnels every word takes before the unresolved ones are gathered (>= 1)
+    uint32_t spin0;         // try_wait rounds of the first wait on a chunk's bulk copies (kStageSpin)
 };
 
 // device error flags
@@ -302,10 +304,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// waits for the phase of the given parity; false when the limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// waits for the phase of the given parity, at most `rounds` try_wait
+// rounds; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t rounds = kStageSpin)
 {
-    for (uint32_t i = 0; i < kStageSpin; ++i)
+    for (uint32_t i = 0; i < rounds; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -399,7 +402,7 @@ void launch_hl_overflow(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st
 void query_sieve_grids(Grids &g);
 void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st);
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st);
-void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st);
+void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, uint32_t tries, const Grids &g, cudaStream_t st);
 void launch_count(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_map_compare(const gbk::BatchDesc &a, const gbk::BatchDesc &b, uint32_t *count, const Grids &g,
                         cudaStream_t st);

@@ -271,9 +271,10 @@ __global__ void __launch_bounds__(256) k_check_low(BatchDesc d, const uint16_t *
 }
 
 // Evens without a witness <= 9781: ascending odd p > 9781 by Miller-Rabin on
-// both p and n - p (n = 4: p = 2). A bounded search: a wait that runs out
-// sets an error flag instead of looping. A CTA per segment.
-__global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
+// both p and n - p (n = 4: p = 2). A bounded search of at most max_tries
+// candidates: one that runs out sets an error flag instead of looping. A
+// CTA per segment.
+__global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min, uint32_t max_tries)
 {
     const uint32_t nseg = d.h->nseg;
     for (uint32_t si = blockIdx.x; si < nseg; si += gridDim.x) {
@@ -287,7 +288,7 @@ __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min)
             else {
                 uint32_t tries = 0;
                 for (uint64_t p = GBC_MAX_CAND + 2; p <= n / 2; p += 2) {
-                    if (++tries > (1u << 22)) {
+                    if (++tries > max_tries) {
                         atomicOr(&res->err, kErrRetry);
                         break;
                     }
@@ -522,7 +523,7 @@ __global__ void __launch_bounds__(kVerifyThreads, 3) k_verify(BatchDesc d, Verif
                         stage_chunk(s_win[warp][buf ^ 1u], bar + (buf ^ 1u), src0 + size_t(nx) * kVChunk, wpc, bytes);
                     }
                 }
-                if (!mbar_wait(bar + buf, (phase >> buf) & 1u)) {
+                if (!mbar_wait(bar + buf, (phase >> buf) & 1u, vt.spin0)) {
                     atomicOr(&res->err, kErrStaging);
                     mbar_wait(bar + buf, (phase >> buf) & 1u);
                 }
@@ -767,9 +768,9 @@ void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const G
     gbk::k_tail<<<g.sm * 2, gbk::kTailThreads, 0, st>>>(d, vt);
 }
 
-void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, const Grids &g, cudaStream_t st)
+void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, uint32_t tries, const Grids &g, cudaStream_t st)
 {
-    gbk::k_retry<<<g.max_seg < 1024 ? g.max_seg : 1024, 64, 0, st>>>(d, ridge_min);
+    gbk::k_retry<<<g.max_seg < 1024 ? g.max_seg : 1024, 64, 0, st>>>(d, ridge_min, tries);
 }
 
 void query_check_grids(Grids &g)

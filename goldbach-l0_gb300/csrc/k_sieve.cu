@@ -283,7 +283,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
     if constexpr (kVec4) {
         const uint32_t n = *nb, staged = min(n, kTbStage);
         if (staged) {
-            bool ok = mbar_wait(bar, *phase & 1u);
+            bool ok = mbar_wait(bar, *phase & 1u, bp.spin0);
             if (!ok) {
                 atomicOr(bp.err, kErrStaging);
                 ok = mbar_wait(bar, *phase & 1u);

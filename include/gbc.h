@@ -96,8 +96,22 @@ typedef struct gbc_config {
     uint32_t hl_cap_pct;     /* the hit-list bins' quotas and capacities in percent of their sizing
                                 (default 100; lower values make marks take the overflow list, which
                                 is cleared after the tiles: for tests of that path) */
-    uint32_t reserved[2];
+    uint32_t test_flags;     /* 0 in production; GBC_TEST_* below, for tests of the failure paths */
+    uint32_t reserved;
 } gbc_config;
+
+/* test_flags: each makes a bounded device wait run out, so a test sees the
+ * batch fail closed (gbc_collect: GBC_E_DEVICE) with no fault and the
+ * context still usable.
+ *   GBC_TEST_STAGING_WAIT  the first wait on every bulk copy into shared
+ *                          memory in the tile sieve and the verify checker
+ *                          gives up at once; its second wait keeps the
+ *                          normal limit, so the copies in flight still land
+ *   GBC_TEST_RETRY_LIMIT   the exact checker keeps the first candidate of
+ *                          each class only, so evens go to the GPU retry,
+ *                          whose search stops after one try */
+#define GBC_TEST_STAGING_WAIT 1u
+#define GBC_TEST_RETRY_LIMIT 2u
 
 #define GBC_MAX_SLOTS 8
 
