@@ -459,6 +459,7 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--sample-every", type=int, default=256)
     ap.add_argument("--tile-log2", type=int, default=0)
+    ap.add_argument("--tile-bits", type=int, default=0, help="bits per tile (a multiple of 4096); overrides the record")
     ap.add_argument("--p-mid", type=int, default=0)
     ap.add_argument("--hl-mode", type=int, default=0)
     ap.add_argument("--mtab-gb", type=int, default=0)
@@ -508,6 +509,8 @@ def run_gb300(args, rep):
         tuned = autotune.load(args.tuning or autotune.DEFAULT_RECORD)
         if tuned:
             knobs.update(tuned)
+    if args.tile_bits:
+        knobs["tile_bits"] = args.tile_bits
     args.batch = knobs["max_batch"]
     # rank r: its own consecutive segments, after those of the ranks below
     allb = batches(start, rep.rank * nb * args.batch, nb, args.batch)

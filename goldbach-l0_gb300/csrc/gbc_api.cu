@@ -251,10 +251,16 @@ static uint32_t hl_quota(double marks_per_bit, uint64_t nblk, uint32_t rlog, uin
 
 // Offsets per tile bin: the expected marks of a tile + 15%, + 2048, whole
 // lines (the density is that of the run's top, where it is highest).
-static size_t tb_capacity(double marks_per_bit, uint32_t tile_log2)
+static size_t tb_capacity(double marks_per_bit, uint32_t tile_bits)
 {
-    return align_up(size_t(1.15 * marks_per_bit * double(1u << tile_log2)) + 2048, 32);
+    return align_up(size_t(1.15 * marks_per_bit * double(tile_bits)) + 2048, 32);
 }
+
+// tiles of a class array of `bits` bits
+static uint32_t tiles_of(uint64_t bits, uint32_t tile_bits) { return uint32_t((bits + tile_bits - 1) / tile_bits); }
+
+// the largest tile the persistent tile kernel takes: 224 KB of shared memory
+constexpr uint32_t kMaxTileBits = 1835008;
 
 // overflow marks a binned batch may leave: 2% of a full batch's, at least 2^22
 static uint32_t overflow_cap(double marks)
@@ -299,10 +305,9 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks / (8.0 * double(nblk)), nblk, rlog, ctas);
         CK(dev_alloc(ctx, &s.hl_buf, std::max<size_t>(s.hl_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.hl_cnt, size_t(ctas) * gbk::kHlMaxBins * 4));
-        // tile bins: wpc_cap is a whole number of tiles
-        const uint32_t tl2 = cfg.tile_log2;
-        s.tb_cnt_words = size_t(8) * ((size_t(ctx->wpc_cap) * 32) >> tl2);
-        s.tb_buf_words = s.tb_cnt_words * tb_capacity(marks / (8.0 * double(nblk)), tl2);
+        // tile bins: the tiles of a class array of wpc_cap words
+        s.tb_cnt_words = size_t(8) * tiles_of(uint64_t(ctx->wpc_cap) * 32, ctx->tile_bits);
+        s.tb_buf_words = s.tb_cnt_words * tb_capacity(marks / (8.0 * double(nblk)), ctx->tile_bits);
         CK(dev_alloc(ctx, &s.tb_buf, std::max<size_t>(s.tb_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.tb_cnt, std::max<size_t>(s.tb_cnt_words, 1) * 4));
         s.ovf_cap = overflow_cap(marks);
@@ -380,6 +385,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     else if (cfg.nslots < 2 || cfg.nslots > GBC_MAX_SLOTS) rc = fail(ctx, GBC_E_ARG, "nslots outside [2, 8]");
     else if (cfg.launch_mode > 2) rc = fail(ctx, GBC_E_ARG, "launch_mode outside [0, 2]");
     else if (cfg.tile_log2 < 14 || cfg.tile_log2 > 20) rc = fail(ctx, GBC_E_ARG, "tile_log2 outside [14, 20]");
+    else if (cfg.tile_bits && (cfg.tile_bits % 4096 || cfg.tile_bits < (1u << 14) || cfg.tile_bits > kMaxTileBits))
+        rc = fail(ctx, GBC_E_ARG, "tile_bits must be a multiple of 4096 in [2^14, 1835008]");
     else if (cfg.p_mid < 128) rc = fail(ctx, GBC_E_ARG, "p_mid below 128");
     else if (uint64_t(cfg.max_batch) * cfg.segment_even / 30 > (1ull << 31))
         rc = fail(ctx, GBC_E_ARG, "max_batch * segment_even / 30 must stay below 2^31 class bits");
@@ -407,7 +414,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     const auto &pr = ctx->primes;
     ctx->i0 = uint32_t(std::lower_bound(pr.begin(), pr.end(), gbk::kFirstSievePrime) - pr.begin());
     ctx->n_mid = uint32_t(std::upper_bound(pr.begin(), pr.end(), cfg.p_mid) - pr.begin());
-    const uint32_t tb = 1u << cfg.tile_log2;
+    ctx->tile_bits = cfg.tile_bits ? cfg.tile_bits : 1u << cfg.tile_log2;
+    const uint32_t tb = ctx->tile_bits;
     // primes with at least 128 marks per tile: a warp per prime; above, a
     // thread per prime (measured on 128-segment batches at 4e18 with 2^20-bit
     // tiles: tb / 64 13.37 ms, tb / 128 13.03, tb / 256 13.55 per tile stage)
@@ -536,7 +544,8 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     ctx->layout = DescLayout(cfg.max_runs, cfg.max_batch);
 
     *out = ctx;
-    gbh::tile_attributes(cfg.tile_log2, ctx->gi);
+    if (!gbh::tile_attributes(ctx->tile_bits, cfg.tile_log2, ctx->gi, cfg.device, &ctx->tile_stage))
+        return fail(ctx, GBC_E_ARG, "tile_bits: the tile does not fit the device's shared memory");
     gbh::query_check_grids(ctx->grids);
     gbh::query_count_grids(ctx->grids);
     gbh::query_sieve_grids(ctx->grids);
@@ -712,11 +721,12 @@ static void plan_run(const gbc_ctx *ctx, gbk::BatchParams &bp, uint64_t s0, uint
     bp.base = qlo / 30 * 30;
     bp.qmax = sN + 3;
     const uint64_t nblk = (bp.qmax - bp.base) / 30 + 1;
-    const uint32_t tb = 1u << ctx->cfg.tile_log2;
     bp.nblk = uint32_t(nblk);
     bp.wpc = uint32_t(run_wpc(nblk));
-    bp.tiles_pc = uint32_t((uint64_t(bp.wpc) * 32 + tb - 1) / tb);
+    bp.tiles_pc = tiles_of(uint64_t(bp.wpc) * 32, ctx->tile_bits);
     bp.tile_log2 = ctx->cfg.tile_log2;
+    bp.tile_bits = ctx->tile_bits;
+    bp.tile_rcp = uint32_t(((uint64_t(1) << 32) + ctx->tile_bits - 1) / ctx->tile_bits);
     bp.primes = ctx->d_primes;
     bp.magic = ctx->d_magic;
     bp.pat = ctx->d_pat;
@@ -848,10 +858,12 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
         const uint32_t pct = ctx->cfg.hl_cap_pct;
         const uint32_t quota = uint32_t(std::max<size_t>(
             32, align_up(size_t(hl_quota(marks / (8.0 * double(bp.nblk)), bp.nblk, rlog, ctas)) * pct / 100, 32)));
-        const uint32_t tl2 = ctx->cfg.tile_log2;
         const size_t tiles = size_t(8) * bp.tiles_pc,
-                     tcap = std::max<size_t>(32, align_up(tb_capacity(marks / (8.0 * double(bp.nblk)), tl2) * pct / 100, 32));
-        const bool tb_fit = rlog >= tl2 && (uint64_t(1) << (rlog - tl2)) <= gbk::kSortMaxTiles &&
+                     tcap = std::max<size_t>(
+                         32, align_up(tb_capacity(marks / (8.0 * double(bp.nblk)), ctx->tile_bits) * pct / 100, 32));
+        // k_binsort sorts a region's offsets by tile in shared memory: at
+        // most kSortMaxTiles tiles meet a region
+        const bool tb_fit = tiles_of(uint64_t(1) << rlog, ctx->tile_bits) + 1 <= gbk::kSortMaxTiles &&
                             tiles <= s.tb_cnt_words && tiles * tcap <= s.tb_buf_words && tcap < (1ull << 31);
         if (size_t(ctas) * nbin * quota <= s.hl_buf_words && tb_fit) {
             bp.hl_buf = s.hl_buf;
@@ -909,7 +921,7 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
     ctx->mtab_bytes = nbytes;
     // sieve [lo, hi] in chunks through a temporary class map, each chunk a
     // one-run batch of its own descriptor (all uploaded before the first launch)
-    const uint32_t tb = 1u << ctx->cfg.tile_log2;
+    const uint32_t tb = ctx->tile_bits;
     const uint64_t chunk = uint64_t(1) << 28;  // blocks (bytes) per chunk, a multiple of 32
     const uint64_t nchunk = (nbytes + chunk - 1) / chunk;
     const uint64_t wpc = align_up(run_wpc(chunk), tb / 32);
@@ -933,6 +945,8 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
         bb.wpc = uint32_t(wpc);
         bb.tiles_pc = uint32_t(wpc * 32 / tb);
         bb.tile_log2 = ctx->cfg.tile_log2;
+        bb.tile_bits = tb;
+        bb.tile_rcp = uint32_t(((uint64_t(1) << 32) + tb - 1) / tb);
         bb.map = tmp;
         bb.primes = ctx->d_primes;
         bb.magic = ctx->d_magic;
@@ -960,7 +974,7 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
     for (uint64_t c = 0; c < nchunk; ++c) {
         const gbk::BatchDesc d = lay.device(ddev + c * lay.bytes);
         gbh::launch_xfirst(d, ctx->grids, st);
-        gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, ctx->grids, st);
+        gbh::launch_tile(d, ctx->gi, ctx->tile_bits, ctx->tile_stage, ctx->grids, st);
         gbh::launch_large(d, ctx->grids, st);
         gbh::launch_wheel_bytes(runs[c], ctx->mtab + c * chunk / 4, st);
         ctx->launches += 4;
@@ -1025,7 +1039,7 @@ static int issue_pipeline(gbc_ctx *ctx, Slot &s, bool capture)
     gbh::launch_hitlist(d, false, g, st);  // binned batches: harvest into region bins
     gbh::launch_binsort(d, g, st);         // ... then into tile bins
     CK(cudaEventRecordWithFlags(s.ev[1], st, rec));
-    gbh::launch_tile(d, ctx->gi, ctx->cfg.tile_log2, g, st);  // with the tile bins' marks
+    gbh::launch_tile(d, ctx->gi, ctx->tile_bits, ctx->tile_stage, g, st);  // with the tile bins' marks
     gbh::launch_large(d, g, st);
     gbh::launch_hitlist(d, true, g, st);   // other batches: direct marks
     gbh::launch_hl_overflow(d, g, st);
@@ -1091,7 +1105,7 @@ static int issue_selfcheck(gbc_ctx *ctx, Slot &s)
     cudaStream_t st = s.st;
     CK(cudaMemcpyAsync(s.chk_desc_dev, s.chk_desc_host, ctx->layout.bytes, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s.chk_count, 0, 4, st));
-    gbh::launch_tile(s.chk_dd, ctx->gi, ctx->cfg.tile_log2, ctx->grids, st);
+    gbh::launch_tile(s.chk_dd, ctx->gi, ctx->tile_bits, ctx->tile_stage, ctx->grids, st);
     gbh::launch_large(s.chk_dd, ctx->grids, st);
     gbh::launch_map_compare(s.dd, s.chk_dd, s.chk_count, ctx->grids, st);
     ctx->launches += 3;

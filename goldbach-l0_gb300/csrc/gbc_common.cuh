@@ -74,7 +74,9 @@ struct BatchParams {
     uint32_t i_warp;          // primes [i0, i_warp): warp-cooperative marking
     uint32_t n_mid;           // primes [i_warp, n_mid): one thread per prime
     uint32_t n_all;           // primes [n_mid, n_all): large-prime kernel
-    uint32_t tile_log2;
+    uint32_t tile_log2;       // the single-run forms' tiles: 2^tile_log2 bits
+    uint32_t tile_bits;       // the batch kernels' tiles: bits per tile, a multiple of 128
+    uint32_t tile_rcp;        // ceil(2^32 / tile_bits): t / tile_bits by one multiply and a correction
     uint32_t tiles_pc;        // tiles per class array
     const uint32_t *pat;      // pattern words of the groups, back to back
     const uint32_t *skip_tab; // bit tables: multipliers to skip (1001 then 7429 bits)
@@ -103,6 +105,19 @@ struct BatchParams {
     uint32_t *ovf_cnt;
     uint32_t spin0;           // try_wait rounds of the first wait on a tile bin's bulk copies (kStageSpin)
 };
+
+// t / tile_bits for t < 2^31 (the estimate umulhi(t, rcp) is exact or one
+// too high)
+__host__ __device__ __forceinline__ uint32_t tile_of(uint32_t t, uint32_t tile_bits, uint32_t rcp)
+{
+#ifdef __CUDA_ARCH__
+    uint32_t q = __umulhi(t, rcp);
+#else
+    uint32_t q = uint32_t((uint64_t(t) * rcp) >> 32);
+#endif
+    if (q * tile_bits > t) --q;
+    return q;
+}
 
 // a one-run batch whose hit lists go through the tile bins
 __host__ __device__ __forceinline__ bool hl_binned(const BatchParams &bp, uint32_t nrun)
@@ -391,8 +406,8 @@ struct Grids {
 };
 void launch_init(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
-void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
-                 cudaStream_t st);
+void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_bits, uint32_t stage,
+                 const Grids &g, cudaStream_t st);
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 // direct = false: the binned harvest (before the tiles); true: the direct
 // marks of every other batch (after the tiles)
@@ -406,7 +421,10 @@ void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, uint32_t tries, c
 void launch_count(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st);
 void launch_map_compare(const gbk::BatchDesc &a, const gbk::BatchDesc &b, uint32_t *count, const Grids &g,
                         cudaStream_t st);
-void tile_attributes(uint32_t tile_log2, const gbk::GroupInfo &gi);
+// the persistent tile kernel's shared memory for tile_bits-bit tiles; sets
+// *stage to the tile-bin offsets it can stage (0 when the tile leaves no room)
+// and returns false when the tile itself does not fit
+bool tile_attributes(uint32_t tile_bits, uint32_t tile_log2, const gbk::GroupInfo &gi, int device, uint32_t *stage);
 void query_check_grids(Grids &g);
 void query_count_grids(Grids &g);
 uint32_t check_vbx(uint64_t evens, int sm);

@@ -106,6 +106,8 @@ struct gbc_ctx {
     // prime-multiplier table (hit lists for the primes >= p_hl)
     bool hl_on = false;
     uint64_t p_hl = 0;
+    uint32_t tile_bits = 0;   // bits per tile of the persistent tile kernel
+    uint32_t tile_stage = 0;  // tile-bin offsets it stages into shared memory
     uint32_t n_hl = 0;                 // index of the first prime >= p_hl
     uint32_t *mtab = nullptr;          // wheel-30 bytes of the primes in [mtab_m0, mtab_m1]
     uint64_t mtab_m0 = 0, mtab_m1 = 0, mtab_bytes = 0;

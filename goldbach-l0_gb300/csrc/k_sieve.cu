@@ -138,21 +138,24 @@ __device__ __forceinline__ uint32_t local_start(uint32_t x, uint32_t t0, uint32_
     return rem ? p - rem : 0;
 }
 
-// Tile-bin staging of the persistent tile kernel: the first kTbStage
-// offsets of an item's tile bin go into shared memory by bulk copies issued
-// at the item's start (they land while the CTA sieves), the rest is
-// prefetched into L2 by the TMA unit and read from there.
+// Tile-bin staging of the persistent tile kernel: the first `cap` offsets
+// of an item's tile bin (cap: what the shared memory beside the tile holds,
+// up to kTbStage, a multiple of kTbPiece, possibly 0) go into shared memory
+// by bulk copies issued at the item's start (they land while the CTA
+// sieves), the rest is prefetched into L2 by the TMA unit and read from
+// there.
 constexpr uint32_t kTbStage = 20480;       // offsets (80 KB), a multiple of kTbPiece
 constexpr uint32_t kTbPiece = 4096;        // offsets per bulk copy (16 KB)
 
-// thread 0 at an item's start: stages the first min(n, kTbStage) offsets of
-// the tile bin e (n offsets; the copy rounded up to 16 bytes, which stays in
-// the bin: capacities are multiples of 32 offsets) into stg, completing on
-// bar, and prefetches the rest into L2. Returns the offsets staged.
-__device__ __forceinline__ uint32_t stage_tile_bin(uint32_t *stg, uint64_t *bar, const uint32_t *e, uint32_t n)
+// thread 0 at an item's start: stages the first min(n, cap) offsets of the
+// tile bin e (n offsets; the copy rounded up to 16 bytes, which stays in the
+// bin: capacities are multiples of 32 offsets) into stg, completing on bar,
+// and prefetches the rest into L2. Returns the offsets staged.
+__device__ __forceinline__ uint32_t stage_tile_bin(uint32_t *stg, uint64_t *bar, const uint32_t *e, uint32_t n,
+                                                   uint32_t cap)
 {
-    const uint32_t staged = min(n, kTbStage);
-    if (n > kTbStage) bulk_prefetch_l2(e + kTbStage, ((n - kTbStage + 3u) & ~3u) * 4u);
+    const uint32_t staged = min(n, cap);
+    if (n > cap) bulk_prefetch_l2(e + cap, ((n - cap + 3u) & ~3u) * 4u);
     if (!staged) return 0;
     const uint32_t words = (staged + 3u) & ~3u;
     fence_proxy_async();  // the CTA's earlier reads of stg before the copies
@@ -163,18 +166,19 @@ __device__ __forceinline__ uint32_t stage_tile_bin(uint32_t *stg, uint64_t *bar,
 }
 
 // Sieves bits [t0, t0 + tl) of class array k of a run in shared memory s
-// (the group patterns already in pat) and stores them. tl is a multiple of
-// 128 bits. Ends with the CTA synchronized, s free for the next tile.
+// (the group patterns already in pat) and stores them: tile ti of the class
+// array, tb bits per tile (the buffer s holds tb bits), tl <= tb a multiple
+// of 128 bits. Ends with the CTA synchronized, s free for the next tile.
 // kVec4: the context's own prime and reciprocal arrays (16-byte aligned,
 // padded by 4 words), read four at a time, and the tile bin staged by
-// stage_tile_bin (*nb offsets, the first min(*nb, kTbStage) in stg once bar
+// stage_tile_bin (*nb offsets, the first min(*nb, cap) in stg once bar
 // completes the phase of parity bit 0 of phase); otherwise any arrays and
 // the tile bin read from global memory.
 template <bool kVec4>
 __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo &gi, const uint32_t *pat,
-                                          uint32_t *s, uint32_t k, uint32_t t0, uint32_t tl,
-                                          const uint32_t *stg = nullptr, uint64_t *bar = nullptr,
-                                          uint32_t *phase = nullptr, const uint32_t *nb = nullptr)
+                                          uint32_t *s, uint32_t k, uint32_t ti, uint32_t t0, uint32_t tl,
+                                          uint32_t tb, const uint32_t *stg = nullptr, uint64_t *bar = nullptr,
+                                          uint32_t *phase = nullptr, const uint32_t *nb = nullptr, uint32_t cap = 0)
 {
     const uint32_t tid = threadIdx.x, bs = blockDim.x;
     const uint32_t tw = tl >> 5;
@@ -279,9 +283,12 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
             m = mn;
         }
     }
-    // a binned batch: the hit-list marks of this tile (offsets within it)
+    // a binned batch: the hit-list marks of this tile (offsets within it,
+    // clamped to the tile buffer: a stale staged word or a damaged bin can
+    // clear a wrong bit, never touch memory outside s)
+    const uint32_t omax = tb - 1;
     if constexpr (kVec4) {
-        const uint32_t n = *nb, staged = min(n, kTbStage);
+        const uint32_t n = *nb, staged = min(n, cap);
         if (staged) {
             bool ok = mbar_wait(bar, *phase & 1u, bp.spin0);
             if (!ok) {
@@ -289,23 +296,20 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
                 ok = mbar_wait(bar, *phase & 1u);
             }
             *phase ^= 1u;
-            // offsets masked to the tile: a copy that missed its wait can
-            // leave stale words, never an access outside s
-            const uint32_t msk = (1u << bp.tile_log2) - 1u;
             const uint4 *v4 = reinterpret_cast<const uint4 *>(stg);
             for (uint32_t i = tid; ok && 4 * i < staged; i += bs) {
                 const uint4 v = v4[i];
                 const uint32_t at = 4 * i;
-                atomicAnd(&s[(v.x & msk) >> 5], ~(1u << (v.x & 31)));
-                if (at + 1 < staged) atomicAnd(&s[(v.y & msk) >> 5], ~(1u << (v.y & 31)));
-                if (at + 2 < staged) atomicAnd(&s[(v.z & msk) >> 5], ~(1u << (v.z & 31)));
-                if (at + 3 < staged) atomicAnd(&s[(v.w & msk) >> 5], ~(1u << (v.w & 31)));
+                atomicAnd(&s[min(v.x, omax) >> 5], ~(1u << (v.x & 31)));
+                if (at + 1 < staged) atomicAnd(&s[min(v.y, omax) >> 5], ~(1u << (v.y & 31)));
+                if (at + 2 < staged) atomicAnd(&s[min(v.z, omax) >> 5], ~(1u << (v.z & 31)));
+                if (at + 3 < staged) atomicAnd(&s[min(v.w, omax) >> 5], ~(1u << (v.w & 31)));
             }
         }
-        if (n > kTbStage) {
+        if (n > cap) {
             // the rest from L2, four groups of four per thread in flight
-            const uint32_t tile = k * bp.tiles_pc + (t0 >> bp.tile_log2), m = n - kTbStage;
-            const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap + kTbStage);
+            const uint32_t tile = k * bp.tiles_pc + ti, m = n - cap;
+            const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap + cap);
             for (uint32_t i = tid; 4 * i < m; i += 4 * bs) {
                 uint4 v[4];
 #pragma unroll
@@ -316,15 +320,15 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 #pragma unroll
                 for (uint32_t u = 0; u < 4; ++u) {
                     const uint32_t at = 4 * (i + u * bs);
-                    if (at < m) atomicAnd(&s[v[u].x >> 5], ~(1u << (v[u].x & 31)));
-                    if (at + 1 < m) atomicAnd(&s[v[u].y >> 5], ~(1u << (v[u].y & 31)));
-                    if (at + 2 < m) atomicAnd(&s[v[u].z >> 5], ~(1u << (v[u].z & 31)));
-                    if (at + 3 < m) atomicAnd(&s[v[u].w >> 5], ~(1u << (v[u].w & 31)));
+                    if (at < m) atomicAnd(&s[min(v[u].x, omax) >> 5], ~(1u << (v[u].x & 31)));
+                    if (at + 1 < m) atomicAnd(&s[min(v[u].y, omax) >> 5], ~(1u << (v[u].y & 31)));
+                    if (at + 2 < m) atomicAnd(&s[min(v[u].z, omax) >> 5], ~(1u << (v[u].z & 31)));
+                    if (at + 3 < m) atomicAnd(&s[min(v[u].w, omax) >> 5], ~(1u << (v[u].w & 31)));
                 }
             }
         }
     } else if (bp.tb_cap && bp.hl_quota) {
-        const uint32_t tile = k * bp.tiles_pc + (t0 >> bp.tile_log2);
+        const uint32_t tile = k * bp.tiles_pc + ti;
         const uint32_t n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
         const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap);
         // four groups of four per thread in flight before their marks
@@ -338,10 +342,10 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 #pragma unroll
             for (uint32_t u = 0; u < 4; ++u) {
                 const uint32_t at = 4 * (i + u * bs);
-                if (at < n) atomicAnd(&s[v[u].x >> 5], ~(1u << (v[u].x & 31)));
-                if (at + 1 < n) atomicAnd(&s[v[u].y >> 5], ~(1u << (v[u].y & 31)));
-                if (at + 2 < n) atomicAnd(&s[v[u].z >> 5], ~(1u << (v[u].z & 31)));
-                if (at + 3 < n) atomicAnd(&s[v[u].w >> 5], ~(1u << (v[u].w & 31)));
+                if (at < n) atomicAnd(&s[min(v[u].x, omax) >> 5], ~(1u << (v[u].x & 31)));
+                if (at + 1 < n) atomicAnd(&s[min(v[u].y, omax) >> 5], ~(1u << (v[u].y & 31)));
+                if (at + 2 < n) atomicAnd(&s[min(v[u].z, omax) >> 5], ~(1u << (v[u].z & 31)));
+                if (at + 3 < n) atomicAnd(&s[min(v[u].w, omax) >> 5], ~(1u << (v[u].w & 31)));
             }
         }
     }
@@ -353,16 +357,16 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 }
 
 // Persistent tile kernel: CTAs take the batch's (run, class, tile) items
-// from a work counter; a run's last tile of a class ends at its class
-// array's end.
-__global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tile_log2)
+// from a work counter; tiles of tb bits (a multiple of 128), a run's last
+// tile of a class ends at its class array's end; up to `cap` offsets of each
+// tile bin staged into shared memory.
+__global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tb, uint32_t cap)
 {
     // shared memory: the tile, the tile-bin staging buffer, the patterns
     extern __shared__ __align__(16) uint32_t sm_tile[];
-    const uint32_t tb = 1u << tile_log2;
     uint32_t *s = sm_tile;
     uint32_t *stg = sm_tile + (tb >> 5);
-    uint32_t *pat = stg + kTbStage;
+    uint32_t *pat = stg + cap;
     const uint32_t nrun = d.h->nrun, items = d.h->tile_items;
     if (!nrun) return;
     __shared__ uint32_t s_j, s_nb;
@@ -379,18 +383,18 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uin
         const uint32_t r = find_prefix(d.tile_pref, nrun, j);
         const BatchParams &bp = d.runs[r];
         const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
-        const uint32_t k = local / tpc, t0 = (local - k * tpc) << tile_log2;
+        const uint32_t k = local / tpc, ti = local - k * tpc, t0 = ti * tb;
         const uint32_t tl = min(tb, bp.wpc * 32 - t0);
         if (threadIdx.x == 0) {
             uint32_t n = 0;
             if (bp.tb_cap && bp.hl_quota) {
-                const uint32_t tile = k * tpc + (t0 >> bp.tile_log2);
+                const uint32_t tile = k * tpc + ti;
                 n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
-                stage_tile_bin(stg, &s_bar, bp.tb_buf + size_t(tile) * bp.tb_cap, n);
+                stage_tile_bin(stg, &s_bar, bp.tb_buf + size_t(tile) * bp.tb_cap, n, cap);
             }
             s_nb = n;
         }
-        tile_body<true>(bp, gi, pat, s, k, t0, tl, stg, &s_bar, &phase, &s_nb);
+        tile_body<true>(bp, gi, pat, s, k, ti, t0, tl, tb, stg, &s_bar, &phase, &s_nb, cap);
     }
 }
 
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(1024, 1) k_tile1(BatchParams bp, GroupInfo gi)
     uint32_t *pat = sm + (tb >> 5);
     for (uint32_t i = threadIdx.x; i < gi.words; i += blockDim.x) pat[i] = bp.pat[i];
     __syncthreads();
-    tile_body<false>(bp, gi, pat, sm, blockIdx.y, blockIdx.x << bp.tile_log2, tb);
+    tile_body<false>(bp, gi, pat, sm, blockIdx.y, blockIdx.x, blockIdx.x << bp.tile_log2, tb, tb);
 }
 
 // Marks class k's multiples p m of the run, m coprime to 30 and to 7..23,
@@ -698,7 +702,7 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
     const BatchParams &bp = d.runs[0];
     const uint32_t tid = threadIdx.x, bs = blockDim.x;
     const uint32_t quota = bp.hl_quota, nreg = bp.hl_nreg, nbin = 8 * nreg, ctas = bp.hl_ctas;
-    const uint32_t rlog = bp.hl_rlog, tl2 = bp.tile_log2, tpr = 1u << (rlog - tl2), tmask = (1u << tl2) - 1u;
+    const uint32_t rlog = bp.hl_rlog, tb = bp.tile_bits, rcp = bp.tile_rcp;
     const uint32_t items = nbin * ctas, cap = bp.tb_cap;
     for (;;) {
         const uint32_t j = next_item(d.work + kWorkBinsort, &s_j);
@@ -707,7 +711,13 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
         const uint32_t k = bin / nreg, reg = bin - k * nreg;
         const uint32_t n = min(bp.hl_cnt[size_t(c) * nbin + bin], quota);
         const uint32_t *e = bp.hl_buf + (size_t(c) * nbin + bin) * quota;
-        const uint32_t tile0 = k * bp.tiles_pc + (reg << (rlog - tl2));
+        // the region's bits [rb, rb + 2^rlog) meet tiles ti0 .. ti0 + tpr - 1
+        // of the class array (tiles may straddle regions: their bins are
+        // filled by every region that meets them)
+        const uint32_t rb = reg << rlog;
+        const uint32_t ti0 = tile_of(rb, tb, rcp);
+        const uint32_t tpr = tile_of(min(rb + ((1u << rlog) - 1u), bp.wpc * 32 - 1), tb, rcp) - ti0 + 1;
+        const uint32_t tile0 = k * bp.tiles_pc + ti0;
         for (uint32_t cs = 0; cs < n; cs += kSortChunk) {
             const uint32_t m = min(n - cs, kSortChunk);
             for (uint32_t t = tid; t < tpr; t += bs) s_cnt[t] = 0;
@@ -724,9 +734,15 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
                 v[4 * u + 3] = 4 * g + 3 < m ? q.w : kNone;
             }
             __syncthreads();
+            // each offset as (tile of the region, bit in the tile): t - ti0 in
+            // the top 11 bits, the bit (< tb <= 2^21) in the low 21
 #pragma unroll
             for (uint32_t u = 0; u < kSortPer; ++u)
-                if (v[u] != kNone) atomicAdd(&s_cnt[v[u] >> tl2], 1u);
+                if (v[u] != kNone) {
+                    const uint32_t t = rb + v[u], ti = tile_of(t, tb, rcp);
+                    v[u] = ((ti - ti0) << 21) | (t - ti * tb);
+                    atomicAdd(&s_cnt[v[u] >> 21], 1u);
+                }
             __syncthreads();
             block_excl_scan4(s_cnt, s_start, tpr, s_wsum);
             __syncthreads();
@@ -738,13 +754,13 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
             __syncthreads();
 #pragma unroll
             for (uint32_t u = 0; u < kSortPer; ++u)
-                if (v[u] != kNone) s_out[atomicAdd(&s_cnt[v[u] >> tl2], 1u)] = v[u];
+                if (v[u] != kNone) s_out[atomicAdd(&s_cnt[v[u] >> 21], 1u)] = v[u];
             __syncthreads();
             for (uint32_t i = tid; i < m; i += bs) {
-                const uint32_t off = s_out[i], t = off >> tl2;
+                const uint32_t off = s_out[i], t = off >> 21, bit = off & ((1u << 21) - 1u);
                 const uint32_t pos = s_gbase[t] + (i - s_start[t]);
-                if (pos < cap) bp.tb_buf[size_t(tile0 + t) * cap + pos] = off & tmask;
-                else ovf_push(bp, k, (reg << rlog) + off);
+                if (pos < cap) bp.tb_buf[size_t(tile0 + t) * cap + pos] = bit;
+                else ovf_push(bp, k, (ti0 + t) * tb + bit);
             }
             __syncthreads();
         }
@@ -823,22 +839,35 @@ void launch_map_compare(const gbk::BatchDesc &a, const gbk::BatchDesc &b, uint32
     gbk::k_map_compare<<<g.sm * 8, 256, 0, st>>>(a, b, count);
 }
 
-static size_t tile_smem(uint32_t tile_log2, const gbk::GroupInfo &gi)
+static size_t tile_smem(uint32_t tile_bits, const gbk::GroupInfo &gi)
 {
-    return size_t(((1u << tile_log2) >> 5) + gi.words) * 4;
+    return size_t((tile_bits >> 5) + gi.words) * 4;
 }
 
-// the persistent tile kernel adds the tile-bin staging buffer
-static size_t tile_smem_staged(uint32_t tile_log2, const gbk::GroupInfo &gi)
+// the persistent tile kernel adds the tile-bin staging buffer (stage offsets)
+static size_t tile_smem_staged(uint32_t tile_bits, uint32_t stage, const gbk::GroupInfo &gi)
 {
-    return tile_smem(tile_log2, gi) + size_t(gbk::kTbStage) * 4;
+    return tile_smem(tile_bits, gi) + size_t(stage) * 4;
 }
 
-void tile_attributes(uint32_t tile_log2, const gbk::GroupInfo &gi)
+bool tile_attributes(uint32_t tile_bits, uint32_t tile_log2, const gbk::GroupInfo &gi, int device, uint32_t *stage)
 {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, gbk::k_tile);
+    const size_t room = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0;
+    const size_t base = tile_smem(tile_bits, gi);
+    if (base > room) return false;
+    // the staging buffer in whole bulk-copy pieces, as much as fits, at most kTbStage
+    size_t st = (room - base) / 4 / gbk::kTbPiece * gbk::kTbPiece;
+    if (st > gbk::kTbStage) st = gbk::kTbStage;
+    *stage = uint32_t(st);
     cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(tile_smem_staged(tile_log2, gi)));
-    cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tile_smem(tile_log2, gi)));
+                         int(tile_smem_staged(tile_bits, *stage, gi)));
+    cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(tile_smem(1u << tile_log2, gi)));
+    return true;
 }
 
 void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
@@ -846,10 +875,10 @@ void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
     gbk::k_xfirst<<<g.sm * 8, 256, 0, st>>>(d);
 }
 
-void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_log2, const Grids &g,
-                 cudaStream_t st)
+void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_bits, uint32_t stage,
+                 const Grids &g, cudaStream_t st)
 {
-    gbk::k_tile<<<g.sm, 1024, tile_smem_staged(tile_log2, gi), st>>>(d, gi, tile_log2);
+    gbk::k_tile<<<g.sm, 1024, tile_smem_staged(tile_bits, stage, gi), st>>>(d, gi, tile_bits, stage);
 }
 
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
@@ -893,7 +922,7 @@ void launch_xfirst1(const gbk::BatchParams &bp, cudaStream_t st)
 void launch_tile1(const gbk::BatchParams &bp, const gbk::GroupInfo &gi, cudaStream_t st)
 {
     dim3 grid(bp.tiles_pc, 8);
-    gbk::k_tile1<<<grid, 1024, tile_smem(bp.tile_log2, gi), st>>>(bp, gi);
+    gbk::k_tile1<<<grid, 1024, tile_smem(1u << bp.tile_log2, gi), st>>>(bp, gi);
 }
 
 void launch_wheel_bytes(const gbk::BatchParams &bp, uint32_t *out, cudaStream_t st)

@@ -43,7 +43,7 @@ class Config(C.Structure):
                 ("mtab_max_gb", C.c_uint32), ("nslots", C.c_uint32), ("sample_every", C.c_uint32),
                 ("plan_funnels", C.c_uint32), ("ridge_min", C.c_uint32), ("launch_mode", C.c_uint32),
                 ("selfcheck_every", C.c_uint32), ("verify_funnels", C.c_uint32), ("hl_cap_pct", C.c_uint32),
-                ("test_flags", C.c_uint32), ("reserved", C.c_uint32)]
+                ("test_flags", C.c_uint32), ("tile_bits", C.c_uint32)]
 
 
 class SegmentResult(C.Structure):
@@ -211,14 +211,14 @@ class Context:
     def __init__(self, limit, segment_even=DEFAULT_SEGMENT, max_batch=8, tile_log2=0, p_mid=0, want_pn=False,
                  device=0, max_runs=0, hl_mode=0, mtab_max_gb=0, nslots=0, sample_every=0,
                  plan_funnels=0, ridge_min=0, launch_mode=0, selfcheck_every=0, verify_funnels=0, hl_cap_pct=0,
-                 test_flags=0):
+                 test_flags=0, tile_bits=0):
         self.lib = load()
         cfg = Config(limit=limit, segment_even=segment_even, max_batch=max_batch, tile_log2=tile_log2,
                      p_mid=p_mid, want_pn=1 if want_pn else 0, device=device, max_runs=max_runs,
                      hl_mode=hl_mode, mtab_max_gb=mtab_max_gb, nslots=nslots,
                      sample_every=sample_every, plan_funnels=plan_funnels, ridge_min=ridge_min,
                      launch_mode=launch_mode, selfcheck_every=selfcheck_every, verify_funnels=verify_funnels,
-                     hl_cap_pct=hl_cap_pct, test_flags=test_flags)
+                     hl_cap_pct=hl_cap_pct, test_flags=test_flags, tile_bits=tile_bits)
         h = C.c_void_p()
         rc = self.lib.gbc_create(C.byref(cfg), C.byref(h))
         self.h = h

@@ -63,7 +63,7 @@ typedef struct gbc_config {
     uint64_t limit;          /* largest even any batch will reach: sizes the sieving primes */
     uint64_t segment_even;   /* integer span of a full segment (default 467.5M) */
     uint32_t max_batch;      /* segments per batch the slots are sized for (default 8, at most 256) */
-    uint32_t tile_log2;      /* log2 of shared-memory tile bits per class (14..20, default 20) */
+    uint32_t tile_log2;      /* log2 of shared-memory tile bits per class (14..20, default 20); see tile_bits */
     uint32_t p_mid;          /* primes <= p_mid: shared-memory tiles; above: large-prime kernel (default 2^22) */
     uint32_t want_pn;        /* 1: slots also hold a per-even u16 p(n) buffer */
     int32_t device;          /* CUDA device ordinal (default 0) */
@@ -97,7 +97,8 @@ typedef struct gbc_config {
                                 (default 100; lower values make marks take the overflow list, which
                                 is cleared after the tiles: for tests of that path) */
     uint32_t test_flags;     /* 0 in production; GBC_TEST_* below, for tests of the failure paths */
-    uint32_t reserved;
+    uint32_t tile_bits;      /* bits per shared-memory tile of a class array when set: a multiple of
+                                4096 in [2^14, 1835008] (up to 224 KB of shared memory); 0: 2^tile_log2 */
 } gbc_config;
 
 /* test_flags: each makes a bounded device wait run out, so a test sees the

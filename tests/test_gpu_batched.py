@@ -101,6 +101,28 @@ def test_map_selfcheck_runs_and_passes():
     assert line == oracle.stats_line(a, b, oracle.SIEVE)
 
 
+@pytest.mark.parametrize("tile_bits", [1835008, 1572864])
+def test_tiles_across_hit_list_regions_selfcheck(tile_bits):
+    """Tiles of any size (not a power of two) in a one-run batch of 20
+    production segments at 4e18: each class array spans two hit-list regions
+    of 2^28 bits, a tile straddles their border, and its bin is filled from
+    both. The maps equal the rebuild without hit lists word for word
+    (self-check), and the map hash of three segments equals the oracle's."""
+    seg = 467_500_000
+    a = 4000008233142500000
+    segs = [(a + i * seg, a + (i + 1) * seg - 2) for i in range(20)]
+    limit = segs[-1][1]
+    with gbc.Context(limit=limit, segment_even=seg, max_batch=20, p_mid=1 << 21, mtab_max_gb=96, hl_mode=1,
+                     tile_bits=tile_bits, selfcheck_every=1) as c:
+        c.enqueue_batch(0, segs, limit, [0] + [gbc.SEG_VERIFY] * 19)
+        res, _ = c.collect(0, 20)
+        assert c.stats().selfchecks == 1 and c.stats().p_hl > 0
+    nblk = (segs[-1][1] + 3 - (a - 9781) // 30 * 30) // 30 + 1
+    assert nblk > 1 << 28
+    for r in (res[0], res[9], res[19]):
+        assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi)
+
+
 def test_prepare_builds_the_table_once():
     with gbc.Context(limit=5 * 10**18, segment_even=1_000_000, max_batch=4, hl_mode=1, mtab_max_gb=16) as c:
         c.prepare(10**16, 5 * 10**18)

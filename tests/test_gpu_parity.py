@@ -75,16 +75,19 @@ def test_segment_hash_and_counts_match_oracle(ctx):
 U30 = [1, 7, 11, 13, 17, 19, 23, 29]
 
 
-@pytest.mark.parametrize("a,tile_log2", [(10**12, 20), (4 * 10**18, 16), (6, 18), (9223372036853775808, 20),
-                                         (gbc.MAX_LIMIT - 2_000_000, 20)])
-def test_class_map_bit_exact(a, tile_log2):
+@pytest.mark.parametrize("a,tile_log2,tile_bits", [(10**12, 20, 0), (4 * 10**18, 16, 0), (6, 18, 0),
+                                                   (9223372036853775808, 20, 0), (gbc.MAX_LIMIT - 2_000_000, 20, 0),
+                                                   (10**12, 20, 1835008), (4 * 10**18, 20, 1572864),
+                                                   (9223372036853775808, 20, 1835008), (6, 20, 53248)])
+def test_class_map_bit_exact(a, tile_log2, tile_bits):
     """Every bit of a batch's class map against Miller-Rabin (the
     reference's debug_map validator): the sieve stages may not lose or add a
     mark anywhere, including q < 67 at the bottom and 2^64 - 2^40 at the top."""
     seg = 500_000
     b = a + 2 * seg - 2
     segs = gbc.segments_of(a, b, seg)
-    with gbc.Context(limit=b, segment_even=seg, max_batch=len(segs), tile_log2=tile_log2, p_mid=1 << 18) as c:
+    with gbc.Context(limit=b, segment_even=seg, max_batch=len(segs), tile_log2=tile_log2, tile_bits=tile_bits,
+                     p_mid=1 << 18) as c:
         c.enqueue_batch(0, segs, b)
         c.collect(0, len(segs))
         base, nblk, wpc, w = c.map(0)
