@@ -463,17 +463,30 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
         }
     }
     ctx->gi.words = uint32_t(pat.size());
-    // multiplier skip bits and inverses (mod 1001, mod 7429)
-    std::vector<uint32_t> skip((gbk::kSkip1 + 31) / 32 + (gbk::kSkip2 + 31) / 32, 0);
-    std::vector<uint16_t> inv(gbk::kSkip1 + gbk::kSkip2, 0);
-    for (uint32_t m = 0; m < gbk::kSkip1; ++m) {
-        if (m % 7 == 0 || m % 11 == 0 || m % 13 == 0) skip[m / 32] |= 1u << (m % 32);
-        inv[m] = uint16_t(inv_mod_small(m, gbk::kSkip1));
-    }
-    const uint32_t w1 = (gbk::kSkip1 + 31) / 32;
-    for (uint32_t m = 0; m < gbk::kSkip2; ++m) {
-        if (m % 17 == 0 || m % 19 == 0 || m % 23 == 0) skip[w1 + m / 32] |= 1u << (m % 32);
-        inv[gbk::kSkip1 + m] = uint16_t(inv_mod_small(m, gbk::kSkip2));
+    // the large primes' multiplier wheel mod 1001 = 7 * 11 * 13: per residue
+    // x the rank of the first unit >= x (wrapping) | its distance << 10, the
+    // gaps between consecutive units, the inverses mod 1001, the inverses mod
+    // each of 17..43 (k_large)
+    std::vector<uint16_t> wheel;
+    {
+        std::vector<uint32_t> units;
+        for (uint32_t x = 0; x < gbk::kWheelM; ++x)
+            if (x % 7 && x % 11 && x % 13) units.push_back(x);
+        for (uint32_t x = 0; x < gbk::kWheelM; ++x) {
+            const auto it = std::lower_bound(units.begin(), units.end(), x);
+            const uint32_t rank = it == units.end() ? 0u : uint32_t(it - units.begin());
+            const uint32_t dist = it == units.end() ? units[0] + gbk::kWheelM - x : *it - x;
+            wheel.push_back(uint16_t(rank | dist << 10));
+        }
+        for (size_t r = 0; r < units.size(); ++r)
+            wheel.push_back(uint16_t(r + 1 < units.size() ? units[r + 1] - units[r] : units[0] + gbk::kWheelM - units[r]));
+        for (uint32_t x = 0; x < gbk::kWheelM; ++x) wheel.push_back(uint16_t(inv_mod_small(x, gbk::kWheelM)));
+        for (uint32_t f : {17u, 19u, 23u, 29u, 31u, 37u, 41u, 43u})
+            for (uint32_t x = 0; x < f; ++x) wheel.push_back(uint16_t(inv_mod_small(x, f)));
+        if (units.size() != 720 || wheel.size() != gbk::kWheelTabWords) {
+            *out = ctx;
+            return fail(ctx, GBC_E_ARG, "wheel table size");
+        }
     }
     // candidates and their per-class lists (useful: r - p coprime to 30)
     std::vector<uint32_t> c32 = gbh_odd_primes_upto(GBC_MAX_CAND);
@@ -555,10 +568,31 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     if (!magic.empty()) CK(cudaMemcpy(ctx->d_magic, magic.data(), magic.size() * 4, cudaMemcpyHostToDevice));
     CK(dev_alloc(ctx, &ctx->d_pat, pat.size() * 4));
     CK(cudaMemcpy(ctx->d_pat, pat.data(), pat.size() * 4, cudaMemcpyHostToDevice));
-    CK(dev_alloc(ctx, &ctx->d_skip, skip.size() * 4));
-    CK(cudaMemcpy(ctx->d_skip, skip.data(), skip.size() * 4, cudaMemcpyHostToDevice));
-    CK(dev_alloc(ctx, &ctx->d_inv, inv.size() * 2));
-    CK(cudaMemcpy(ctx->d_inv, inv.data(), inv.size() * 2, cudaMemcpyHostToDevice));
+    CK(dev_alloc(ctx, &ctx->d_wheel, wheel.size() * 2));
+    CK(cudaMemcpy(ctx->d_wheel, wheel.data(), wheel.size() * 2, cudaMemcpyHostToDevice));
+    // the large primes from n_mid on, one byte each: (p_i - p_(i-1)) / 2, 0
+    // at the start of each group of kPackGroup, whose first prime is kept
+    // whole (pack_large_primes, src/host_math.cpp:187-209)
+    {
+        const size_t n = pr.size() > ctx->n_mid ? pr.size() - ctx->n_mid : 0;
+        const size_t groups = std::max<size_t>((n + gbk::kPackGroup - 1) / gbk::kPackGroup, 1);
+        std::vector<uint8_t> gap(groups * gbk::kPackGroup, 0);
+        std::vector<uint32_t> gbase(groups, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const uint32_t p = pr[ctx->n_mid + i];
+            if (i % gbk::kPackGroup == 0) {
+                gbase[i / gbk::kPackGroup] = p;
+                continue;
+            }
+            const uint32_t g = p - pr[ctx->n_mid + i - 1];
+            if ((g & 1) || g / 2 > 255) return fail(ctx, GBC_E_ARG, "a prime gap does not fit the packed stream");
+            gap[i] = uint8_t(g / 2);
+        }
+        CK(dev_alloc(ctx, &ctx->d_pk_gap, gap.size()));
+        CK(cudaMemcpy(ctx->d_pk_gap, gap.data(), gap.size(), cudaMemcpyHostToDevice));
+        CK(dev_alloc(ctx, &ctx->d_pk_base, gbase.size() * 4));
+        CK(cudaMemcpy(ctx->d_pk_base, gbase.data(), gbase.size() * 4, cudaMemcpyHostToDevice));
+    }
     CK(dev_alloc(ctx, &ctx->d_cand, cand.size() * 2));
     CK(cudaMemcpy(ctx->d_cand, cand.data(), cand.size() * 2, cudaMemcpyHostToDevice));
     CK(dev_alloc(ctx, &ctx->d_list, list.size() * 2));
@@ -634,8 +668,9 @@ extern "C" void gbc_destroy(gbc_ctx *ctx)
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_magic);
     cudaFree(ctx->d_pat);
-    cudaFree(ctx->d_skip);
-    cudaFree(ctx->d_inv);
+    cudaFree(ctx->d_wheel);
+    cudaFree(ctx->d_pk_gap);
+    cudaFree(ctx->d_pk_base);
     cudaFree(ctx->d_cand);
     cudaFree(ctx->d_list);
     delete ctx;
@@ -711,6 +746,14 @@ extern "C" int gbc_get_stats(const gbc_ctx *ctx, gbc_ctx_stats *out)
     return GBC_OK;
 }
 
+// the run base's residues the large-prime kernel's wheel and skip lanes start from
+static void set_residues(gbk::BatchParams &bp)
+{
+    bp.bm1 = uint32_t(bp.base % gbk::kWheelM);
+    const uint32_t f[8] = {17, 19, 23, 29, 31, 37, 41, 43};
+    for (int j = 0; j < 8; ++j) bp.bres[j] = uint8_t(bp.base % f[j]);
+}
+
 // One run (class map) of a batch: geometry, primes that reach it, and the
 // shared tables (the reference's segment_geometry / class_geometry,
 // src/host_math.cpp:13-78, for one map per run).
@@ -730,16 +773,17 @@ static void plan_run(const gbc_ctx *ctx, gbk::BatchParams &bp, uint64_t s0, uint
     bp.primes = ctx->d_primes;
     bp.magic = ctx->d_magic;
     bp.pat = ctx->d_pat;
-    bp.skip_tab = ctx->d_skip;
-    bp.inv_tab = ctx->d_inv;
+    bp.wheel = ctx->d_wheel;
+    bp.pk_gap = ctx->d_pk_gap;
+    bp.pk_base = ctx->d_pk_base;
+    bp.pk_i0 = ctx->n_mid;
     const uint64_t root = isqrt64(bp.qmax);
     bp.n_all = uint32_t(std::upper_bound(pr.begin(), pr.end(), root) - pr.begin());
     bp.i0 = std::min(ctx->i0, bp.n_all);
     bp.n_mid = std::max(std::min(ctx->n_mid, bp.n_all), bp.i0);
     bp.i_warp = std::min(std::max(ctx->i_warp, bp.i0), bp.n_mid);
     bp.n_hl = ctx->hl_on ? std::min(std::max(ctx->n_hl, bp.n_mid), bp.n_all) : bp.n_all;
-    bp.bm1 = uint32_t(bp.base % gbk::kSkip1);
-    bp.bm2 = uint32_t(bp.base % gbk::kSkip2);
+    set_residues(bp);
 }
 
 // Fills the descriptor prefix arrays and header counts from its runs and
@@ -952,8 +996,10 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
         bb.magic = ctx->d_magic;
         bb.xfirst = xf;
         bb.pat = ctx->d_pat;
-        bb.skip_tab = ctx->d_skip;
-        bb.inv_tab = ctx->d_inv;
+        bb.wheel = ctx->d_wheel;
+        bb.pk_gap = ctx->d_pk_gap;
+        bb.pk_base = ctx->d_pk_base;
+        bb.pk_i0 = ctx->n_mid;
         bb.err = ctx->slot[0].err;
         bb.spin0 = gbk::kStageSpin;
         const uint64_t root = isqrt64(bb.qmax);
@@ -962,8 +1008,7 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
         bb.n_mid = std::max(std::min(ctx->n_mid, bb.n_all), bb.i0);
         bb.i_warp = std::min(std::max(ctx->i_warp, bb.i0), bb.n_mid);
         bb.n_hl = bb.n_all;
-        bb.bm1 = uint32_t(bb.base % gbk::kSkip1);
-        bb.bm2 = uint32_t(bb.base % gbk::kSkip2);
+        set_residues(bb);
         img.h->nrun = 1;
         img.h->nseg = 0;
         finish_desc(ctx, img);

@@ -21,8 +21,12 @@ namespace gbk {
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kNumGroups = 7;         // small-prime pattern groups (primes 7..67)
 constexpr uint32_t kFirstSievePrime = 71;
-constexpr uint32_t kSkip1 = 1001;     // 7 * 11 * 13: large-prime multiplier skip
-constexpr uint32_t kSkip2 = 7429;     // 17 * 19 * 23
+constexpr uint32_t kWheelM = 1001;    // 7 * 11 * 13: the large-prime multiplier wheel
+// the wheel table: per residue the next unit's rank | distance << 10 (1001),
+// the 720 unit gaps, the inverses mod 1001 (1001), the inverses mod 17..43
+// back to back (240)
+constexpr uint32_t kWheelTabWords = 1001 + 720 + 1001 + 240;
+constexpr uint32_t kPackGroup = 256;  // packed large primes per group (one warp decodes a group)
 
 // u_k, the residue of class array k
 __host__ __device__ __forceinline__ uint32_t unit30(uint32_t k)
@@ -79,14 +83,17 @@ struct BatchParams {
     uint32_t tile_rcp;        // ceil(2^32 / tile_bits): t / tile_bits by one multiply and a correction
     uint32_t tiles_pc;        // tiles per class array
     const uint32_t *pat;      // pattern words of the groups, back to back
-    const uint32_t *skip_tab; // bit tables: multipliers to skip (1001 then 7429 bits)
-    const uint16_t *inv_tab;  // inverses mod 1001 then mod 7429 (0: none)
+    const uint16_t *wheel;    // the large primes' multiplier wheel (kWheelTabWords)
+    const uint8_t *pk_gap;    // packed large primes [pk_i0, ...): half gaps, 0 at each group start
+    const uint32_t *pk_base;  // the first prime of each group of kPackGroup
+    uint32_t pk_i0;           // index of the first packed prime
     uint32_t *err;            // device error word of the slot
     // prime-multiplier table: primes [n_hl, n_all) mark only p m with m prime
     uint32_t n_hl;            // first hit-listed prime (n_all: none)
     const uint32_t *mtab;     // bit k of byte i <-> m = m0 + 30 i + u_k is prime
     uint64_t m0, m1;          // the table covers m in [m0, m1]
-    uint32_t bm1, bm2;        // base mod 1001 and mod 7429
+    uint32_t bm1;             // base mod 1001
+    uint8_t bres[8];          // base mod 17, 19, 23, 29, 31, 37, 41, 43
     // binned hit lists (a batch of one run, hl_quota and tb_cap both set):
     // the harvest files each mark's offset in its (harvest CTA, region bin)
     // quota, bin = class * hl_nreg + (t >> hl_rlog); k_binsort moves them to

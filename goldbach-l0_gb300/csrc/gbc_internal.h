@@ -84,8 +84,10 @@ struct gbc_ctx {
     uint32_t i0 = 0, n_mid = 0, i_warp = 0;
     uint32_t wpc_cap = 0;              // class-array words of max_batch full segments in one run
     DescLayout layout;
-    uint32_t *d_primes = nullptr, *d_magic = nullptr, *d_pat = nullptr, *d_skip = nullptr;
-    uint16_t *d_inv = nullptr, *d_cand = nullptr, *d_list = nullptr;
+    uint32_t *d_primes = nullptr, *d_magic = nullptr, *d_pat = nullptr;
+    uint16_t *d_wheel = nullptr, *d_cand = nullptr, *d_list = nullptr;
+    uint8_t *d_pk_gap = nullptr;   // packed large primes from n_mid: half gaps
+    uint32_t *d_pk_base = nullptr; // and the first prime of each group
     uint2 *d_fun = nullptr, *d_fpair = nullptr;
     uint16_t *d_rest = nullptr;
     gbk::GroupInfo gi{};

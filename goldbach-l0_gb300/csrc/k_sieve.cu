@@ -12,12 +12,13 @@
 //             seven prime groups, then every prime 71..p_mid by shared-memory
 //             atomics (small primes warp-cooperatively, the rest one per
 //             thread); one coalesced store of the finished tile.
-//   k_large   primes above p_mid, one thread per prime and every run it
-//             reaches, marking every multiple p m (m coprime to 30) with a
-//             global atomic AND after a read (read-before-mark, goldbach.cl:
-//             328-336), skipping multipliers divisible by 7..23 whose
-//             multiples the pattern stage already cleared (the 30030 wheel
-//             and the 17..29 skip of goldbach.cl:638-748).
+//   k_large   primes in (p_mid, p_hl), streamed at one byte per prime and
+//             decoded by warps, every run they reach: every multiple p m (m
+//             coprime to 30) by a global atomic AND after a read
+//             (read-before-mark, goldbach.cl:328-336), stepping over the
+//             multipliers with a factor 7..43, whose multiples the pattern
+//             stage clears (the 30030 wheel and the 17..43 skip of
+//             goldbach.cl:638-748).
 //   k_hitlist the primes above p_hl through the prime-multiplier table.
 // A thread reads its prime once and applies it to every run of the batch,
 // so a batch of many short windows streams the sieving primes once.
@@ -409,99 +410,170 @@ __global__ void __launch_bounds__(1024, 1) k_tile1(BatchParams bp, GroupInfo gi)
     tile_body<false>(bp, gi, pat, sm, blockIdx.y, blockIdx.x, blockIdx.x << bp.tile_log2, tb, tb);
 }
 
-// Marks class k's multiples p m of the run, m coprime to 30 and to 7..23,
-// from class bit t on: read the word, clear with an atomic AND only if the
-// bit is still set.
-template <uint32_t K>
-__device__ __forceinline__ void large_walk(uint32_t *map, uint32_t wpc, uint32_t nblk, uint32_t t, uint32_t p,
-                                           uint32_t pi1, uint32_t pi2, uint32_t bm1, uint32_t bm2,
-                                           const uint32_t *s_skip)
+// The packed large-prime tier (the reference's pack_large_primes,
+// decode_large and large_packed_body, src/host_math.cpp:187-209,
+// kernels/goldbach.cl:1678-1829 with the wheel walk of 638-748, in this
+// repository's own form): the primes of [p_mid, p_hl) stream at one byte per
+// prime, a half gap (p_i - p_{i-1}) / 2, with the first prime of every group
+// of kPackGroup primes in a table of its own; a warp decodes a group (lane
+// l: eight primes, its gap bytes as one 8-byte load, the group's running sum
+// by a warp scan). Each prime then marks every run it reaches, class by
+// class: the multiples q = p m of class k are the bits t0, t0 + p, t0 + 2 p,
+// ... with m = m0 + 30 j. Multipliers with a factor 7, 11 or 13 are stepped
+// over by a wheel mod 7 * 11 * 13 = 1001 (720 steps in 1001; inside one class
+// array this is the reference's 30030 wheel, whose factor 30 the class
+// layout already holds); multipliers with a factor 17..43 are skipped by a
+// test of their residues, four 8-bit lanes per word. Either way q has a prime
+// factor the pattern stage clears. A mark reads the word and clears the bit
+// with an atomic AND only if it is still set.
+constexpr uint32_t kWheelUnits = 720;          // residues mod 1001 coprime to it
+constexpr uint32_t kSkipLanes1 = 0x1D171311u;  // 17, 19, 23, 29 as bytes
+constexpr uint32_t kSkipLanes2 = 0x2B29251Fu;  // 31, 37, 41, 43
+constexpr uint32_t kSkipBias1 = 0x63696D6Fu;   // 128 - 17, 128 - 19, 128 - 23, 128 - 29
+constexpr uint32_t kSkipBias2 = 0x55575B61u;   // 128 - 31, 128 - 37, 128 - 41, 128 - 43
+
+// per byte lane, (x + d) mod f for lanes x < f and d <= 4: add, then subtract
+// f where the sum reached f (the bias 128 - f carries that into bit 7)
+__device__ __forceinline__ uint32_t lanes_step(uint32_t x, uint32_t d, uint32_t f, uint32_t bias)
 {
-    constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
-    constexpr uint32_t u = (0x1D1713110D0B0701ull >> (8 * K)) & 0xFF;
-    if (t >= nblk) return;
-    uint32_t *wk = map + size_t(K) * wpc;
-    // multiplier m = q / p modulo 1001 and 7429: m = q p^-1, q = base + 30 t + u
-    uint32_t m1 = (bm1 + (30 * (t % kSkip1) + u) % kSkip1) % kSkip1 * pi1 % kSkip1;
-    uint32_t m2 = (bm2 + (30 * (t % kSkip2) + u) % kSkip2) % kSkip2 * pi2 % kSkip2;
+    x += d * 0x01010101u;
+    const uint32_t ge = ((x + bias) >> 7) & 0x01010101u;
+    return x - ((ge * 0xFFu) & f);
+}
+
+// nonzero iff some byte lane of x is zero
+__device__ __forceinline__ uint32_t lanes_zero(uint32_t x) { return (x - 0x01010101u) & ~x & 0x80808080u; }
+
+// Marks the multiples of p in one class array wk of nblk bits from bit t on.
+// c = m0 / 30 mod 1001 and the lanes r1 (17..29), r2 (31..43) = m0 / 30 mod
+// f for the multiplier m0 of bit t, so that m0 + 30 j has the factor f iff
+// (c + j) or lane f of r + j is 0 mod f. wheel[x], x < 1001: the rank of the
+// first unit >= x (wrapping) | its distance << 10; wheel[1001 + rank]: the
+// gap from that unit to the next.
+__device__ __forceinline__ void large_walk(uint32_t *wk, uint32_t nblk, uint32_t t, uint32_t p, uint32_t c,
+                                           uint32_t r1, uint32_t r2, const uint16_t *wheel)
+{
+    const uint32_t e = wheel[c];
+    uint32_t rank = e & 1023u;
+    const uint32_t d0 = e >> 10;
+    if (d0) {
+        if (uint64_t(nblk - t) <= uint64_t(d0) * p) return;
+        t += d0 * p;
+        r1 = lanes_step(r1, d0, kSkipLanes1, kSkipBias1);
+        r2 = lanes_step(r2, d0, kSkipLanes2, kSkipBias2);
+    }
     for (;;) {
-        const uint32_t sk = ((s_skip[m1 >> 5] >> (m1 & 31)) | (s_skip[kW1 + (m2 >> 5)] >> (m2 & 31))) & 1u;
-        if (!sk) {
+        if (!(lanes_zero(r1) | lanes_zero(r2))) {
             uint32_t *a = wk + (t >> 5);
             const uint32_t bit = 1u << (t & 31);
             if (__ldcg(a) & bit) atomicAnd(a, ~bit);
         }
-        if (nblk - t <= p) break;
-        t += p;
-        m1 += 30;
-        if (m1 >= kSkip1) m1 -= kSkip1;
-        m2 += 30;
-        if (m2 >= kSkip2) m2 -= kSkip2;
+        const uint32_t g = wheel[kWheelM + rank];
+        if (uint64_t(nblk - t) <= uint64_t(g) * p) break;
+        t += g * p;
+        rank = rank + 1 == kWheelUnits ? 0u : rank + 1;
+        r1 = lanes_step(r1, g, kSkipLanes1, kSkipBias1);
+        r2 = lanes_step(r2, g, kSkipLanes2, kSkipBias2);
     }
 }
 
-// The large primes [n_mid, n_hl) of every run: a thread per prime, the
-// runs in turn.
+// The packed large primes [n_mid, n_hl) of every run: a warp per group of
+// kPackGroup primes, a lane per eight of them, the runs in turn.
 __global__ void __launch_bounds__(256) k_large(BatchDesc d)
 {
-    __shared__ uint32_t s_skip[(kSkip1 + 31) / 32 + (kSkip2 + 31) / 32];
-    __shared__ uint16_t s_inv[kSkip1 + kSkip2];
-    constexpr uint32_t kW1 = (kSkip1 + 31) / 32;
+    __shared__ uint16_t s_wheel[kWheelTabWords];
     const uint32_t nrun = d.h->nrun;
     if (!nrun) return;
     const BatchParams &b0 = d.runs[0];
-    for (uint32_t i = threadIdx.x; i < kW1 + (kSkip2 + 31) / 32; i += blockDim.x) s_skip[i] = b0.skip_tab[i];
-    for (uint32_t i = threadIdx.x; i < kSkip1 + kSkip2; i += blockDim.x) s_inv[i] = b0.inv_tab[i];
+    // runs whose large range is empty may have n_mid below the stream's start
+    const uint32_t lo = max(d.h->n_mid_min, b0.pk_i0), hi = d.h->n_hl_max;
+    if (lo >= hi) return;
+    for (uint32_t i = threadIdx.x; i < kWheelTabWords; i += blockDim.x) s_wheel[i] = b0.wheel[i];
     __syncthreads();
-    const uint32_t *primes = b0.primes;
-    const uint32_t nhi = d.h->n_hl_max;
-    for (uint32_t i = d.h->n_mid_min + blockIdx.x * blockDim.x + threadIdx.x; i < nhi;
-         i += gridDim.x * blockDim.x) {
-        const uint32_t p = primes[i];
-        const float rp = __frcp_rn(float(p));
-        const uint32_t iv = inv30_mod(p);
-        const uint32_t d2 = addmod(iv, iv, p), d4 = addmod(d2, d2, p), d6 = addmod(d4, d2, p);
-        const uint32_t pi1 = s_inv[p % kSkip1], pi2 = s_inv[kSkip1 + p % kSkip2];
-        for (uint32_t ri = 0; ri < nrun; ++ri) {
-            const BatchParams &bp = d.runs[ri];
-            if (i < bp.n_mid || i >= bp.n_hl) continue;
-            const uint64_t base = bp.base;
-            const uint32_t nblk = bp.nblk, wpc = bp.wpc, bm1 = bp.bm1, bm2 = bp.bm2;
-            uint32_t *map = bp.map;
-            const uint32_t r = mod_u64(base, p, rp);
-            // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
-            const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
-            uint32_t c = iv;
-            uint32_t t[8];
+    const uint16_t *s_inv = s_wheel + kWheelM + kWheelUnits;  // x^-1 mod 1001 (0: none)
+    const uint16_t *s_invf = s_inv + kWheelM;                  // x^-1 mod f, f = 17..43 back to back
+    constexpr uint32_t kF[8] = {17, 19, 23, 29, 31, 37, 41, 43};
+    constexpr uint32_t kFo[8] = {0, 17, 36, 59, 88, 119, 156, 197};
+    const uint32_t lane = threadIdx.x & 31, i0 = b0.pk_i0;
+    const uint32_t g_lo = (lo - i0) / kPackGroup, g_hi = (hi - i0 + kPackGroup - 1) / kPackGroup;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t g = g_lo + wid; g < g_hi; g += nw) {
+        // decode: this lane's eight half gaps, plus the sums of the lanes below
+        const uint2 gv = __ldg(reinterpret_cast<const uint2 *>(b0.pk_gap) + size_t(g) * (kPackGroup / 8) + lane);
+        uint32_t sum = 0;
 #pragma unroll
-            for (uint32_t k = 0; k < 8; ++k) {
-                uint32_t x = tb - c;
-                if (tb < c) x += p;
-                t[k] = x;
-                const uint32_t dd = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
-                c = addmod(c, dd, p);
-            }
-            if (uint64_t(p) * p > base) {  // only near the bottom of the range
-                const uint64_t pp = uint64_t(p) * p;
+        for (uint32_t b = 0; b < 32; b += 8) sum += ((gv.x >> b) & 0xFFu) + ((gv.y >> b) & 0xFFu);
+        uint32_t incl = sum;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(~0u, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t p = __ldg(b0.pk_base + g) + 2u * (incl - sum);
+#pragma unroll 1
+        for (uint32_t u = 0; u < 8; ++u) {
+            p += 2u * (((u < 4 ? gv.x : gv.y) >> (8 * (u & 3))) & 0xFFu);
+            const uint32_t i = i0 + g * kPackGroup + lane * 8 + u;
+            if (i < lo || i >= hi) continue;
+            const float rp = __frcp_rn(float(p));
+            const uint32_t iv = inv30_mod(p);
+            const uint32_t d2 = addmod(iv, iv, p), d4 = addmod(d2, d2, p), d6 = addmod(d4, d2, p);
+            // (30 p)^-1 mod 1001 and mod each skip prime f
+            const uint32_t a1001 = s_inv[30u * (p % kWheelM) % kWheelM];
+            uint32_t af[8];
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j) af[j] = s_invf[kFo[j] + 30u * (p % kF[j]) % kF[j]];
+            for (uint32_t ri = 0; ri < nrun; ++ri) {
+                const BatchParams &bp = d.runs[ri];
+                if (i < bp.n_mid || i >= bp.n_hl) continue;
+                const uint64_t base = bp.base;
+                const uint32_t nblk = bp.nblk, wpc = bp.wpc;
+                const uint32_t r = mod_u64(base, p, rp);
+                // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
+                const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
+                uint32_t cc = iv;
+                uint32_t t[8];
 #pragma unroll
                 for (uint32_t k = 0; k < 8; ++k) {
-                    const uint64_t u = unit30(k);
-                    const uint64_t q = base + 30ull * t[k] + u;
-                    if (q < pp) {
-                        const uint64_t tmin = (pp - base - u + 29) / 30;
-                        const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
-                        t[k] = tt < nblk ? uint32_t(tt) : kNone;
+                    uint32_t x = tb - cc;
+                    if (tb < cc) x += p;
+                    t[k] = x;
+                    const uint32_t dd = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
+                    cc = addmod(cc, dd, p);
+                }
+                if (uint64_t(p) * p > base) {  // only near the bottom of the range
+                    const uint64_t pp = uint64_t(p) * p;
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; ++k) {
+                        const uint64_t uu = unit30(k);
+                        const uint64_t q = base + 30ull * t[k] + uu;
+                        if (q < pp) {
+                            const uint64_t tmin = (pp - base - uu + 29) / 30;
+                            const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
+                            t[k] = tt < nblk ? uint32_t(tt) : kNone;
+                        }
                     }
                 }
+#pragma unroll 1
+                for (uint32_t k = 0; k < 8; ++k) {
+                    const uint32_t tk = t[k];
+                    if (tk >= nblk) continue;
+                    // m0 = q0 / p with q0 = base + 30 tk + u_k, so m0 / 30 = q0 (30 p)^-1
+                    // mod 1001 and mod f (base mod 1001 and mod f: the run's)
+                    const uint32_t uk = unit30(k);
+                    const uint32_t c = (bp.bm1 + 30u * (tk % kWheelM) + uk) % kWheelM * a1001 % kWheelM;
+                    uint32_t r1 = 0, r2 = 0;
+#pragma unroll
+                    for (uint32_t j = 0; j < 8; ++j) {
+                        const uint32_t f = kF[j];
+                        const uint32_t q = (uint32_t(bp.bres[j]) + 30u * (tk % f) + uk) % f;
+                        const uint32_t rho = q * af[j] % f;
+                        if (j < 4) r1 |= rho << (8 * j);
+                        else r2 |= rho << (8 * (j - 4));
+                    }
+                    large_walk(bp.map + size_t(k) * wpc, nblk, tk, p, c, r1, r2, s_wheel);
+                }
             }
-            large_walk<0>(map, wpc, nblk, t[0], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<1>(map, wpc, nblk, t[1], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<2>(map, wpc, nblk, t[2], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<3>(map, wpc, nblk, t[3], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<4>(map, wpc, nblk, t[4], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<5>(map, wpc, nblk, t[5], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<6>(map, wpc, nblk, t[6], p, pi1, pi2, bm1, bm2, s_skip);
-            large_walk<7>(map, wpc, nblk, t[7], p, pi1, pi2, bm1, bm2, s_skip);
         }
     }
 }

@@ -123,6 +123,25 @@ def test_tiles_across_hit_list_regions_selfcheck(tile_bits):
         assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi)
 
 
+def test_packed_large_tier_selfcheck_production():
+    """The packed large-prime tier active between p_mid = 2^21 and the hit
+    lists (a 24 GB multiplier table puts p_hl near 5.6e6): two production
+    segments at 4e18, the map equal to the rebuild without hit lists word for
+    word, the hashes and the first segment's statistics equal the oracle's."""
+    seg = 467_500_000
+    a = 4000008233142500000
+    segs = [(a, a + seg - 2), (a + seg, a + 2 * seg - 2)]
+    limit = segs[-1][1]
+    with gbc.Context(limit=limit, segment_even=seg, max_batch=2, p_mid=1 << 21, mtab_max_gb=24, hl_mode=1,
+                     selfcheck_every=1) as c:
+        assert c.stats().p_hl > 5_000_000
+        c.enqueue_batch(0, segs, limit, [0, gbc.SEG_VERIFY])
+        res, _ = c.collect(0, 2)
+        assert c.stats().selfchecks == 1
+    for r in res:
+        assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi)
+
+
 def test_prepare_builds_the_table_once():
     with gbc.Context(limit=5 * 10**18, segment_even=1_000_000, max_batch=4, hl_mode=1, mtab_max_gb=16) as c:
         c.prepare(10**16, 5 * 10**18)
