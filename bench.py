@@ -473,6 +473,9 @@ def main():
     ap.add_argument("--windows", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-sweep", default="500,2000",
+                    help="more request rates (per s) for the serving loop under load, comma-separated ('': none)")
+    ap.add_argument("--sweep-seconds", type=float, default=10.0)
     ap.add_argument("--slice", action="store_true")
     ap.add_argument("--sparse-segments", type=int, default=2, help="segments of the sparse leg (0: none)")
     ap.add_argument("--sparse-dlt-log2", type=int, default=26)
@@ -676,6 +679,12 @@ def run_gb300(args, rep):
         out["windows"] = windows_leg(gbc, args.windows)
     if args.serve_seconds > 0:
         out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate)
+        # the same loop under load: continuous batching as the request rate grows
+        sweep = [float(x) for x in args.serve_sweep.split(",") if x.strip()]
+        if sweep:
+            out["serving_sweep"] = [
+                {k: v for k, v in serving_leg(gbc, args.sweep_seconds, r, check=16).items() if k != "config"}
+                for r in sweep]
     if args.sparse_segments:
         out["sparse"] = sparse_leg(gbc, args.sparse_segments, args.sparse_dlt_log2)
     if not args.no_cpu:

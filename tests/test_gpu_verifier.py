@@ -2,11 +2,12 @@
 include/gb_verifier.hpp (tests/cpp/run_gpu_main.cpp) calls gb::run_gpu with
 the reference's signature.
 
-The five runs of tests/golden/gstats/ (what the reference's own
-GoldbachStats wrote for them: merged, adjacent, refused, without gaps, a gap
-backfill) go through gb::run_gpu with the reference's environment knobs; the
-state file, the gap state and the log must equal the reference's byte for
-byte after every run. A window at 1e12 checks the RunStats counts against the
+The runs of tests/golden/gstats/ (what the reference's own GoldbachStats
+wrote for them, production sampling: merged, adjacent, refused, without
+gaps, a gap backfill) and of tests/golden/gstats_gaps/ (statistics-only runs
+around the record gaps 1476 and 1442, out of order) go through gb::run_gpu
+with the reference's environment knobs; the state file, the gap state and
+the log must equal the reference's byte for byte after every run. A window at 1e12 checks the RunStats counts against the
 oracle and the per-segment records against the segment plan."""
 import os
 import subprocess
@@ -16,14 +17,10 @@ import pytest
 import gbc
 import oracle
 from conftest import golden_path
+from test_stats_campaign import SCENARIOS
 from test_verifier_abi import build_main
 
 pytestmark = pytest.mark.gpu
-
-T = 2**63
-RUNS = [(1, T - 10**6, T - 2), (1, T, T + 10**6), (1, T - 10**6, T - 2),
-        (0, T + 10**6 + 2, T + 1_400_000), (1, T + 10**6 + 2, T + 1_400_000)]
-
 
 def read(p):
     with open(p, "rb") as f:
@@ -43,18 +40,20 @@ def kv(out):
     return dict(ln.split("=", 1) for ln in out.splitlines() if "=" in ln and not ln.startswith("ridge="))
 
 
-def test_run_gpu_statistics_files_equal_the_references(tmp_path):
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_run_gpu_statistics_files_equal_the_references(tmp_path, name):
+    every, seg, runs, _ = SCENARIOS[name]
     exe = build_main(tmp_path)
-    for i, (g, a, b) in enumerate(RUNS, 1):
-        env = env_for(tmp_path, GB_STATS_SAMPLE="2", GB_GAPS="exact" if g else "0")
-        r = subprocess.run([exe, str(b), "600000", str(a), "0"], env=env, cwd=tmp_path, capture_output=True, text=True)
+    for i, (g, a, b) in enumerate(runs, 1):
+        env = env_for(tmp_path, GB_STATS_SAMPLE=str(every), GB_GAPS="exact" if g else "0")
+        r = subprocess.run([exe, str(b), str(seg), str(a), "0"], env=env, cwd=tmp_path, capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
         assert kv(r.stdout)["stats_on"] == "1"
-        assert read(tmp_path / "goldbach_stats.state") == read(golden_path(f"gstats/after{i}.state")), i
-        gp = golden_path(f"gstats/after{i}.gaps")
+        assert read(tmp_path / "goldbach_stats.state") == read(golden_path(f"{name}/after{i}.state")), i
+        gp = golden_path(f"{name}/after{i}.gaps")
         if os.path.exists(gp):
             assert read(tmp_path / "goldbach_stats.state.gaps") == read(gp), i
-    assert read(tmp_path / "goldbach_stats.log") == read(golden_path("gstats/goldbach_stats.log"))
+    assert read(tmp_path / "goldbach_stats.log") == read(golden_path(f"{name}/goldbach_stats.log"))
 
 
 def test_run_gpu_counts_and_per_segment_records(tmp_path):

@@ -2,9 +2,12 @@
 
 tests/golden/gstats/ holds what the reference's GoldbachStats (include/
 gstats.hpp, compiled into oracle/_ref by tests/golden/make_gstats_golden.py)
-wrote for five runs around 2^63: a run merged, an adjacent run merged into
-one range, a repeated run refused (GBPSAMP row), a run without gap
-statistics, and that run again with gaps (a backfill: GBPSAMP + GBGAPS rows).
+wrote for five runs around 2^63 in production sampling (every second segment
+sampled): a run merged, an adjacent run merged into one range, a repeated run
+refused (GBPSAMP row), a run without gap statistics, and that run again with
+gaps (a backfill: GBPSAMP + GBGAPS rows). tests/golden/gstats_gaps/ holds
+three statistics-only runs (every segment sampled) around the record prime
+gaps 1476 and 1442, committed out of order.
 Here the same runs' per-segment results (restated from the oracle,
 tests/stats_results.py) go through gbc_stats_commit; the state file, the gap
 state and the log must equal the reference's byte for byte after every run.
@@ -26,6 +29,13 @@ SAMPLE_EVERY = 2
 RUNS = [(1, T - 10**6, T - 2), (1, T, T + 10**6), (1, T - 10**6, T - 2),
         (0, T + 10**6 + 2, T + 1_400_000), (1, T + 10**6 + 2, T + 1_400_000)]
 MERGED = [True, True, False, True, False]
+# (fixture directory, segments sampled every, segment integers, runs (gaps on, start, limit), merged)
+SCENARIOS = {
+    "gstats": (SAMPLE_EVERY, SEG_EVEN, RUNS, MERGED),
+    "gstats_gaps": (1, 100_000, [(1, 1425172824437600000, 1425172824437800000),
+                                 (1, 804212830686600000, 804212830686800000),
+                                 (1, 804212830686800002, 804212830687000000)], [True, True, True]),
+}
 
 
 @pytest.fixture(scope="module")
@@ -48,18 +58,20 @@ def read(p):
         return f.read()
 
 
-def test_statistics_files_equal_the_references(tmp_path, results):
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_statistics_files_equal_the_references(tmp_path, name):
+    every, seg, runs, merged_want = SCENARIOS[name]
     lib = gbc.load()
     state, log = tmp_path / "goldbach_stats.state", tmp_path / "goldbach_stats.log"
-    for i, (g, a, b) in enumerate(RUNS, 1):
-        rc, line, merged, err = commit(lib, state, log, g, a, b, results[(a, b)])
+    for i, (g, a, b) in enumerate(runs, 1):
+        rc, line, merged, err = commit(lib, state, log, g, a, b, segment_results(a, b, seg, every))
         assert rc == 0, err
-        assert merged == MERGED[i - 1]
-        assert read(state) == read(golden_path(f"gstats/after{i}.state")), f"state after run {i}"
-        gp = golden_path(f"gstats/after{i}.gaps")
+        assert merged == merged_want[i - 1]
+        assert read(state) == read(golden_path(f"{name}/after{i}.state")), f"state after run {i}"
+        gp = golden_path(f"{name}/after{i}.gaps")
         if os.path.exists(gp):
             assert read(str(state) + ".gaps") == read(gp), f"gap state after run {i}"
-    assert read(log) == read(golden_path("gstats/goldbach_stats.log"))
+    assert read(log) == read(golden_path(f"{name}/goldbach_stats.log"))
 
 
 def test_adjacent_runs_merge_to_one_run(tmp_path):
