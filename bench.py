@@ -24,9 +24,13 @@ value  = evens verified per second over the timed steps, device time from
 e2e    = the same metric through the C ABI as a caller uses it: two slots in
          flight, gbc_enqueue_batch + gbc_collect, per-segment results copied
          to host memory inside the timed region, wall clock.
-plain  = the plain per-segment form on the same GPU: one segment per batch,
-         two slots in flight, kernels launched one by one; batched_over_plain
-         is value / plain.value.
+plain  = the plain form on the same GPU, as the reference runs it: the hit
+         lists harvested once per batch of segments, then every segment
+         through its own launches of the sieve, large-prime, checker and
+         count kernels (launch mode 3); batched_over_plain is value /
+         plain.value (device) and e2e / plain.e2e. plain_one_segment_batches:
+         one segment per batch with every stage, the hit lists included, per
+         segment.
 windows = 256 windows of log-uniform widths in [1e6, 1e10] at uniform starts
          in [1e15, 5e18] (seed 7) verified in shared batches, against the same
          windows run one at a time; every window's statistics compared.
@@ -286,6 +290,40 @@ def plain_leg(gbc, start, nseg, first_seg, knobs=None):
             "config": "one production segment per batch, kernels launched one by one, funnel verify + exact tail, "
                       "hit lists on (table built before timing), the batched form's other knobs; value: one slot, "
                       "device events; e2e: two slots in flight, wall clock"}
+
+
+def plain_form_leg(gbc, start, first_seg, knobs=None, k=128):
+    """The reference's plain form (src/verifier.cpp:2487-2517, 1136-1143):
+    the hit lists harvested once per batch of k segments, then every segment
+    through its own launches of the sieve, the large primes, the checkers and
+    the count kernel (launch mode 3), production sampling. value: device time
+    of one batch of k segments on one slot (CUDA events); e2e: wall time of
+    the next two batches with two slots in flight."""
+    segs = [(start + i * SEG, start + i * SEG + SEG - 2) for i in range(first_seg, first_seg + 4 * k)]
+    limit = segs[-1][1]
+    kn = {n: v for n, v in (knobs or {}).items()
+          if n in ("p_mid", "mtab_max_gb", "tile_log2", "tile_bits", "plan_funnels", "verify_funnels")}
+    flags = [0 if i % 256 == 0 else gbc.SEG_VERIFY for i in range(k)]
+    batches = [segs[i * k:(i + 1) * k] for i in range(4)]
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=k, launch_mode=3, hl_mode=1, **kn) as ctx:
+        ctx.enqueue_batch(0, batches[0], limit, flags)        # warm-up: tables
+        ctx.collect(0, k)
+        ctx.enqueue_batch(0, batches[1], limit, flags)
+        _, t = ctx.collect(0, k)
+        dev_ms = t.ms_total
+        t0 = time.perf_counter()
+        ctx.enqueue_batch(0, batches[2], limit, flags)
+        ctx.enqueue_batch(1, batches[3], limit, flags)
+        ctx.collect(0, k)
+        ctx.collect(1, k)
+        wall = time.perf_counter() - t0
+    evens = k * (SEG // 2)
+    return {"value": evens / (dev_ms / 1e3) / 1e9, "unit": "G evens/s",
+            "e2e": {"value": 2 * evens / wall / 1e9, "unit": "G evens/s"}, "segments_per_batch": k,
+            "config": f"the plain form: hit lists harvested once per {k} segments, then each production segment "
+                      "by its own launches (sieve, large primes, checkers, counts), production sampling, the "
+                      "batched form's other knobs; value: one batch on one slot, device events; e2e: two batches "
+                      "on two slots, wall clock"}
 
 
 def log_uniform(rnd, lo, hi):
@@ -672,7 +710,10 @@ def run_gb300(args, rep):
             print(json.dumps(out))
         return 0
     if args.plain_segments:
-        out["plain"] = plain_leg(gbc, start, args.plain_segments, nb * args.batch, knobs)
+        # the plain form as the reference runs it (hit lists once per batch of
+        # segments), and one segment per batch with every stage per segment
+        out["plain"] = plain_form_leg(gbc, start, nb * args.batch, knobs, args.batch)
+        out["plain_one_segment_batches"] = plain_leg(gbc, start, args.plain_segments, (nb + 4) * args.batch, knobs)
         out["batched_over_plain"] = {"device": value / out["plain"]["value"],
                                      "e2e": e2e / out["plain"]["e2e"]["value"]}
     if args.windows:

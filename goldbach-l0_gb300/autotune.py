@@ -2,7 +2,10 @@
 include/config.hpp: SMEM tile size, the tile / large-prime split, the
 hit-list split through the prime-multiplier table's budget, segments per
 batch, the verify plan's funnel count and how many of them every word takes
-before the unresolved words are gathered).
+before the unresolved words are gathered). A table budget below what the
+hit lists need from p_mid on leaves the primes between p_mid and the hit
+lists to the packed large-prime tier, so the (p_mid, budget) knob also
+decides how much work that tier gets.
 
 Coordinate descent on calibration batches of the workload: from the
 defaults, each knob in turn takes the value with the highest throughput
@@ -35,14 +38,15 @@ SEG = 467_500_000
 KNOBS = {
     # the tile / hit-list split and the table budget that sets where the hit
     # lists start: one joint knob (a small budget pushes p_hl above p_mid)
-    ("p_mid", "mtab_max_gb"): [(p, g) for p in (1 << 20, 1 << 21, 1 << 22, 1 << 23) for g in (48, 96, 160)],
+    ("p_mid", "mtab_max_gb"): [(p, g) for p in (1 << 20, 1 << 21, 1 << 22, 1 << 23) for g in (16, 24, 48, 96, 160)],
     "tile_log2": [19, 20],
+    "tile_bits": [0, 1572864, 1835008],  # 0: 2^tile_log2 bits
     "max_batch": [32, 48, 64, 96, 128],
     "plan_funnels": [6, 8, 12, 16],
     "verify_funnels": [2, 3, 4],
 }
-DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "max_batch": 16, "plan_funnels": 8,
-            "verify_funnels": 3}
+DEFAULTS = {"p_mid": 1 << 22, "mtab_max_gb": 48, "tile_log2": 20, "tile_bits": 0, "max_batch": 16,
+            "plan_funnels": 8, "verify_funnels": 3}
 DEFAULT_RECORD = os.path.join(HERE, "tuning", "gb300_production_4e18.json")
 
 
@@ -75,8 +79,10 @@ def gpu_name():
         return "unknown"
 
 
-def tune(start, rounds=3, nseg=192, log=print):
+def tune(start, rounds=3, nseg=192, log=print, init=None):
+    """Coordinate descent from init (default: DEFAULTS)."""
     best = dict(DEFAULTS)
+    best.update(init or {})
     trials = []
     cache = {}
 
@@ -124,7 +130,7 @@ def tune(start, rounds=3, nseg=192, log=print):
                                  "segment p(n) of every even"},
             "method": "coordinate descent over the knobs ((p_mid, table budget) as one), up to three rounds, "
                       "device time of the pipeline's events",
-            "defaults": DEFAULTS, "default_g_evens_s": base,
+            "defaults": DEFAULTS, "start_knobs": dict(init or DEFAULTS), "default_g_evens_s": base,
             "choice": best, "choice_g_evens_s": cache[tuple(sorted(best.items()))], "trials": trials}
 
 
@@ -143,8 +149,9 @@ def main():
     ap.add_argument("--segments", type=int, default=192)
     ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--out", default=DEFAULT_RECORD)
+    ap.add_argument("--from-record", default="", help="start the descent from this record's choice")
     a = ap.parse_args()
-    rec = tune(a.start, a.rounds, a.segments)
+    rec = tune(a.start, a.rounds, a.segments, init=load(a.from_record) if a.from_record else None)
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
     with open(a.out, "w") as f:
         json.dump(rec, f, indent=1)

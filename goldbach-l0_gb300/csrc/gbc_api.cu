@@ -315,6 +315,7 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         CK(dev_alloc(ctx, &s.ovf_cnt, 4));
     }
     CK(cudaMallocHost(&s.desc_host, ctx->layout.bytes));
+    CK(cudaMallocHost(&s.win_host, sizeof(gbk::BatchHeader) * cfg.max_batch));
     std::memset(s.desc_host, 0, ctx->layout.bytes);
     CK(dev_alloc(ctx, &s.desc_dev, ctx->layout.bytes));
     CK(cudaMemset(s.desc_dev, 0, ctx->layout.bytes));
@@ -343,6 +344,7 @@ static void slot_free(Slot &s)
     cudaFree(s.ovf_buf);
     cudaFree(s.ovf_cnt);
     if (s.desc_host) cudaFreeHost(s.desc_host);
+    if (s.win_host) cudaFreeHost(s.win_host);
     cudaFree(s.chk_map);
     cudaFree(s.chk_desc_dev);
     cudaFree(s.chk_count);
@@ -383,7 +385,7 @@ extern "C" int gbc_create(const gbc_config *cfg_in, gbc_ctx **out)
     else if (cfg.max_batch > 256) rc = fail(ctx, GBC_E_ARG, "max_batch above 256");
     else if (cfg.max_runs > cfg.max_batch) rc = fail(ctx, GBC_E_ARG, "max_runs above max_batch");
     else if (cfg.nslots < 2 || cfg.nslots > GBC_MAX_SLOTS) rc = fail(ctx, GBC_E_ARG, "nslots outside [2, 8]");
-    else if (cfg.launch_mode > 2) rc = fail(ctx, GBC_E_ARG, "launch_mode outside [0, 2]");
+    else if (cfg.launch_mode > 3) rc = fail(ctx, GBC_E_ARG, "launch_mode outside [0, 3]");
     else if (cfg.tile_log2 < 14 || cfg.tile_log2 > 20) rc = fail(ctx, GBC_E_ARG, "tile_log2 outside [14, 20]");
     else if (cfg.tile_bits && (cfg.tile_bits % 4096 || cfg.tile_bits < (1u << 14) || cfg.tile_bits > kMaxTileBits))
         rc = fail(ctx, GBC_E_ARG, "tile_bits must be a multiple of 4096 in [2^14, 1835008]");
@@ -826,6 +828,41 @@ static void finish_desc(const gbc_ctx *ctx, DescImage &img)
     img.chk_pref[nseg] = h.chk_vb;
     img.ver_pref[nseg] = h.ver_vb;
     img.cnt_pref[nseg] = h.cnt_vb;
+    h.seg0 = 0;  // the whole batch
+    h.win_b0 = 0;
+    h.win_b1 = UINT32_MAX;
+}
+
+// The plain form's per-segment headers (launch mode 3, a one-run batch):
+// segment i's tiles (those of its q range [hash_lo, hash_hi] and 64 bits of
+// the checkers' slack; a tile shared with a neighbour is sieved again, the
+// same bits), its virtual CTAs of the checkers and the count kernel, and the
+// class bits of those tiles for the large primes and the overflow marks.
+static void plain_windows(const gbc_ctx *ctx, Slot &s)
+{
+    const DescImage &img = s.img;
+    const gbk::BatchParams &bp = img.runs[0];
+    const uint32_t tb = ctx->tile_bits, nseg = img.h->nseg;
+    for (uint32_t i = 0; i < nseg; ++i) {
+        const gbk::SegParams &sp = img.segs[i];
+        gbk::BatchHeader h = *img.h;
+        const uint64_t lo = sp.hash_lo > bp.base ? (sp.hash_lo - bp.base) / 30 : 0;
+        const uint64_t hi = (sp.hash_hi - bp.base) / 30 + 64;
+        const uint32_t ti0 = uint32_t(lo / tb), ti1 = uint32_t(std::min<uint64_t>(hi / tb, bp.tiles_pc - 1));
+        h.tile_items = 8 * (ti1 + 1);
+        h.work[gbk::kWorkTile] = 8 * ti0;
+        h.chk_vb = img.chk_pref[i + 1];
+        h.work[gbk::kWorkCheck] = img.chk_pref[i];
+        h.ver_vb = img.ver_pref[i + 1];
+        h.work[gbk::kWorkVerify] = img.ver_pref[i];
+        h.cnt_vb = img.cnt_pref[i + 1];
+        h.work[gbk::kWorkCount] = img.cnt_pref[i];
+        h.nseg = i + 1;
+        h.seg0 = i;
+        h.win_b0 = ti0 * tb;
+        h.win_b1 = uint32_t(std::min<uint64_t>(uint64_t(ti1 + 1) * tb, uint64_t(bp.wpc) * 32));
+        s.win_host[i] = h;
+    }
 }
 
 // Plans a batch into the slot's descriptor image: runs, their maps in the
@@ -1068,6 +1105,44 @@ extern "C" int gbc_prepare(gbc_ctx *ctx, uint64_t lo, uint64_t hi)
     return ensure_mtab(ctx, base / pr[n_all - 1], (qmax + 29) / pr[ctx->n_hl]);
 }
 
+// The plain form (launch mode 3): the batch's hit lists harvested and sorted
+// once, as the reference harvests them once per batch of segments
+// (src/verifier.cpp:1136-1143), then every segment in turn through the
+// sieve, the large primes, the checkers and the count kernel, each launch
+// narrowed to the segment by its header (plain_windows).
+static int issue_plain(gbc_ctx *ctx, Slot &s)
+{
+    cudaStream_t st = s.st;
+    const gbk::BatchDesc &d = s.dd;
+    const gbh::Grids &g = ctx->grids;
+    CK(cudaMemcpyAsync(s.desc_dev, s.desc_host, ctx->layout.bytes, cudaMemcpyHostToDevice, st));
+    gbh::launch_init(d, g, st);
+    gbh::launch_xfirst(d, g, st);
+    gbh::launch_hitlist(d, false, g, st);
+    gbh::launch_binsort(d, g, st);
+    CK(cudaEventRecord(s.ev[1], st));
+    const uint32_t nseg = s.img.h->nseg;
+    for (uint32_t i = 0; i < nseg; ++i) {
+        // the header sits at the descriptor's start
+        CK(cudaMemcpyAsync(s.desc_dev, s.win_host + i, sizeof(gbk::BatchHeader), cudaMemcpyHostToDevice, st));
+        gbh::launch_tile(d, ctx->gi, ctx->tile_bits, ctx->tile_stage, g, st);
+        gbh::launch_large(d, g, st);
+        gbh::launch_hitlist(d, true, g, st);
+        gbh::launch_hl_overflow(d, g, st);
+        gbh::launch_check(d, ctx->ct, g, st);
+        gbh::launch_verify(d, ctx->vt, g, st);
+        gbh::launch_retry(d, ctx->cfg.ridge_min, (ctx->cfg.test_flags & GBC_TEST_RETRY_LIMIT) ? 1u : (1u << 22), g,
+                          st);
+        gbh::launch_count(d, g, st);
+    }
+    // the stages interleave segment by segment: the sieve event takes the loop
+    CK(cudaEventRecord(s.ev[2], st));
+    CK(cudaEventRecord(s.ev[3], st));
+    CK(cudaEventRecord(s.ev[4], st));
+    ctx->launches += 4 + 9 * uint64_t(nseg);
+    return GBC_OK;
+}
+
 // The pipeline of one batch on the slot's stream (the same calls are
 // captured into the slot's graph): descriptor upload, result init, first
 // bits, tiles | large primes, hit lists (filed by region, then applied
@@ -1174,7 +1249,11 @@ static int enqueue_planned(gbc_ctx *ctx, Slot &s)
     }
     cudaStream_t st = s.st;
     CK(cudaEventRecord(s.ev[0], st));
-    if (ctx->cfg.launch_mode == 2) {
+    if (ctx->cfg.launch_mode == 3 && img.h->nrun == 1) {
+        plain_windows(ctx, s);
+        if (int r = issue_plain(ctx, s)) return r;
+        ctx->launches -= kPipelineKernels;  // counted by issue_plain
+    } else if (ctx->cfg.launch_mode >= 2) {
         if (int r = issue_pipeline(ctx, s, false)) return r;
     } else {
         if (!s.exec)

@@ -175,13 +175,21 @@ struct SegParams {
 // replays every batch.
 struct BatchHeader {
     uint32_t nrun, nseg;
-    uint32_t tile_items;           // (run, class, tile) items of the tile kernel
+    uint32_t tile_items;           // (run, tile, class) items of the tile kernel, tile-major per run
     uint32_t n_mid_max;            // first bits: primes [i0, n_mid_max)
     uint32_t n_mid_min, n_hl_max;  // large primes: [n_mid_min, n_hl_max)
     uint32_t n_hl_min, n_all_max;  // hit-listed primes: [n_hl_min, n_all_max)
     uint32_t chk_vb, ver_vb, cnt_vb; // virtual CTAs of k_check, k_verify, k_count
     uint32_t nlow;                 // segments that need the generic low checker
-    uint32_t pad[2];
+    // a window of the batch for the per-segment launches of the plain form
+    // (launch mode 3; the whole batch otherwise): segments [seg0, nseg) for
+    // the kernels that walk segments, class bits [win_b0, win_b1) of run 0
+    // for the large primes and the overflow marks (tile-aligned); the item
+    // ranges of the other kernels are their work counters' start values
+    // and limits
+    uint32_t seg0;
+    uint32_t win_b0, win_b1;
+    uint32_t pad;
     // work counters of the persistent kernels (CTAs take their next item
     // with an atomic add); zero in the host image, so every batch's
     // descriptor copy resets them

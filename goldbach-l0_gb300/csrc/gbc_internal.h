@@ -63,6 +63,9 @@ struct Slot {
     uint32_t ovf_cap = 0;
     // the batch descriptor: pinned host image, device copy
     uint8_t *desc_host = nullptr, *desc_dev = nullptr;
+    // the plain form (launch mode 3): one header per segment of the batch,
+    // each the batch's header narrowed to the segment (pinned, max_batch)
+    gbk::BatchHeader *win_host = nullptr;
     DescImage img;
     gbk::BatchDesc dd{};
     cudaGraphExec_t exec = nullptr;    // the captured pipeline (launch modes 0 and 1)

@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256) k_check_low(BatchDesc d, const uint16_t *
 {
     if (!d.h->nlow) return;
     const uint32_t nseg = d.h->nseg;
-    for (uint32_t si = 0; si < nseg; ++si) {
+    for (uint32_t si = d.h->seg0; si < nseg; ++si) {
         const SegParams &sp = d.segs[si];
         if (!sp.low) continue;
         const BatchParams &bp = d.runs[sp.run];
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(256) k_check_low(BatchDesc d, const uint16_t *
 __global__ void __launch_bounds__(64) k_retry(BatchDesc d, uint32_t ridge_min, uint32_t max_tries)
 {
     const uint32_t nseg = d.h->nseg;
-    for (uint32_t si = blockIdx.x; si < nseg; si += gridDim.x) {
+    for (uint32_t si = d.h->seg0 + blockIdx.x; si < nseg; si += gridDim.x) {
         const SegParams &sp = d.segs[si];
         gbc_segment_result *res = sp.res;
         const uint32_t nl = res->nleft < GBC_LEFT_CAP ? res->nleft : GBC_LEFT_CAP;
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(BatchDesc d, VerifyTables
     // s_pref[.][s]: pending words of the segments before s (Hillis-Steele)
     {
         uint32_t c = 0;
-        if (tid < nseg) {
+        if (tid < nseg && tid >= d.h->seg0) {  // the segments of the window
             const SegParams &sp = d.segs[tid];
             const uint32_t np = sp.res->npend;
             c = sp.sampled ? 0u : (np < sp.pend_cap ? np : sp.pend_cap);

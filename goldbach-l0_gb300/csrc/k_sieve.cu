@@ -359,10 +359,14 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 
 // Persistent tile kernel: CTAs take the batch's (run, class, tile) items
 // from a work counter; tiles of tb bits (a multiple of 128), a run's last
-// tile of a class ends at its class array's end; up to `cap` offsets of each
-// tile bin staged into shared memory.
-__global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tb, uint32_t cap)
+// tile of a class ends at its class array's end; up to kCap offsets of each
+// tile bin staged into shared memory. kCap is a compile-time constant: with
+// it as a runtime parameter the kernel measured 3.7 times slower (47.9
+// against 13.05 ms per 128-segment batch at 2^20-bit tiles, one GB300).
+template <uint32_t kCap>
+__global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uint32_t tb)
 {
+    constexpr uint32_t cap = kCap;
     // shared memory: the tile, the tile-bin staging buffer, the patterns
     extern __shared__ __align__(16) uint32_t sm_tile[];
     uint32_t *s = sm_tile;
@@ -383,8 +387,10 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uin
         if (j >= items) break;
         const uint32_t r = find_prefix(d.tile_pref, nrun, j);
         const BatchParams &bp = d.runs[r];
+        // items tile-major within a run: a tile's eight classes side by side,
+        // so the tiles of one segment are one range of items
         const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
-        const uint32_t k = local / tpc, ti = local - k * tpc, t0 = ti * tb;
+        const uint32_t k = local & 7u, ti = local >> 3, t0 = ti * tb;
         const uint32_t tl = min(tb, bp.wpc * 32 - t0);
         if (threadIdx.x == 0) {
             uint32_t n = 0;
@@ -398,6 +404,12 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uin
         tile_body<true>(bp, gi, pat, s, k, ti, t0, tl, tb, stg, &s_bar, &phase, &s_nb, cap);
     }
 }
+
+// the staging capacities the host chooses from (the largest that fits)
+constexpr uint32_t kTbStages[3] = {kTbStage, 2 * kTbPiece, 0};
+template __global__ void k_tile<kTbStages[0]>(BatchDesc, GroupInfo, uint32_t);
+template __global__ void k_tile<kTbStages[1]>(BatchDesc, GroupInfo, uint32_t);
+template __global__ void k_tile<kTbStages[2]>(BatchDesc, GroupInfo, uint32_t);
 
 // one run by value: grid (tiles_pc, 8), full tiles (wpc = tiles_pc tiles)
 __global__ void __launch_bounds__(1024, 1) k_tile1(BatchParams bp, GroupInfo gi)
@@ -526,8 +538,13 @@ __global__ void __launch_bounds__(256) k_large(BatchDesc d)
             for (uint32_t ri = 0; ri < nrun; ++ri) {
                 const BatchParams &bp = d.runs[ri];
                 if (i < bp.n_mid || i >= bp.n_hl) continue;
-                const uint64_t base = bp.base;
-                const uint32_t nblk = bp.nblk, wpc = bp.wpc;
+                // run 0's window (the plain form's per-segment launches):
+                // bits [b0, b1), b0 a multiple of 32, as a run of its own
+                const uint32_t b0 = ri ? 0u : d.h->win_b0, b1 = ri ? bp.nblk : min(bp.nblk, d.h->win_b1);
+                if (b0 >= b1) continue;
+                const uint64_t base = bp.base + 30ull * b0;
+                const uint32_t nblk = b1 - b0, wpc = bp.wpc;
+                const uint32_t bm1 = (bp.bm1 + 30u * (b0 % kWheelM)) % kWheelM;
                 const uint32_t r = mod_u64(base, p, rp);
                 // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
                 const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
@@ -561,17 +578,18 @@ __global__ void __launch_bounds__(256) k_large(BatchDesc d)
                     // m0 = q0 / p with q0 = base + 30 tk + u_k, so m0 / 30 = q0 (30 p)^-1
                     // mod 1001 and mod f (base mod 1001 and mod f: the run's)
                     const uint32_t uk = unit30(k);
-                    const uint32_t c = (bp.bm1 + 30u * (tk % kWheelM) + uk) % kWheelM * a1001 % kWheelM;
+                    const uint32_t c = (bm1 + 30u * (tk % kWheelM) + uk) % kWheelM * a1001 % kWheelM;
                     uint32_t r1 = 0, r2 = 0;
 #pragma unroll
                     for (uint32_t j = 0; j < 8; ++j) {
                         const uint32_t f = kF[j];
-                        const uint32_t q = (uint32_t(bp.bres[j]) + 30u * (tk % f) + uk) % f;
+                        const uint32_t bf = (uint32_t(bp.bres[j]) + 30u * (b0 % f)) % f;
+                        const uint32_t q = (bf + 30u * (tk % f) + uk) % f;
                         const uint32_t rho = q * af[j] % f;
                         if (j < 4) r1 |= rho << (8 * j);
                         else r2 |= rho << (8 * (j - 4));
                     }
-                    large_walk(bp.map + size_t(k) * wpc, nblk, tk, p, c, r1, r2, s_wheel);
+                    large_walk(bp.map + size_t(k) * wpc + (b0 >> 5), nblk, tk, p, c, r1, r2, s_wheel);
                 }
             }
         }
@@ -847,9 +865,10 @@ __global__ void __launch_bounds__(256) k_hl_overflow(BatchDesc d)
     const uint32_t cnt = *bp.ovf_cnt;
     if (cnt > bp.ovf_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bp.err, kErrHlOverflow);
     const uint32_t n = min(cnt, bp.ovf_cap);
+    const uint32_t b0 = d.h->win_b0, b1 = d.h->win_b1;  // the plain form's window (else everything)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint2 e = bp.ovf_buf[i];
-        atomicAnd(bp.map + size_t(e.x) * bp.wpc + (e.y >> 5), ~(1u << (e.y & 31)));
+        if (e.y >= b0 && e.y < b1) atomicAnd(bp.map + size_t(e.x) * bp.wpc + (e.y >> 5), ~(1u << (e.y & 31)));
     }
 }
 
@@ -927,16 +946,18 @@ bool tile_attributes(uint32_t tile_bits, uint32_t tile_log2, const gbk::GroupInf
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, gbk::k_tile);
+    cudaFuncGetAttributes(&fa, gbk::k_tile<gbk::kTbStages[0]>);
     const size_t room = size_t(optin) > fa.sharedSizeBytes ? size_t(optin) - fa.sharedSizeBytes : 0;
     const size_t base = tile_smem(tile_bits, gi);
     if (base > room) return false;
-    // the staging buffer in whole bulk-copy pieces, as much as fits, at most kTbStage
-    size_t st = (room - base) / 4 / gbk::kTbPiece * gbk::kTbPiece;
-    if (st > gbk::kTbStage) st = gbk::kTbStage;
-    *stage = uint32_t(st);
-    cudaFuncSetAttribute(gbk::k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(tile_smem_staged(tile_bits, *stage, gi)));
+    // the largest staging buffer of the kernel's instantiations that fits
+    uint32_t c = 0;
+    while (c < 2 && base + size_t(gbk::kTbStages[c]) * 4 > room) ++c;
+    *stage = gbk::kTbStages[c];
+    const int bytes = int(tile_smem_staged(tile_bits, *stage, gi));
+    if (c == 0) cudaFuncSetAttribute(gbk::k_tile<gbk::kTbStages[0]>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (c == 1) cudaFuncSetAttribute(gbk::k_tile<gbk::kTbStages[1]>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (c == 2) cudaFuncSetAttribute(gbk::k_tile<gbk::kTbStages[2]>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(gbk::k_tile1, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(tile_smem(1u << tile_log2, gi)));
     return true;
@@ -950,7 +971,10 @@ void launch_xfirst(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 void launch_tile(const gbk::BatchDesc &d, const gbk::GroupInfo &gi, uint32_t tile_bits, uint32_t stage,
                  const Grids &g, cudaStream_t st)
 {
-    gbk::k_tile<<<g.sm, 1024, tile_smem_staged(tile_bits, stage, gi), st>>>(d, gi, tile_bits, stage);
+    const size_t bytes = tile_smem_staged(tile_bits, stage, gi);
+    if (stage == gbk::kTbStages[0]) gbk::k_tile<gbk::kTbStages[0]><<<g.sm, 1024, bytes, st>>>(d, gi, tile_bits);
+    else if (stage == gbk::kTbStages[1]) gbk::k_tile<gbk::kTbStages[1]><<<g.sm, 1024, bytes, st>>>(d, gi, tile_bits);
+    else gbk::k_tile<gbk::kTbStages[2]><<<g.sm, 1024, bytes, st>>>(d, gi, tile_bits);
 }
 
 void launch_large(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)

@@ -86,7 +86,10 @@ typedef struct gbc_config {
                                 include/config.hpp:104 RIDGE_MIN_DEFAULT) */
     uint32_t launch_mode;    /* 0 or 1: a batch is one replay of the slot's CUDA graph of the whole
                                 pipeline (captured at the slot's first batch); 2: the same kernels
-                                launched one by one */
+                                launched one by one; 3: the plain form (the reference's per-segment
+                                pipeline, src/verifier.cpp:2487-2517): a batch's hit lists harvested
+                                once, then each segment by its own launches of the sieve, large-prime,
+                                checker and count kernels (batches of several runs: as 2) */
     uint32_t selfcheck_every;/* every selfcheck_every-th batch that uses hit lists rebuilds its maps
                                 without them and compares every word (src/verifier.cpp:2057-2112);
                                 a mismatch fails the batch closed. 0: never (default) */
