@@ -142,6 +142,25 @@ def test_packed_large_tier_selfcheck_production():
         assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi)
 
 
+def result_fields(r):
+    """A segment result as comparable fields; the lists the kernels append
+    to with atomics (leftovers, gap tails, ridges) in no fixed order, as
+    sorted lists."""
+    import ctypes as C
+    out = {}
+    lists = {"left_n": "nleft", "left_p": "nleft", "tail_g": "ntail", "tail_lo": "ntail", "ridge_p": "nridge",
+             "ridge_n": "nridge"}
+    for name, _ in gbc.SegmentResult._fields_:
+        v = getattr(r, name)
+        if name in lists:
+            continue
+        out[name] = C.string_at(C.addressof(v), C.sizeof(v)) if hasattr(v, "_length_") else v
+    out["left"] = sorted(zip(r.left_n[:r.nleft], r.left_p[:r.nleft]))
+    out["tail"] = sorted(zip(r.tail_lo[:r.ntail], r.tail_g[:r.ntail]))
+    out["ridges"] = sorted(zip(r.ridge_n[:r.nridge], r.ridge_p[:r.nridge]))
+    return out
+
+
 @pytest.mark.parametrize("tile_bits", [0, 1835008])
 def test_plain_form_equals_batched_form(tile_bits):
     """The plain form (launch mode 3: hit lists harvested once for the
@@ -150,7 +169,6 @@ def test_plain_form_equals_batched_form(tile_bits):
     the same results, byte for byte, as the batched form's graph replay:
     four production segments at 4e18 with the packed tier and the hit lists
     on, production sampling; the map hashes equal the oracle's."""
-    import ctypes as C
     seg = 467_500_000
     a = 4000008233142500000
     segs = [(a + i * seg, a + (i + 1) * seg - 2) for i in range(4)]
@@ -162,11 +180,12 @@ def test_plain_form_equals_batched_form(tile_bits):
                          tile_bits=tile_bits, launch_mode=mode) as c:
             c.enqueue_batch(0, segs, limit, flags)
             res, _ = c.collect(0, 4)
-            out[mode] = [C.string_at(C.addressof(r), C.sizeof(r)) for r in res]
+            out[mode] = [result_fields(r) for r in res]
             if mode == 3:
                 for r in res:
                     assert (r.map_hash, r.map_primes) == oracle.map_hash(r.hash_lo, r.hash_hi)
-    assert out[1] == out[3]
+    for i, (x, y) in enumerate(zip(out[1], out[3])):
+        assert x == y, (i, [k for k in x if x[k] != y[k]])
 
 
 def test_prepare_builds_the_table_once():
