@@ -457,7 +457,7 @@ def slice_mode(args):
     evens = (b - a) // 2 + 1
     import autotune
     knobs = autotune.load(args.tuning or autotune.DEFAULT_RECORD) if args.tuning != "none" else None
-    knobs = knobs or {"max_batch": args.batch}
+    knobs = knobs or {"max_batch": args.batch or 16}
     args.batch = knobs["max_batch"]
     with gbc.Context(limit=b, segment_even=SEG, sample_every=args.sample_every, **knobs) as ctx:
         ctx.prepare(a, b)
@@ -494,7 +494,7 @@ def main():
     ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=0, help="segments per batch (0: the record's, else 16)")
     ap.add_argument("--sample-every", type=int, default=256)
     ap.add_argument("--tile-log2", type=int, default=0)
     ap.add_argument("--tile-bits", type=int, default=0, help="bits per tile (a multiple of 4096); overrides the record")
@@ -541,17 +541,18 @@ def run_gb300(args, rep):
     start = workload_start()
     nb = args.warmup + 2 * args.steps + 2 + args.exact_steps
     # knobs: the autotuner's record when there is one (goldbach-l0_gb300/autotune.py),
-    # command-line values otherwise
-    knobs = {"max_batch": args.batch, "tile_log2": args.tile_log2, "p_mid": args.p_mid,
-             "plan_funnels": args.plan_funnels, "mtab_max_gb": args.mtab_gb}
+    # then every knob given on the command line (0: not given)
+    knobs = {"max_batch": 16, "tile_log2": 0, "p_mid": 0, "plan_funnels": 0, "mtab_max_gb": 0}
     tuned = None
     if args.tuning != "none":
         import autotune
         tuned = autotune.load(args.tuning or autotune.DEFAULT_RECORD)
         if tuned:
             knobs.update(tuned)
-    if args.tile_bits:
-        knobs["tile_bits"] = args.tile_bits
+    for name, v in (("max_batch", args.batch), ("tile_log2", args.tile_log2), ("p_mid", args.p_mid),
+                    ("plan_funnels", args.plan_funnels), ("mtab_max_gb", args.mtab_gb), ("tile_bits", args.tile_bits)):
+        if v:
+            knobs[name] = v
     args.batch = knobs["max_batch"]
     # rank r: its own consecutive segments, after those of the ranks below
     allb = batches(start, rep.rank * nb * args.batch, nb, args.batch)

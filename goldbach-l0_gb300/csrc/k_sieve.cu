@@ -489,11 +489,18 @@ __device__ __forceinline__ void large_walk(uint32_t *wk, uint32_t nblk, uint32_t
     }
 }
 
-// The packed large primes [n_mid, n_hl) of every run: a warp per group of
-// kPackGroup primes, a lane per eight of them, the runs in turn.
+// The packed large primes [n_mid, n_hl) of every run: a CTA per item of 32
+// consecutive primes, a thread per (prime, class) walk, so that every walk of
+// a batch (about eight per prime) runs side by side (the walks wait on
+// global memory; a thread per prime walking its classes in turn measured
+// about half the pipeline's speed with 46 K primes on this tier). Warp 0
+// decodes the item's packing group (lane l: eight primes from one 8-byte
+// load, the group's running sum by a warp scan) into shared memory.
+constexpr uint32_t kLargeItem = 32;  // primes per CTA item; kPackGroup / kLargeItem items per group
 __global__ void __launch_bounds__(256) k_large(BatchDesc d)
 {
     __shared__ uint16_t s_wheel[kWheelTabWords];
+    __shared__ uint32_t s_p[kLargeItem];
     const uint32_t nrun = d.h->nrun;
     if (!nrun) return;
     const BatchParams &b0 = d.runs[0];
@@ -501,97 +508,87 @@ __global__ void __launch_bounds__(256) k_large(BatchDesc d)
     const uint32_t lo = max(d.h->n_mid_min, b0.pk_i0), hi = d.h->n_hl_max;
     if (lo >= hi) return;
     for (uint32_t i = threadIdx.x; i < kWheelTabWords; i += blockDim.x) s_wheel[i] = b0.wheel[i];
-    __syncthreads();
     const uint16_t *s_inv = s_wheel + kWheelM + kWheelUnits;  // x^-1 mod 1001 (0: none)
     const uint16_t *s_invf = s_inv + kWheelM;                  // x^-1 mod f, f = 17..43 back to back
     constexpr uint32_t kF[8] = {17, 19, 23, 29, 31, 37, 41, 43};
     constexpr uint32_t kFo[8] = {0, 17, 36, 59, 88, 119, 156, 197};
-    const uint32_t lane = threadIdx.x & 31, i0 = b0.pk_i0;
-    const uint32_t g_lo = (lo - i0) / kPackGroup, g_hi = (hi - i0 + kPackGroup - 1) / kPackGroup;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t g = g_lo + wid; g < g_hi; g += nw) {
-        // decode: this lane's eight half gaps, plus the sums of the lanes below
-        const uint2 gv = __ldg(reinterpret_cast<const uint2 *>(b0.pk_gap) + size_t(g) * (kPackGroup / 8) + lane);
-        uint32_t sum = 0;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, i0 = b0.pk_i0;
+    const uint32_t j_lo = (lo - i0) / kLargeItem, j_hi = (hi - i0 + kLargeItem - 1) / kLargeItem;
+    const uint32_t k = tid & 7;        // this thread's class
+    const uint32_t slot = tid >> 3;    // and prime of the item
+    for (uint32_t j = j_lo + blockIdx.x; j < j_hi; j += gridDim.x) {
+        __syncthreads();  // the wheel table loaded; the last item's primes read
+        if (tid < 32) {
+            const uint32_t g = j / (kPackGroup / kLargeItem), sl = j % (kPackGroup / kLargeItem);
+            const uint2 gv = __ldg(reinterpret_cast<const uint2 *>(b0.pk_gap) + size_t(g) * (kPackGroup / 8) + lane);
+            uint32_t sum = 0;
 #pragma unroll
-        for (uint32_t b = 0; b < 32; b += 8) sum += ((gv.x >> b) & 0xFFu) + ((gv.y >> b) & 0xFFu);
-        uint32_t incl = sum;
+            for (uint32_t b = 0; b < 32; b += 8) sum += ((gv.x >> b) & 0xFFu) + ((gv.y >> b) & 0xFFu);
+            uint32_t incl = sum;
 #pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(~0u, incl, o);
-            if (lane >= o) incl += y;
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(~0u, incl, o);
+                if (lane >= o) incl += y;
+            }
+            uint32_t p = __ldg(b0.pk_base + g) + 2u * (incl - sum);
+            const uint32_t first = sl * (kLargeItem / 8);  // the lanes of this item's slice of the group
+#pragma unroll
+            for (uint32_t u = 0; u < 8; ++u) {
+                p += 2u * (((u < 4 ? gv.x : gv.y) >> (8 * (u & 3))) & 0xFFu);
+                if (lane >= first && lane < first + kLargeItem / 8) s_p[(lane - first) * 8 + u] = p;
+            }
         }
-        uint32_t p = __ldg(b0.pk_base + g) + 2u * (incl - sum);
-#pragma unroll 1
-        for (uint32_t u = 0; u < 8; ++u) {
-            p += 2u * (((u < 4 ? gv.x : gv.y) >> (8 * (u & 3))) & 0xFFu);
-            const uint32_t i = i0 + g * kPackGroup + lane * 8 + u;
-            if (i < lo || i >= hi) continue;
-            const float rp = __frcp_rn(float(p));
-            const uint32_t iv = inv30_mod(p);
-            const uint32_t d2 = addmod(iv, iv, p), d4 = addmod(d2, d2, p), d6 = addmod(d4, d2, p);
-            // (30 p)^-1 mod 1001 and mod each skip prime f
-            const uint32_t a1001 = s_inv[30u * (p % kWheelM) % kWheelM];
-            uint32_t af[8];
+        __syncthreads();
+        const uint32_t i = i0 + j * kLargeItem + slot;
+        if (i < lo || i >= hi) continue;
+        const uint32_t p = s_p[slot];
+        const float rp = __frcp_rn(float(p));
+        const uint32_t iv = inv30_mod(p);
+        const uint32_t uk = unit30(k);
+        const uint32_t ck = mod_below(uint64_t(uk) * iv, p, rp);  // u_k / 30 mod p
+        // (30 p)^-1 mod 1001 and mod each skip prime f
+        const uint32_t a1001 = s_inv[30u * (p % kWheelM) % kWheelM];
+        uint32_t af[8];
 #pragma unroll
-            for (uint32_t j = 0; j < 8; ++j) af[j] = s_invf[kFo[j] + 30u * (p % kF[j]) % kF[j]];
-            for (uint32_t ri = 0; ri < nrun; ++ri) {
-                const BatchParams &bp = d.runs[ri];
-                if (i < bp.n_mid || i >= bp.n_hl) continue;
-                // run 0's window (the plain form's per-segment launches):
-                // bits [b0, b1), b0 a multiple of 32, as a run of its own
-                const uint32_t b0 = ri ? 0u : d.h->win_b0, b1 = ri ? bp.nblk : min(bp.nblk, d.h->win_b1);
-                if (b0 >= b1) continue;
-                const uint64_t base = bp.base + 30ull * b0;
-                const uint32_t nblk = b1 - b0, wpc = bp.wpc;
-                const uint32_t bm1 = (bp.bm1 + 30u * (b0 % kWheelM)) % kWheelM;
-                const uint32_t r = mod_u64(base, p, rp);
-                // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30, c_k = u_k / 30
-                const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
-                uint32_t cc = iv;
-                uint32_t t[8];
-#pragma unroll
-                for (uint32_t k = 0; k < 8; ++k) {
-                    uint32_t x = tb - cc;
-                    if (tb < cc) x += p;
-                    t[k] = x;
-                    const uint32_t dd = (k == 0 || k == 6) ? d6 : (k == 1 || k == 3 || k == 5) ? d4 : d2;
-                    cc = addmod(cc, dd, p);
-                }
-                if (uint64_t(p) * p > base) {  // only near the bottom of the range
-                    const uint64_t pp = uint64_t(p) * p;
-#pragma unroll
-                    for (uint32_t k = 0; k < 8; ++k) {
-                        const uint64_t uu = unit30(k);
-                        const uint64_t q = base + 30ull * t[k] + uu;
-                        if (q < pp) {
-                            const uint64_t tmin = (pp - base - uu + 29) / 30;
-                            const uint64_t tt = t[k] + (tmin - t[k] + p - 1) / p * p;
-                            t[k] = tt < nblk ? uint32_t(tt) : kNone;
-                        }
-                    }
-                }
-#pragma unroll 1
-                for (uint32_t k = 0; k < 8; ++k) {
-                    const uint32_t tk = t[k];
-                    if (tk >= nblk) continue;
-                    // m0 = q0 / p with q0 = base + 30 tk + u_k, so m0 / 30 = q0 (30 p)^-1
-                    // mod 1001 and mod f (base mod 1001 and mod f: the run's)
-                    const uint32_t uk = unit30(k);
-                    const uint32_t c = (bm1 + 30u * (tk % kWheelM) + uk) % kWheelM * a1001 % kWheelM;
-                    uint32_t r1 = 0, r2 = 0;
-#pragma unroll
-                    for (uint32_t j = 0; j < 8; ++j) {
-                        const uint32_t f = kF[j];
-                        const uint32_t bf = (uint32_t(bp.bres[j]) + 30u * (b0 % f)) % f;
-                        const uint32_t q = (bf + 30u * (tk % f) + uk) % f;
-                        const uint32_t rho = q * af[j] % f;
-                        if (j < 4) r1 |= rho << (8 * j);
-                        else r2 |= rho << (8 * (j - 4));
-                    }
-                    large_walk(bp.map + size_t(k) * wpc + (b0 >> 5), nblk, tk, p, c, r1, r2, s_wheel);
+        for (uint32_t jj = 0; jj < 8; ++jj) af[jj] = s_invf[kFo[jj] + 30u * (p % kF[jj]) % kF[jj]];
+        for (uint32_t ri = 0; ri < nrun; ++ri) {
+            const BatchParams &bp = d.runs[ri];
+            if (i < bp.n_mid || i >= bp.n_hl) continue;
+            // run 0's window (the plain form's per-segment launches):
+            // bits [b0, b1), b0 a multiple of 32, as a run of its own
+            const uint32_t w0 = ri ? 0u : d.h->win_b0, w1 = ri ? bp.nblk : min(bp.nblk, d.h->win_b1);
+            if (w0 >= w1) continue;
+            const uint64_t base = bp.base + 30ull * w0;
+            const uint32_t nblk = w1 - w0;
+            const uint32_t r = mod_u64(base, p, rp);
+            // t_k = -(base + u_k) / 30 mod p = tb - c_k, tb = -base / 30
+            const uint32_t tb = mod_below(uint64_t(r ? p - r : 0) * iv, p, rp);
+            uint32_t tk = tb >= ck ? tb - ck : tb + (p - ck);
+            if (uint64_t(p) * p > base) {  // only near the bottom of the range: q >= p^2
+                const uint64_t pp = uint64_t(p) * p;
+                const uint64_t q = base + 30ull * tk + uk;
+                if (q < pp) {
+                    const uint64_t tmin = (pp - base - uk + 29) / 30;
+                    const uint64_t tt = tk + (tmin - tk + p - 1) / p * p;
+                    tk = tt < nblk ? uint32_t(tt) : kNone;
                 }
             }
+            if (tk >= nblk) continue;
+            // m0 = q0 / p with q0 = base + 30 tk + u_k, so m0 / 30 = q0 (30 p)^-1
+            // mod 1001 and mod f (the run base's residues, moved to the window)
+            const uint32_t bm1 = (bp.bm1 + 30u * (w0 % kWheelM)) % kWheelM;
+            const uint32_t c = (bm1 + 30u * (tk % kWheelM) + uk) % kWheelM * a1001 % kWheelM;
+            uint32_t r1 = 0, r2 = 0;
+#pragma unroll
+            for (uint32_t jj = 0; jj < 8; ++jj) {
+                const uint32_t f = kF[jj];
+                const uint32_t bf = (uint32_t(bp.bres[jj]) + 30u * (w0 % f)) % f;
+                const uint32_t q = (bf + 30u * (tk % f) + uk) % f;
+                const uint32_t rho = q * af[jj] % f;
+                if (jj < 4) r1 |= rho << (8 * jj);
+                else r2 |= rho << (8 * (jj - 4));
+            }
+            large_walk(bp.map + size_t(k) * bp.wpc + (w0 >> 5), nblk, tk, p, c, r1, r2, s_wheel);
         }
     }
 }
