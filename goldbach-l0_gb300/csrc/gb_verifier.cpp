@@ -21,9 +21,10 @@
 //     GB_STATS_STATE / GB_STATS_LOG (goldbach_stats.state / .log), the ridge
 //     store, records file, live snapshot and hook (GB_RIDGE, GB_RIDGE_FILE,
 //     GB_RECORDS_FILE, GB_STATS_LIVE, GB_RECORD_HOOK) and GB_RIDGE_MIN;
-//   - the batched form's tuned knobs (segments per batch up to 128, tile
-//     2^20 bits, hit lists from 2^21 through a 96 GB multiplier table, 16
-//     funnels of which 3 on every word) are this implementation's defaults;
+//   - the batched form's tuned knobs (segments per batch up to 128, tiles
+//     of 1,835,008 bits, hit lists from 2^21 through a 96 GB multiplier
+//     table, 16 funnels of which 3 on every word) are this implementation's
+//     defaults;
 //   - it throws std::runtime_error on any failure, as the reference, and the
 //     statistics files are written only after the run passed.
 #include "../../include/gb_verifier.hpp"
@@ -159,6 +160,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, const std::string &spv_p
     cfg.p_mid = p_mid;
     cfg.mtab_max_gb = 96;
     cfg.tile_log2 = 20;
+    cfg.tile_bits = 1835008;
     cfg.plan_funnels = 16;
     cfg.verify_funnels = 3;
     cfg.sample_every = sample;
