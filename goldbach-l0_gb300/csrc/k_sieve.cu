@@ -166,6 +166,26 @@ __device__ __forceinline__ uint32_t stage_tile_bin(uint32_t *stg, uint64_t *bar,
     return staged;
 }
 
+// Clears bit b of the shared-memory tile s: ~(1 << (b mod 32)) as one
+// funnel-shift rotation of ~1.
+__device__ __forceinline__ void clear_bit(uint32_t *s, uint32_t b)
+{
+    atomicAnd(&s[b >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, b));
+}
+
+// Clears bits b, b + st, b + 2 st, ... below tl (b < tl + st, tl + 4 st < 2^32):
+// four marks per bound check.
+__device__ __forceinline__ void clear_stride(uint32_t *s, uint32_t b, uint32_t st, uint32_t tl)
+{
+    for (; b + 3u * st < tl; b += 4u * st) {
+        clear_bit(s, b);
+        clear_bit(s, b + st);
+        clear_bit(s, b + 2u * st);
+        clear_bit(s, b + 3u * st);
+    }
+    for (; b < tl; b += st) clear_bit(s, b);
+}
+
 // Sieves bits [t0, t0 + tl) of class array k of a run in shared memory s
 // (the group patterns already in pat) and stores them: tile ti of the class
 // array, tb bits per tile (the buffer s holds tb bits), tl <= tb a multiple
@@ -233,7 +253,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
         const uint32_t p = bp.primes[i];
         const uint32_t l = local_start(xk[i], t0, p, bp.magic[i], tl);
         if (l >= tl) continue;
-        for (uint32_t b = l + lane * p; b < tl; b += 32 * p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+        clear_stride(s, l + lane * p, 32u * p, tl);
     }
     if constexpr (kVec4) {
         // the rest: four consecutive primes per thread and round, their
@@ -253,7 +273,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
                 if (i + u < i_lo) continue;
                 const uint32_t p = pv[u];
                 const uint32_t l = local_start(x4[u], t0, p, mv[u], tl);
-                for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+                if (l < tl) clear_stride(s, l, p, tl);
             }
         }
     } else {
@@ -277,7 +297,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
                 mn = __ldg(mg + j);
             }
             const uint32_t l = local_start(x, t0, p, m, tl);
-            for (uint32_t b = l; b < tl; b += p) atomicAnd(&s[b >> 5], ~(1u << (b & 31)));
+            if (l < tl) clear_stride(s, l, p, tl);
             i = j;
             p = pn;
             x = xn;
@@ -301,10 +321,10 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
             for (uint32_t i = tid; ok && 4 * i < staged; i += bs) {
                 const uint4 v = v4[i];
                 const uint32_t at = 4 * i;
-                atomicAnd(&s[min(v.x, omax) >> 5], ~(1u << (v.x & 31)));
-                if (at + 1 < staged) atomicAnd(&s[min(v.y, omax) >> 5], ~(1u << (v.y & 31)));
-                if (at + 2 < staged) atomicAnd(&s[min(v.z, omax) >> 5], ~(1u << (v.z & 31)));
-                if (at + 3 < staged) atomicAnd(&s[min(v.w, omax) >> 5], ~(1u << (v.w & 31)));
+                atomicAnd(&s[min(v.x, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v.x));
+                if (at + 1 < staged) atomicAnd(&s[min(v.y, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v.y));
+                if (at + 2 < staged) atomicAnd(&s[min(v.z, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v.z));
+                if (at + 3 < staged) atomicAnd(&s[min(v.w, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v.w));
             }
         }
         if (n > cap) {
@@ -321,10 +341,10 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 #pragma unroll
                 for (uint32_t u = 0; u < 4; ++u) {
                     const uint32_t at = 4 * (i + u * bs);
-                    if (at < m) atomicAnd(&s[min(v[u].x, omax) >> 5], ~(1u << (v[u].x & 31)));
-                    if (at + 1 < m) atomicAnd(&s[min(v[u].y, omax) >> 5], ~(1u << (v[u].y & 31)));
-                    if (at + 2 < m) atomicAnd(&s[min(v[u].z, omax) >> 5], ~(1u << (v[u].z & 31)));
-                    if (at + 3 < m) atomicAnd(&s[min(v[u].w, omax) >> 5], ~(1u << (v[u].w & 31)));
+                    if (at < m) atomicAnd(&s[min(v[u].x, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].x));
+                    if (at + 1 < m) atomicAnd(&s[min(v[u].y, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].y));
+                    if (at + 2 < m) atomicAnd(&s[min(v[u].z, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].z));
+                    if (at + 3 < m) atomicAnd(&s[min(v[u].w, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].w));
                 }
             }
         }
@@ -343,10 +363,10 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
 #pragma unroll
             for (uint32_t u = 0; u < 4; ++u) {
                 const uint32_t at = 4 * (i + u * bs);
-                if (at < n) atomicAnd(&s[min(v[u].x, omax) >> 5], ~(1u << (v[u].x & 31)));
-                if (at + 1 < n) atomicAnd(&s[min(v[u].y, omax) >> 5], ~(1u << (v[u].y & 31)));
-                if (at + 2 < n) atomicAnd(&s[min(v[u].z, omax) >> 5], ~(1u << (v[u].z & 31)));
-                if (at + 3 < n) atomicAnd(&s[min(v[u].w, omax) >> 5], ~(1u << (v[u].w & 31)));
+                if (at < n) atomicAnd(&s[min(v[u].x, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].x));
+                if (at + 1 < n) atomicAnd(&s[min(v[u].y, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].y));
+                if (at + 2 < n) atomicAnd(&s[min(v[u].z, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].z));
+                if (at + 3 < n) atomicAnd(&s[min(v[u].w, omax) >> 5], __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v[u].w));
             }
         }
     }
