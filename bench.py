@@ -331,8 +331,16 @@ def log_uniform(rnd, lo, hi):
     return math.exp(rnd.uniform(math.log(lo), math.log(hi)))
 
 
-def windows_leg(gbc, n=256, seed=7):
-    """Batched uneven windows against the same windows one at a time."""
+def sieve_knobs(knobs):
+    """The sieve knobs of a knob set (tile size, split, table budget, verify
+    plan), without its batch shape."""
+    keep = ("tile_log2", "tile_bits", "p_mid", "mtab_max_gb", "plan_funnels", "verify_funnels")
+    return {k: v for k, v in (knobs or {}).items() if k in keep and v}
+
+
+def windows_leg(gbc, n=256, seed=7, knobs=None):
+    """Batched uneven windows against the same windows one at a time; knobs:
+    the sieve knobs of the tuning record (the batch shape stays 16 segments)."""
     rnd = random.Random(seed)
     wins = []
     for _ in range(n):
@@ -341,7 +349,7 @@ def windows_leg(gbc, n=256, seed=7):
         wins.append((a, a + w))
     limit = max(b for _, b in wins)
     evens = sum((b - a) // 2 + 1 for a, b in wins)
-    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3) as ctx:
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3, **sieve_knobs(knobs)) as ctx:
         ctx.prepare(min(a for a, _ in wins), limit)
         ctx.verify_windows(wins[:4])                               # warm-up: graphs
         t0 = time.perf_counter()
@@ -361,7 +369,7 @@ def windows_leg(gbc, n=256, seed=7):
                       f"p(n) of every even, 16 segments / 16 runs per batch, 3 slots"}
 
 
-def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64):
+def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64, knobs=None):
     """Poisson arrivals into the serving loop; latency = submission to
     completion of each window."""
     rnd = random.Random(seed)
@@ -375,7 +383,7 @@ def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64):
         reqs.append((t, a, a + max(w, 2)))
     limit = max(b for _, _, b in reqs)
     evens = sum((b - a) // 2 + 1 for _, a, b in reqs)
-    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=4) as ctx:
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=4, **sieve_knobs(knobs)) as ctx:
         with gbc.Server(ctx, hbm_budget=150 * 10**9, lo=10**10, hi=limit) as srv:
             warm = [srv.submit(a, b) for _, a, b in reqs[:16]]      # warm-up: graphs of every slot
             for tk in warm:
@@ -718,14 +726,14 @@ def run_gb300(args, rep):
         out["batched_over_plain"] = {"device": value / out["plain"]["value"],
                                      "e2e": e2e / out["plain"]["e2e"]["value"]}
     if args.windows:
-        out["windows"] = windows_leg(gbc, args.windows)
+        out["windows"] = windows_leg(gbc, args.windows, knobs=knobs)
     if args.serve_seconds > 0:
-        out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate)
+        out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate, knobs=knobs)
         # the same loop under load: continuous batching as the request rate grows
         sweep = [float(x) for x in args.serve_sweep.split(",") if x.strip()]
         if sweep:
             out["serving_sweep"] = [
-                {k: v for k, v in serving_leg(gbc, args.sweep_seconds, r, check=16).items() if k != "config"}
+                {k: v for k, v in serving_leg(gbc, args.sweep_seconds, r, check=16, knobs=knobs).items() if k != "config"}
                 for r in sweep]
     if args.sparse_segments:
         out["sparse"] = sparse_leg(gbc, args.sparse_segments, args.sparse_dlt_log2)

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
     __shared__ uint32_t s_hist[GBC_NCAND];
     __shared__ uint32_t s_first[GBC_NCAND];
     __shared__ uint32_t s_win[kCheckWarps][8 * kWin];
-    __shared__ uint32_t s_dmin, s_dmax;
+    __shared__ uint32_t s_dmin, s_dmax, s_cridge;
 
     __shared__ uint32_t s_vb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
         if (tid == 0) {
             s_dmin = kNone;
             s_dmax = 0;
+            s_cridge = ncand;  // the first candidate with p >= ridge_min (ascending list)
         }
         __syncthreads();
         // q = n0 + 30 t - p = base + 30 (D + t) + u: D is the bit of the
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
             const uint32_t dd = uint32_t((n0 - base - p - u) / 30) - dlo;
             // word offset of the window in the warp's staging area | shift << 16
             s_ent[c] = (class_of(u) * kWin + (dd >> 5)) | ((dd & 31) << 16);
+            if (p >= ct.ridge_min) atomicMin(&s_cridge, c);
             s_p[c] = uint16_t(p);
             s_ci[c] = uint16_t(ci);
             s_hist[c] = 0;
@@ -137,6 +139,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
         __syncthreads();
 
         const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
+        const uint32_t c_ridge = s_cridge;
         uint32_t *win = s_win[warp];
         for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps) {
             const uint32_t J = ch * 64;
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
                     write_pn(pn, idx0, jA, hA, s_p[c]);
                     write_pn(pn, idx0, jB, hB, s_p[c]);
                 }
-                if (s_p[c] >= ct.ridge_min) {
+                if (c >= c_ridge) {
                     for (uint32_t h = hA; h; h &= h - 1u)
                         append_ridge(res, n0 + 30ull * (32ull * jA + __ffs(h) - 1u), s_p[c]);
                     for (uint32_t h = hB; h; h &= h - 1u)
@@ -186,10 +189,11 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
                 const uint32_t hA1 = uA & a1, hB1 = uB & b1;
                 uA ^= hA1;
                 uB ^= hB1;
-                const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
-                const uint32_t cnt1 = __reduce_add_sync(~0u, __popc(hA1) + __popc(hB1));
-                if (cnt0) record(c, hA0, hB0, cnt0);
-                if (cnt1) record(c + 1, hA1, hB1, cnt1);
+                // both candidates' hit counts in one reduction (each < 2^12)
+                const uint32_t cnt = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0) +
+                                                                ((__popc(hA1) + __popc(hB1)) << 16));
+                if (cnt & 0xFFFFu) record(c, hA0, hB0, cnt & 0xFFFFu);
+                if (cnt >> 16) record(c + 1, hA1, hB1, cnt >> 16);
             }
             if (c < ncand && __any_sync(~0u, uA | uB)) {
                 const uint32_t e0 = s_ent[c];

@@ -58,7 +58,8 @@ __device__ __forceinline__ uint32_t mod_below(uint64_t x, uint32_t p, float rp)
 // x mod p for any 64-bit x (two base-2^32 digits)
 __device__ __forceinline__ uint32_t mod_u64(uint64_t x, uint32_t p, float rp)
 {
-    const uint32_t r = mod_below(uint32_t(x >> 32), p, rp);
+    const uint32_t hi = uint32_t(x >> 32);
+    const uint32_t r = hi < p ? hi : mod_below(hi, p, rp);
     return mod_below((uint64_t(r) << 32) | uint32_t(x), p, rp);
 }
 
@@ -620,7 +621,7 @@ __global__ void __launch_bounds__(256) k_large(BatchDesc d)
 __device__ __forceinline__ uint64_t divmod_u64(uint64_t x, uint32_t p, float rp, uint32_t pinv, uint32_t &rem)
 {
     const uint32_t hi = uint32_t(x >> 32), lo = uint32_t(x);
-    const uint32_t rh = mod_below(hi, p, rp);
+    const uint32_t rh = hi < p ? hi : mod_below(hi, p, rp);
     const uint32_t qh = (hi - rh) * pinv;
     const uint64_t x2 = (uint64_t(rh) << 32) | lo;
     rem = mod_below(x2, p, rp);
@@ -699,7 +700,11 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
             // second quotient from the first and a division of r0 + span < 2^37
             uint32_t r0;
             const uint64_t qb = divmod_u64(base, p, rp, pinv, r0);
-            const uint64_t x = uint64_t(r0) + (30ull * bp.nblk - 1);
+            const uint64_t span = 30ull * bp.nblk - 1;
+            // a run narrower than p (most pairs of a batch of short windows)
+            // holds a multiple of p only if r0 is 0 or above p - span
+            if (span < p && r0 && p - r0 > span) continue;
+            const uint64_t x = uint64_t(r0) + span;
             const uint32_t r1 = mod_below(x, p, rp);
             const uint64_t mlo = qb + (r0 ? 1 : 0), mhi = qb + uint32_t(x - r1) * pinv;
             if (mhi < mlo) continue;
