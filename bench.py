@@ -338,9 +338,12 @@ def sieve_knobs(knobs):
     return {k: v for k, v in (knobs or {}).items() if k in keep and v}
 
 
-def windows_leg(gbc, n=256, seed=7, knobs=None):
+def windows_leg(gbc, n=256, seed=7, knobs=None, sample_every=0):
     """Batched uneven windows against the same windows one at a time; knobs:
-    the sieve knobs of the tuning record (the batch shape stays 16 segments)."""
+    the sieve knobs of the tuning record (the batch shape stays 16 segments);
+    sample_every 0: p(n) of every even (the campaign statistics' sampling
+    of a window's first segment), gbc.SAMPLE_NONE: the funnel verify + exact
+    tail everywhere (largest p(n), prime / twin counts, gaps)."""
     rnd = random.Random(seed)
     wins = []
     for _ in range(n):
@@ -349,7 +352,8 @@ def windows_leg(gbc, n=256, seed=7, knobs=None):
         wins.append((a, a + w))
     limit = max(b for _, b in wins)
     evens = sum((b - a) // 2 + 1 for a, b in wins)
-    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3, **sieve_knobs(knobs)) as ctx:
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3, sample_every=sample_every,
+                     **sieve_knobs(knobs)) as ctx:
         ctx.prepare(min(a for a, _ in wins), limit)
         ctx.verify_windows(wins[:4])                               # warm-up: graphs
         t0 = time.perf_counter()
@@ -366,7 +370,8 @@ def windows_leg(gbc, n=256, seed=7, knobs=None):
             "batched_over_alone": wall_alone / wall, "bit_exact_vs_alone": f"{same}/{n}",
             "mtab_gb": st.mtab_bytes / 1e9,
             "config": f"{n} windows, widths log-uniform [1e6, 1e10], starts uniform [1e15, 5e18], seed {seed}, "
-                      f"p(n) of every even, 16 segments / 16 runs per batch, 3 slots"}
+                      + ("funnel verify + exact tail (largest p(n), counts, gaps)" if sample_every == gbc.SAMPLE_NONE
+                         else "p(n) of every even") + ", 16 segments / 16 runs per batch, 3 slots"}
 
 
 def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64, knobs=None):
@@ -727,6 +732,7 @@ def run_gb300(args, rep):
                                      "e2e": e2e / out["plain"]["e2e"]["value"]}
     if args.windows:
         out["windows"] = windows_leg(gbc, args.windows, knobs=knobs)
+        out["windows_verify"] = windows_leg(gbc, args.windows, knobs=knobs, sample_every=gbc.SAMPLE_NONE)
     if args.serve_seconds > 0:
         out["serving"] = serving_leg(gbc, args.serve_seconds, args.serve_rate, knobs=knobs)
         # the same loop under load: continuous batching as the request rate grows

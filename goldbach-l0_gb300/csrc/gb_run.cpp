@@ -444,7 +444,7 @@ RangeStats run_range(gbc_ctx *ctx, uint64_t start, uint64_t limit, uint64_t segm
         batches.emplace_back(segs.begin() + i, segs.begin() + std::min(segs.size(), i + max_batch));
         std::vector<uint32_t> f;
         for (size_t j = i; j < std::min(segs.size(), i + max_batch); ++j)
-            f.push_back(sample_every > 1 && j % sample_every && !pn ? GBC_SEG_VERIFY : 0u);
+            f.push_back(pn ? 0u : segment_flag(sample_every, j));
         flags.push_back(f);
     }
     std::vector<gbc_segment_result> out[2];

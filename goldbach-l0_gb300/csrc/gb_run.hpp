@@ -187,6 +187,16 @@ constexpr uint64_t kStatsMinStart = 1000000;
 // (it takes the generic checker), the last one ragged.
 std::vector<std::pair<uint64_t, uint64_t>> plan_segments(uint64_t start, uint64_t limit, uint64_t segment_even);
 
+// The checker of segment j of a run under gbc_config.sample_every: p(n) of
+// every even (0) for every sample_every-th segment from segment 0, the
+// funnel verify + exact tail (GBC_SEG_VERIFY) for the others and for every
+// segment under GBC_SAMPLE_NONE.
+inline uint32_t segment_flag(uint32_t sample_every, size_t j)
+{
+    if (sample_every == GBC_SAMPLE_NONE) return GBC_SEG_VERIFY;
+    return sample_every > 1 && j % sample_every ? GBC_SEG_VERIFY : 0u;
+}
+
 // Runs [start, limit] on an existing context. pn: p(n) of every even, or
 // nullptr. sample_every: every sample_every-th segment (segment 0 always)
 // gets p(n) of every even, the others the funnel verify + exact tail.

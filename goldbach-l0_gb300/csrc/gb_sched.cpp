@@ -29,7 +29,7 @@ Window::Window(uint64_t id_, uint64_t start_, uint64_t limit_, uint64_t segment_
 {
     segs = plan_segments(start, limit, segment_even);
     flags.resize(segs.size());
-    for (size_t j = 0; j < segs.size(); ++j) flags[j] = sample_every > 1 && j % sample_every ? GBC_SEG_VERIFY : 0u;
+    for (size_t j = 0; j < segs.size(); ++j) flags[j] = segment_flag(sample_every, j);
     t_submit = Clock::now();
 }
 

@@ -139,7 +139,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, const std::string &spv_p
     // the knobs, read up front (a malformed one fails before any GPU work)
     const bool stats_on = start >= kStatsMinStart && env_onoff("GB_STATS", true);
     const std::string gaps = env_choice("GB_GAPS", "exact", {"exact", "1", "sampled", "0"});
-    const uint32_t sample = env_u32("GB_STATS_SAMPLE", 256, 1, UINT32_MAX);
+    const uint32_t sample = env_u32("GB_STATS_SAMPLE", 256, 1, UINT32_MAX - 1);  // segment 0 always sampled
     const uint32_t ridge_min = env_u32("GB_RIDGE_MIN", GBC_TAIL_T, 0, UINT32_MAX);
     uint32_t p_mid = kTunedPmid, split_used = 0;
     {

@@ -29,6 +29,7 @@ DEFAULT_SEGMENT = 467_500_000
 MAX_LIMIT = 18446742974197923840
 SEG_NOHASH = 2
 SEG_VERIFY = 4
+SAMPLE_NONE = 0xFFFFFFFF  # Config.sample_every: no segment gets p(n) of every even (GBC_SAMPLE_NONE)
 TEST_STAGING_WAIT = 1
 TEST_RETRY_LIMIT = 2
 MAX_SLOTS = 8

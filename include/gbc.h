@@ -56,6 +56,7 @@ extern "C" {
 #define GBC_SEG_LAST 1u     /* the run's last segment: counts end at limit - 1 */
 #define GBC_SEG_NOHASH 2u   /* skip the class-map hash */
 #define GBC_SEG_VERIFY 4u   /* funnel verify + exact tail instead of p(n) of every even */
+#define GBC_SAMPLE_NONE 0xFFFFFFFFu  /* gbc_config.sample_every: no segment gets p(n) of every even */
 
 /* Context configuration (the knobs of include/config.hpp and the GB_*
  * environment, as fields). Zero means "default" for every field. */
@@ -78,7 +79,10 @@ typedef struct gbc_config {
     uint32_t sample_every;   /* run driver: every sample_every-th segment of a run (segment 0 always)
                                 gets p(n) of every even, the others the funnel verify + exact tail
                                 (GB_STATS_SAMPLE, include/gstats.hpp:62); 0 or 1: every segment
-                                (default) */
+                                (default); GBC_SAMPLE_NONE: no segment (verification without the
+                                p(n) histogram: counts, gaps, ridges, and the largest p(n) where it
+                                reaches the exact tail's bound GBC_TAIL_T, else 0, as the reference's
+                                run_pmax over tail counts alone, include/gstats.hpp:690-701) */
     uint32_t plan_funnels;   /* funnels per class of the verify plan (default 8, at most 32; below 6
                                 the evens a production segment leaves to the exact continuation can
                                 overflow its pending list, and the batch fails closed) */

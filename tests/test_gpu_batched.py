@@ -421,3 +421,24 @@ def test_verify_plan_knobs_same_statistics(plan, first):
         assert [sum(r1.hist[cr][i] for cr in range(15)) for i in tail] == \
             [sum(r2.hist[cr][i] for cr in range(15)) for i in tail]
         assert [r1.first[i] for i in tail] == [r2.first[i] for i in tail]
+
+
+def test_windows_without_sampling_equal_alone_and_the_sampled_run():
+    """sample_every = GBC_SAMPLE_NONE: every segment takes the funnel verify +
+    exact tail. The windows in shared batches give the same line as alone;
+    against the same windows with p(n) of every even, the prime and twin
+    counts are equal, and the largest p(n) too wherever it reaches the exact
+    tail's bound (else it is reported as 0)."""
+    wins = uneven_windows()[:24]
+    limit = max(b for _, b in wins)
+    kw = dict(limit=limit, segment_even=gbc.DEFAULT_SEGMENT, max_batch=16, max_runs=16, nslots=3)
+    with gbc.Context(sample_every=gbc.SAMPLE_NONE, **kw) as c:
+        out, summ = c.verify_windows(wins)
+        assert summ.batches < summ.segments
+        for i in random.Random(10).sample(range(len(wins)), 6):
+            assert out[i][1] == c.verify_range(*wins[i])[1], wins[i]
+    with gbc.Context(**kw) as c:
+        full, _ = c.verify_windows(wins)
+    for (a, b), (r, _), (f, _) in zip(wins, out, full):
+        assert (r.primes, r.twins, r.evens) == (f.primes, f.twins, f.evens), (a, b)
+        assert r.pmax == (f.pmax if f.pmax >= gbc.TAIL_T else 0), (a, b, r.pmax, f.pmax)
