@@ -694,7 +694,7 @@ def run_gb300(args, rep):
                             f"+ exact p(n) >= plan bound; primes, twins, gap walk, map hash on every segment",
                    "l2": f"inputs larger than L2: {args.batch * SEG / 30 / 1e6:.0f} MB of class maps + 393 MB "
                          f"of sieving primes per step",
-                   "tile_log2": cfg.tile_log2, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
+                   "tile_log2": cfg.tile_log2, "tile_bits": cfg.tile_bits, "p_mid": cfg.p_mid, "hl_mode": cfg.hl_mode,
                    "mtab_max_gb": cfg.mtab_max_gb, "plan_funnels": cfg.plan_funnels,
                    "verify_funnels": cfg.verify_funnels,
                    "launch": "graph replay" if cfg.launch_mode != 2 else "direct launches",

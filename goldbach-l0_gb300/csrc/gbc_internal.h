@@ -8,8 +8,8 @@
 
 #include "gbc_common.cuh"
 
-// Slack after the last class array: the checker's and the count kernel's
-// warps read up to 33 words past a class array's last used word.
+// Slack after the last class array: the checker stages up to 160 words past
+// a class array's last used word, the count kernel reads 33.
 constexpr size_t kMapPadBytes = 64 * 1024;
 
 // Byte offsets of the parts of a batch descriptor for nrun_cap runs and

@@ -45,7 +45,10 @@ __device__ __forceinline__ void append_ridge(gbc_segment_result *res, uint64_t n
 
 constexpr int kCheckThreads = 256;
 constexpr int kCheckWarps = kCheckThreads / 32;
-constexpr uint32_t kWin = 80;  // staged words per class array per warp: 64 + span of the candidates + 2
+constexpr uint32_t kWL = 4;                 // words per lane of a warp's chunk
+constexpr uint32_t kChunk = 32 * kWL;       // words per chunk
+constexpr uint32_t kWin = kChunk + 16;      // staged words per class array per warp: chunk + span of the candidates + 2
+constexpr uint32_t kCheckSmem = kCheckWarps * 8 * kWin * 4;  // dynamic shared memory of k_check (bytes)
 
 // valid-even mask of word j of a class with ecount evens
 __device__ __forceinline__ uint32_t word_mask(uint32_t j, uint64_t ecount)
@@ -65,11 +68,16 @@ __device__ __forceinline__ void write_pn(uint16_t *pn, uint32_t idx0, uint32_t j
 }
 
 // Virtual CTA (chunk column bx of vbx, class r) of a sampled segment; each
-// warp takes 64 consecutive words (2048 evens) of class r at a time, stages
-// the 8 class-array windows they read (64 words + the candidates' span) in
-// its own shared memory, and tests the class's useful candidates in
-// ascending order: lane l holds words l and l + 32 of the chunk, so every
-// shared-memory read of the warp is 32 consecutive words.
+// warp takes kChunk consecutive words (32 kWL words, 1024 kWL evens) of class
+// r at a time, stages the 8 class-array windows they read (the chunk + the
+// candidates' span) in its own shared memory, and tests the class's useful
+// candidates in ascending order: lane l holds words l, l + 32, ..., so every
+// shared-memory read of the warp is 32 consecutive words. Four words per
+// lane share each candidate's warp reduction and bookkeeping among 4096
+// evens: against two words per lane, the windows leg's checker took 200.2
+// instead of 239.7 ms and p(n) of every even on production segments ran at
+// 369 instead of 326 G evens/s (one GB300), although a chunk then waits for
+// the slowest of twice as many evens.
 __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTables ct)
 {
     __shared__ uint32_t s_ent[GBC_NCAND];   // word offset | shift << 16
@@ -77,7 +85,7 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
     __shared__ uint16_t s_ci[GBC_NCAND];
     __shared__ uint32_t s_hist[GBC_NCAND];
     __shared__ uint32_t s_first[GBC_NCAND];
-    __shared__ uint32_t s_win[kCheckWarps][8 * kWin];
+    extern __shared__ __align__(16) uint32_t s_chk_win[];  // kCheckWarps x 8 x kWin words
     __shared__ uint32_t s_dmin, s_dmax, s_cridge;
 
     __shared__ uint32_t s_vb;
@@ -121,8 +129,8 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
             atomicMax(&s_dmax, D);
         }
         __syncthreads();
-        const uint32_t dlo = s_dmin & ~31u;                 // staged windows start at word dlo / 32 + J
-        const uint32_t nstage = (s_dmax - dlo) / 32 + 66;   // words per class array (<= kWin)
+        const uint32_t dlo = s_dmin & ~31u;                        // staged windows start at word dlo / 32 + J
+        const uint32_t nstage = (s_dmax - dlo) / 32 + kChunk + 2;  // words per class array (<= kWin)
         for (uint32_t c = tid; c < ncand; c += blockDim.x) {
             const uint32_t ci = ct.list[ct.off[cr] + c];
             const uint32_t p = ct.cand[ci];
@@ -140,82 +148,91 @@ __global__ void __launch_bounds__(kCheckThreads) k_check(BatchDesc d, CheckTable
 
         const uint32_t idx0 = uint32_t((n0 - seg_start) / 2);  // index of n0 among the segment's evens
         const uint32_t c_ridge = s_cridge;
-        uint32_t *win = s_win[warp];
-        for (uint32_t ch = bx * kCheckWarps + warp; ch * 64 < nwords; ch += gx * kCheckWarps) {
-            const uint32_t J = ch * 64;
+        uint32_t *win = s_chk_win + warp * (8 * kWin);
+        for (uint32_t ch = bx * kCheckWarps + warp; ch * kChunk < nwords; ch += gx * kCheckWarps) {
+            const uint32_t J = ch * kChunk;
             // stage the windows: class array k, words dlo / 32 + J + [0, nstage)
             const uint32_t *src = map + (dlo >> 5) + J;
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k)
                 for (uint32_t i = lane; i < nstage; i += 32) win[k * kWin + i] = __ldg(src + size_t(k) * wpc + i);
             __syncwarp();
-            const uint32_t jA = J + lane, jB = J + 32 + lane;
-            uint32_t uA = word_mask(jA, ecount), uB = word_mask(jB, ecount);
+            uint32_t um[kWL];  // evens of word J + 32 w + lane still without a witness
+#pragma unroll
+            for (uint32_t w = 0; w < kWL; ++w) um[w] = word_mask(J + 32 * w + lane, ecount);
             const uint32_t chunk_min = idx0 + 15u * 32u * J;  // smallest even index of this chunk
             const uint32_t *wl = win + lane;
-            // records the hits hA / hB of candidate c (uA / uB already updated)
-            auto record = [&](uint32_t c, uint32_t hA, uint32_t hB, uint32_t cnt) {
+            // records the hits h of candidate c (um already updated)
+            auto record = [&](uint32_t c, const uint32_t (&h)[kWL], uint32_t cnt) {
                 if (s_first[c] > chunk_min) {  // this chunk can still hold the first occurrence
-                    const uint32_t mine = hA ? idx0 + 15u * (32u * jA + __ffs(hA) - 1u)
-                                             : hB ? idx0 + 15u * (32u * jB + __ffs(hB) - 1u) : kNone;
+                    uint32_t mine = kNone;
+#pragma unroll
+                    for (int w = kWL - 1; w >= 0; --w)
+                        if (h[w]) mine = idx0 + 15u * (32u * (J + 32u * w + lane) + __ffs(h[w]) - 1u);
                     const uint32_t mn = __reduce_min_sync(~0u, mine);
                     if (lane == 0) atomicMin(&s_first[c], mn);
                 }
                 if (lane == 0) atomicAdd(&s_hist[c], cnt);
                 if (pn) {
-                    write_pn(pn, idx0, jA, hA, s_p[c]);
-                    write_pn(pn, idx0, jB, hB, s_p[c]);
+#pragma unroll
+                    for (uint32_t w = 0; w < kWL; ++w) write_pn(pn, idx0, J + 32 * w + lane, h[w], s_p[c]);
                 }
                 if (c >= c_ridge) {
-                    for (uint32_t h = hA; h; h &= h - 1u)
-                        append_ridge(res, n0 + 30ull * (32ull * jA + __ffs(h) - 1u), s_p[c]);
-                    for (uint32_t h = hB; h; h &= h - 1u)
-                        append_ridge(res, n0 + 30ull * (32ull * jB + __ffs(h) - 1u), s_p[c]);
+#pragma unroll
+                    for (uint32_t w = 0; w < kWL; ++w)
+                        for (uint32_t x = h[w]; x; x &= x - 1u)
+                            append_ridge(res, n0 + 30ull * (32ull * (J + 32 * w + lane) + __ffs(x) - 1u), s_p[c]);
                 }
+            };
+            auto open = [&]() {
+                uint32_t o = 0;
+#pragma unroll
+                for (uint32_t w = 0; w < kWL; ++w) o |= um[w];
+                return __any_sync(~0u, o);
             };
             uint32_t c = 0;
             // two candidates per trip: their window reads are independent; the
             // second one only tests what the first one left
             for (; c + 1 < ncand; c += 2) {
-                if (!__any_sync(~0u, uA | uB)) break;
+                if (!open()) break;
                 const uint32_t e0 = s_ent[c], e1 = s_ent[c + 1];
                 const uint32_t *w0 = wl + (e0 & 0xFFFF), *w1 = wl + (e1 & 0xFFFF);
                 const uint32_t s0 = e0 >> 16, s1 = e1 >> 16;
-                const uint32_t a0 = __funnelshift_r(w0[0], w0[1], s0), b0 = __funnelshift_r(w0[32], w0[33], s0);
-                const uint32_t a1 = __funnelshift_r(w1[0], w1[1], s1), b1 = __funnelshift_r(w1[32], w1[33], s1);
-                const uint32_t hA0 = uA & a0, hB0 = uB & b0;
-                uA ^= hA0;
-                uB ^= hB0;
-                const uint32_t hA1 = uA & a1, hB1 = uB & b1;
-                uA ^= hA1;
-                uB ^= hB1;
-                // both candidates' hit counts in one reduction (each < 2^12)
-                const uint32_t cnt = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0) +
-                                                                ((__popc(hA1) + __popc(hB1)) << 16));
-                if (cnt & 0xFFFFu) record(c, hA0, hB0, cnt & 0xFFFFu);
-                if (cnt >> 16) record(c + 1, hA1, hB1, cnt >> 16);
+                uint32_t h0[kWL], h1[kWL], n0c = 0, n1c = 0;
+#pragma unroll
+                for (uint32_t w = 0; w < kWL; ++w) {
+                    const uint32_t a0 = __funnelshift_r(w0[32 * w], w0[32 * w + 1], s0);
+                    const uint32_t a1 = __funnelshift_r(w1[32 * w], w1[32 * w + 1], s1);
+                    h0[w] = um[w] & a0;
+                    um[w] ^= h0[w];
+                    h1[w] = um[w] & a1;
+                    um[w] ^= h1[w];
+                    n0c += __popc(h0[w]);
+                    n1c += __popc(h1[w]);
+                }
+                // both candidates' hit counts in one reduction (each <= 32 kWL 32 < 2^16)
+                const uint32_t cnt = __reduce_add_sync(~0u, n0c + (n1c << 16));
+                if (cnt & 0xFFFFu) record(c, h0, cnt & 0xFFFFu);
+                if (cnt >> 16) record(c + 1, h1, cnt >> 16);
             }
-            if (c < ncand && __any_sync(~0u, uA | uB)) {
+            if (c < ncand && open()) {
                 const uint32_t e0 = s_ent[c];
                 const uint32_t *w0 = wl + (e0 & 0xFFFF);
                 const uint32_t s0 = e0 >> 16;
-                const uint32_t hA0 = uA & __funnelshift_r(w0[0], w0[1], s0);
-                const uint32_t hB0 = uB & __funnelshift_r(w0[32], w0[33], s0);
-                uA ^= hA0;
-                uB ^= hB0;
-                const uint32_t cnt0 = __reduce_add_sync(~0u, __popc(hA0) + __popc(hB0));
-                if (cnt0) record(c, hA0, hB0, cnt0);
+                uint32_t h0[kWL], n0c = 0;
+#pragma unroll
+                for (uint32_t w = 0; w < kWL; ++w) {
+                    h0[w] = um[w] & __funnelshift_r(w0[32 * w], w0[32 * w + 1], s0);
+                    um[w] ^= h0[w];
+                    n0c += __popc(h0[w]);
+                }
+                const uint32_t cnt0 = __reduce_add_sync(~0u, n0c);
+                if (cnt0) record(c, h0, cnt0);
             }
-            while (uA) {
-                const uint32_t b = __ffs(uA) - 1u;
-                append_leftover(res, n0 + 30ull * (32ull * jA + b));
-                uA &= uA - 1u;
-            }
-            while (uB) {
-                const uint32_t b = __ffs(uB) - 1u;
-                append_leftover(res, n0 + 30ull * (32ull * jB + b));
-                uB &= uB - 1u;
-            }
+#pragma unroll
+            for (uint32_t w = 0; w < kWL; ++w)
+                for (uint32_t x = um[w]; x; x &= x - 1u)
+                    append_leftover(res, n0 + 30ull * (32ull * (J + 32 * w + lane) + __ffs(x) - 1u));
             __syncwarp();
         }
         __syncthreads();
@@ -747,12 +764,12 @@ void launch_init(const gbk::BatchDesc &d, const Grids &g, cudaStream_t st)
 }
 
 // checker CTAs per class of a segment with the given evens (a virtual grid
-// column count: each warp about six 64-word chunks, to spread the CTA's
-// table setup; at most two per SM)
+// column count: each warp about three chunks of 128 words, to spread the
+// CTA's table setup; at most two per SM)
 uint32_t check_vbx(uint64_t evens, int sm)
 {
     const uint64_t words = (evens / 15 + 32) / 32 + 1;
-    constexpr uint64_t kPerVb = gbk::kCheckWarps * 64 * 6;
+    constexpr uint64_t kPerVb = gbk::kCheckWarps * 384;  // about 384 words (three chunks) per warp
     uint64_t bx = (words + kPerVb - 1) / kPerVb;
     const uint64_t cap = uint64_t(sm) * 2;
     if (bx > cap) bx = cap;
@@ -763,7 +780,7 @@ uint32_t check_vbx(uint64_t evens, int sm)
 void launch_check(const gbk::BatchDesc &d, const gbk::CheckTables &ct, const Grids &g, cudaStream_t st)
 {
     gbk::k_check_low<<<g.sm * 16, 256, 0, st>>>(d, ct.cand, ct.ridge_min);
-    gbk::k_check<<<g.sm * g.check, gbk::kCheckThreads, 0, st>>>(d, ct);
+    gbk::k_check<<<g.sm * g.check, gbk::kCheckThreads, gbk::kCheckSmem, st>>>(d, ct);
 }
 
 void launch_verify(const gbk::BatchDesc &d, const gbk::VerifyTables &vt, const Grids &g, cudaStream_t st)
@@ -780,7 +797,8 @@ void launch_retry(const gbk::BatchDesc &d, uint32_t ridge_min, uint32_t tries, c
 void query_check_grids(Grids &g)
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_check, gbk::kCheckThreads, 0);
+    cudaFuncSetAttribute(gbk::k_check, cudaFuncAttributeMaxDynamicSharedMemorySize, int(gbk::kCheckSmem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbk::k_check, gbk::kCheckThreads, gbk::kCheckSmem);
     g.check = n > 0 ? n : 1;
     n = 0;
     cudaFuncSetAttribute(gbk::k_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, int(gbk::kVerifySmem));
