@@ -262,6 +262,10 @@ static uint32_t tiles_of(uint64_t bits, uint32_t tile_bits) { return uint32_t((b
 // the largest tile the persistent tile kernel takes: 224 KB of shared memory
 constexpr uint32_t kMaxTileBits = 1835008;
 
+// runs a batch's binned hit lists are sized for (the windows' and the
+// serving loop's batches hold 16)
+constexpr uint32_t kHlBinnedRuns = 16;
+
 // overflow marks a binned batch may leave: 2% of a full batch's, at least 2^22
 static uint32_t overflow_cap(double marks)
 {
@@ -294,9 +298,11 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
     s.pend_cap = uint32_t(std::max<uint64_t>(4096, (cfg.segment_even / 2 / 32 + 64) / 16));
     CK(dev_alloc(ctx, &s.pend, size_t(cfg.max_batch) * s.pend_cap * sizeof(uint2)));
     if (ctx->hl_on) {
-        // binned hit lists for a one-run batch of max_batch full segments at
-        // the density of the context's top
-        const uint64_t nblk = uint64_t(ctx->wpc_cap) * 32;
+        // binned hit lists for max_batch full segments at the density of the
+        // context's top, in up to kHlBinnedRuns runs (each run's class array
+        // starts a whole tile of the virtual array: a tile of slack per run;
+        // batches of more runs, or that do not fit, clear their marks directly)
+        const uint64_t nblk = uint64_t(ctx->wpc_cap) * 32 + uint64_t(kHlBinnedRuns) * ctx->tile_bits;
         uint32_t rlog, nreg;
         hl_regions(nblk, rlog, nreg);
         const uint32_t ctas = uint32_t(ctx->grids.sm) * uint32_t(ctx->grids.hitlist);
@@ -305,8 +311,8 @@ static int slot_alloc(gbc_ctx *ctx, Slot &s)
         s.hl_buf_words = size_t(ctas) * 8 * nreg * hl_quota(marks / (8.0 * double(nblk)), nblk, rlog, ctas);
         CK(dev_alloc(ctx, &s.hl_buf, std::max<size_t>(s.hl_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.hl_cnt, size_t(ctas) * gbk::kHlMaxBins * 4));
-        // tile bins: the tiles of a class array of wpc_cap words
-        s.tb_cnt_words = size_t(8) * tiles_of(uint64_t(ctx->wpc_cap) * 32, ctx->tile_bits);
+        // tile bins: the tiles of a class array of wpc_cap words, and a tile per further run
+        s.tb_cnt_words = size_t(8) * (tiles_of(uint64_t(ctx->wpc_cap) * 32, ctx->tile_bits) + kHlBinnedRuns);
         s.tb_buf_words = s.tb_cnt_words * tb_capacity(marks / (8.0 * double(nblk)), ctx->tile_bits);
         CK(dev_alloc(ctx, &s.tb_buf, std::max<size_t>(s.tb_buf_words, 1) * 4));
         CK(dev_alloc(ctx, &s.tb_cnt, std::max<size_t>(s.tb_cnt_words, 1) * 4));
@@ -769,6 +775,8 @@ static void plan_run(const gbc_ctx *ctx, gbk::BatchParams &bp, uint64_t s0, uint
     bp.nblk = uint32_t(nblk);
     bp.wpc = uint32_t(run_wpc(nblk));
     bp.tiles_pc = tiles_of(uint64_t(bp.wpc) * 32, ctx->tile_bits);
+    bp.tb_vt0 = 0;
+    bp.tb_tiles = bp.tiles_pc;
     bp.tile_log2 = ctx->cfg.tile_log2;
     bp.tile_bits = ctx->tile_bits;
     bp.tile_rcp = uint32_t(((uint64_t(1) << 32) + ctx->tile_bits - 1) / ctx->tile_bits);
@@ -927,38 +935,55 @@ static int plan_batch(gbc_ctx *ctx, Slot &s, const uint64_t *b, const uint32_t *
     }
     img.h->nrun = nrun;
     img.h->nseg = uint32_t(nseg);
-    // a batch of one hit-listed run: marks binned by map region, then by tile
-    if (nrun == 1 && s.hl_buf && img.runs[0].n_hl < img.runs[0].n_all) {
-        gbk::BatchParams &bp = img.runs[0];
+    // a batch with hit-listed runs: marks binned by region of the virtual
+    // class array (the runs end to end, each from a whole tile), then by tile
+    bool any_hl = false;
+    for (uint32_t r = 0; r < nrun; ++r) any_hl |= img.runs[r].n_hl < img.runs[r].n_all;
+    if (s.hl_buf && any_hl) {
+        uint64_t vt = 0;        // virtual tiles per class
+        double density = 0.0;   // marks per class bit, the densest run's
+        for (uint32_t r = 0; r < nrun; ++r) {
+            const gbk::BatchParams &bp = img.runs[r];
+            vt += bp.tiles_pc;
+            if (bp.n_hl < bp.n_all)
+                density = std::max(density, hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
+                                                       double(ctx->primes[bp.n_all - 1])));
+        }
+        const uint64_t vbits = vt * ctx->tile_bits;
         uint32_t rlog, nreg;
-        hl_regions(bp.nblk, rlog, nreg);
+        hl_regions(vbits, rlog, nreg);
         const uint32_t ctas = uint32_t(ctx->grids.sm) * uint32_t(ctx->grids.hitlist), nbin = 8 * nreg;
-        const double marks = 8.0 * double(bp.nblk) *
-                             hl_density(double(bp.qmax), double(ctx->primes[bp.n_hl]),
-                                        double(ctx->primes[bp.n_all - 1]));
         const uint32_t pct = ctx->cfg.hl_cap_pct;
-        const uint32_t quota = uint32_t(std::max<size_t>(
-            32, align_up(size_t(hl_quota(marks / (8.0 * double(bp.nblk)), bp.nblk, rlog, ctas)) * pct / 100, 32)));
-        const size_t tiles = size_t(8) * bp.tiles_pc,
-                     tcap = std::max<size_t>(
-                         32, align_up(tb_capacity(marks / (8.0 * double(bp.nblk)), ctx->tile_bits) * pct / 100, 32));
+        const uint32_t quota = uint32_t(
+            std::max<size_t>(32, align_up(size_t(hl_quota(density, vbits, rlog, ctas)) * pct / 100, 32)));
+        const size_t tiles = size_t(8) * vt,
+                     tcap = std::max<size_t>(32, align_up(tb_capacity(density, ctx->tile_bits) * pct / 100, 32));
         // k_binsort sorts a region's offsets by tile in shared memory: at
-        // most kSortMaxTiles tiles meet a region
+        // most kSortMaxTiles tiles meet a region; virtual bits stay below
+        // 2^31 (tile_of)
         const bool tb_fit = tiles_of(uint64_t(1) << rlog, ctx->tile_bits) + 1 <= gbk::kSortMaxTiles &&
-                            tiles <= s.tb_cnt_words && tiles * tcap <= s.tb_buf_words && tcap < (1ull << 31);
+                            tiles <= s.tb_cnt_words && tiles * tcap <= s.tb_buf_words && tcap < (1ull << 31) &&
+                            vbits < (uint64_t(1) << 31) && nbin <= gbk::kHlMaxBins;
         if (size_t(ctas) * nbin * quota <= s.hl_buf_words && tb_fit) {
-            bp.hl_buf = s.hl_buf;
-            bp.hl_cnt = s.hl_cnt;
-            bp.hl_quota = quota;
-            bp.hl_rlog = rlog;
-            bp.hl_nreg = nreg;
-            bp.hl_ctas = ctas;
-            bp.tb_buf = s.tb_buf;
-            bp.tb_cnt = s.tb_cnt;
-            bp.tb_cap = uint32_t(tcap);
-            bp.ovf_buf = s.ovf_buf;
-            bp.ovf_cnt = s.ovf_cnt;
-            bp.ovf_cap = s.ovf_cap;
+            uint32_t vt0 = 0;
+            for (uint32_t r = 0; r < nrun; ++r) {
+                gbk::BatchParams &bp = img.runs[r];
+                bp.hl_buf = s.hl_buf;
+                bp.hl_cnt = s.hl_cnt;
+                bp.hl_quota = quota;
+                bp.hl_rlog = rlog;
+                bp.hl_nreg = nreg;
+                bp.hl_ctas = ctas;
+                bp.tb_buf = s.tb_buf;
+                bp.tb_cnt = s.tb_cnt;
+                bp.tb_cap = uint32_t(tcap);
+                bp.tb_vt0 = vt0;
+                bp.tb_tiles = uint32_t(vt);
+                bp.ovf_buf = s.ovf_buf;
+                bp.ovf_cnt = s.ovf_cnt;
+                bp.ovf_cap = s.ovf_cap;
+                vt0 += bp.tiles_pc;
+            }
         }
     }
     finish_desc(ctx, img);
@@ -1025,6 +1050,7 @@ static int ensure_mtab(gbc_ctx *ctx, uint64_t need0, uint64_t need1)
         bb.qmax = bb.base + 30ull * bb.nblk;
         bb.wpc = uint32_t(wpc);
         bb.tiles_pc = uint32_t(wpc * 32 / tb);
+        bb.tb_tiles = bb.tiles_pc;
         bb.tile_log2 = ctx->cfg.tile_log2;
         bb.tile_bits = tb;
         bb.tile_rcp = uint32_t(((uint64_t(1) << 32) + tb - 1) / tb);
@@ -1334,7 +1360,7 @@ extern "C" int gbc_collect(gbc_ctx *ctx, int slot, gbc_segment_result *out, int 
     uint32_t berr = 0, bad_words = 0;
     CK(cudaMemcpy(&berr, s.err, 4, cudaMemcpyDeviceToHost));
     if (s.did_selfcheck) CK(cudaMemcpy(&bad_words, s.chk_count, 4, cudaMemcpyDeviceToHost));
-    if (ctx->cfg.hl_cap_pct < 100 && gbk::hl_binned(s.img.runs[0], s.img.h->nrun)) {
+    if (ctx->cfg.hl_cap_pct < 100 && s.img.h->nrun && gbk::hl_binned(s.img.runs[0])) {
         uint32_t ov = 0;
         CK(cudaMemcpy(&ov, s.ovf_cnt, 4, cudaMemcpyDeviceToHost));
         ctx->hl_overflow += ov;

@@ -94,21 +94,26 @@ struct BatchParams {
     uint64_t m0, m1;          // the table covers m in [m0, m1]
     uint32_t bm1;             // base mod 1001
     uint8_t bres[8];          // base mod 17, 19, 23, 29, 31, 37, 41, 43
-    // binned hit lists (a batch of one run, hl_quota and tb_cap both set):
-    // the harvest files each mark's offset in its (harvest CTA, region bin)
-    // quota, bin = class * hl_nreg + (t >> hl_rlog); k_binsort moves them to
-    // one bin per tile; the tile kernel clears its tile's marks in shared
-    // memory before storing the tile. Marks beyond a quota or a tile bin's
-    // capacity go to the overflow list, cleared after the tiles. Otherwise
-    // the harvest clears its marks directly, after the tiles.
+    // binned hit lists (hl_quota and tb_cap both set, in every run of the
+    // batch): the runs' class arrays are laid end to end, each from a whole
+    // tile, as one virtual array per class (run r's bit t is virtual bit
+    // tb_vt0 * tile_bits + t, below 2^31); the harvest files each mark's
+    // virtual offset in its (harvest CTA, region bin) quota, bin = class *
+    // hl_nreg + (v >> hl_rlog); k_binsort moves them to one bin per virtual
+    // tile; the tile kernel clears its tile's marks in shared memory before
+    // storing the tile. Marks beyond a quota or a tile bin's capacity go to
+    // the overflow list, cleared after the tiles. Otherwise the harvest
+    // clears its marks directly, after the tiles.
     uint32_t *hl_buf;         // hl_ctas * hl_nbin * hl_quota offsets
     uint32_t *hl_cnt;         // hl_ctas * hl_nbin counts (capped at the quota when read)
     uint32_t hl_quota, hl_rlog, hl_nreg, hl_ctas;
-    uint32_t *tb_buf;         // 8 * tiles_pc tile bins of tb_cap offsets within the tile
-    uint32_t *tb_cnt;         // 8 * tiles_pc counts (capped at tb_cap when read)
+    uint32_t *tb_buf;         // 8 * tb_tiles tile bins of tb_cap offsets within the tile
+    uint32_t *tb_cnt;         // 8 * tb_tiles counts (capped at tb_cap when read)
     uint32_t tb_cap;          // multiple of 32
+    uint32_t tb_vt0;          // the run's first virtual tile (0 for a one-run batch)
+    uint32_t tb_tiles;        // virtual tiles per class (the batch's tiles_pc summed)
     uint32_t ovf_cap;
-    uint2 *ovf_buf;           // (class, bit) of each overflow mark
+    uint2 *ovf_buf;           // (class, virtual bit) of each overflow mark
     uint32_t *ovf_cnt;
     uint32_t spin0;           // try_wait rounds of the first wait on a tile bin's bulk copies (kStageSpin)
 };
@@ -126,10 +131,10 @@ __host__ __device__ __forceinline__ uint32_t tile_of(uint32_t t, uint32_t tile_b
     return q;
 }
 
-// a one-run batch whose hit lists go through the tile bins
-__host__ __device__ __forceinline__ bool hl_binned(const BatchParams &bp, uint32_t nrun)
+// a batch whose hit lists go through the tile bins (set in every run of it)
+__host__ __device__ __forceinline__ bool hl_binned(const BatchParams &bp0)
 {
-    return nrun == 1 && bp.hl_quota != 0 && bp.tb_cap != 0;
+    return bp0.hl_quota != 0 && bp0.tb_cap != 0;
 }
 
 struct GroupInfo {

@@ -182,6 +182,7 @@ extern "C" int gbc_class_map_noalloc(uint64_t q_lo, uint64_t q_hi, const uint32_
     const uint64_t tiles = (nblk + 64 + tb - 1) / tb;
     bp.nblk = uint32_t(nblk);
     bp.tiles_pc = uint32_t(tiles);
+    bp.tb_tiles = bp.tiles_pc;
     bp.wpc = uint32_t(tiles * tw);
     if (base_out) *base_out = bp.base;
     if (nblk_out) *nblk_out = bp.nblk;

@@ -330,7 +330,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
         }
         if (n > cap) {
             // the rest from L2, four groups of four per thread in flight
-            const uint32_t tile = k * bp.tiles_pc + ti, m = n - cap;
+            const uint32_t tile = k * bp.tb_tiles + bp.tb_vt0 + ti, m = n - cap;
             const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap + cap);
             for (uint32_t i = tid; 4 * i < m; i += 4 * bs) {
                 uint4 v[4];
@@ -350,7 +350,7 @@ __device__ __forceinline__ void tile_body(const BatchParams &bp, const GroupInfo
             }
         }
     } else if (bp.tb_cap && bp.hl_quota) {
-        const uint32_t tile = k * bp.tiles_pc + ti;
+        const uint32_t tile = k * bp.tb_tiles + bp.tb_vt0 + ti;
         const uint32_t n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
         const uint4 *e = reinterpret_cast<const uint4 *>(bp.tb_buf + size_t(tile) * bp.tb_cap);
         // four groups of four per thread in flight before their marks
@@ -410,13 +410,13 @@ __global__ void __launch_bounds__(1024, 1) k_tile(BatchDesc d, GroupInfo gi, uin
         const BatchParams &bp = d.runs[r];
         // items tile-major within a run: a tile's eight classes side by side,
         // so the tiles of one segment are one range of items
-        const uint32_t local = j - __ldg(d.tile_pref + r), tpc = bp.tiles_pc;
+        const uint32_t local = j - __ldg(d.tile_pref + r);
         const uint32_t k = local & 7u, ti = local >> 3, t0 = ti * tb;
         const uint32_t tl = min(tb, bp.wpc * 32 - t0);
         if (threadIdx.x == 0) {
             uint32_t n = 0;
             if (bp.tb_cap && bp.hl_quota) {
-                const uint32_t tile = k * tpc + ti;
+                const uint32_t tile = k * bp.tb_tiles + bp.tb_vt0 + ti;
                 n = min(__ldcg(bp.tb_cnt + tile), bp.tb_cap);
                 stage_tile_bin(stg, &s_bar, bp.tb_buf + size_t(tile) * bp.tb_cap, n, cap);
             }
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
 {
     const uint32_t nrun = d.h->nrun;
     if (!nrun) return;
-    const bool binned = hl_binned(d.runs[0], nrun);
+    const bool binned = hl_binned(d.runs[0]);
     if (binned == (direct != 0)) return;
     // per (class of p, class of m): the class kq of q = p m, its residue
     // u_kq and u_m, as kq | u_kq << 8 | u_m << 16; the class of a residue
@@ -716,6 +716,7 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
             uint32_t *map = bp.map;
             const uint32_t wpc = bp.wpc;
             const uint32_t *mtab = bp.mtab;
+            const uint32_t vbase = bp.tb_vt0 * run0.tile_bits;  // the run's first virtual bit (binned)
             // table bytes b0..b1; in the end bytes only the classes inside [mlo, mhi]
             const uint64_t b0 = (mlo - m0) / 30, b1 = (mhi - m0) / 30;
             const uint32_t dl = uint32_t(mlo - m0 - 30 * b0), dh = uint32_t(mhi - m0 - 30 * b1);
@@ -745,10 +746,11 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
                     const uint64_t xq = xw + uint64_t(p) * (30u * (j >> 3) + (e >> 16)) - ((e >> 8) & 0xFFu);
                     const uint32_t t = uint32_t(xq >> 1) * kInv15;
                     if (quota) {
-                        const uint32_t bin = (e & 0xFFu) * nreg + (t >> rlog);
+                        const uint32_t v = vbase + t;
+                        const uint32_t bin = (e & 0xFFu) * nreg + (v >> rlog);
                         const uint32_t pos = atomicAdd(&s_hcnt[bin], 1u);
-                        if (pos < quota) hl_mine[size_t(bin) * quota + pos] = t & ((1u << rlog) - 1u);
-                        else ovf_push(run0, e & 0xFFu, t);
+                        if (pos < quota) hl_mine[size_t(bin) * quota + pos] = v & ((1u << rlog) - 1u);
+                        else ovf_push(run0, e & 0xFFu, v);
                         continue;
                     }
                     atomicAnd(map + size_t(e & 0xFFu) * wpc + (t >> 5), ~(1u << (t & 31)));
@@ -810,7 +812,7 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
     __shared__ uint32_t s_cnt[kSortMaxTiles], s_start[kSortMaxTiles], s_gbase[kSortMaxTiles];
     __shared__ uint32_t s_wsum[8];
     __shared__ uint32_t s_j;
-    if (!hl_binned(d.runs[0], d.h->nrun)) return;
+    if (!hl_binned(d.runs[0])) return;
     const BatchParams &bp = d.runs[0];
     const uint32_t tid = threadIdx.x, bs = blockDim.x;
     const uint32_t quota = bp.hl_quota, nreg = bp.hl_nreg, nbin = 8 * nreg, ctas = bp.hl_ctas;
@@ -828,8 +830,8 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
         // filled by every region that meets them)
         const uint32_t rb = reg << rlog;
         const uint32_t ti0 = tile_of(rb, tb, rcp);
-        const uint32_t tpr = tile_of(min(rb + ((1u << rlog) - 1u), bp.wpc * 32 - 1), tb, rcp) - ti0 + 1;
-        const uint32_t tile0 = k * bp.tiles_pc + ti0;
+        const uint32_t tpr = tile_of(min(rb + ((1u << rlog) - 1u), bp.tb_tiles * tb - 1), tb, rcp) - ti0 + 1;
+        const uint32_t tile0 = k * bp.tb_tiles + ti0;
         for (uint32_t cs = 0; cs < n; cs += kSortChunk) {
             const uint32_t m = min(n - cs, kSortChunk);
             for (uint32_t t = tid; t < tpr; t += bs) s_cnt[t] = 0;
@@ -882,15 +884,27 @@ __global__ void __launch_bounds__(256, 6) k_binsort(BatchDesc d)
 // The overflow list of a binned batch, cleared after the tiles.
 __global__ void __launch_bounds__(256) k_hl_overflow(BatchDesc d)
 {
-    if (!hl_binned(d.runs[0], d.h->nrun)) return;
-    const BatchParams &bp = d.runs[0];
-    const uint32_t cnt = *bp.ovf_cnt;
-    if (cnt > bp.ovf_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bp.err, kErrHlOverflow);
-    const uint32_t n = min(cnt, bp.ovf_cap);
-    const uint32_t b0 = d.h->win_b0, b1 = d.h->win_b1;  // the plain form's window (else everything)
+    const uint32_t nrun = d.h->nrun;
+    if (!nrun || !hl_binned(d.runs[0])) return;
+    const BatchParams &bp0 = d.runs[0];
+    const uint32_t cnt = *bp0.ovf_cnt, tb = bp0.tile_bits;
+    if (cnt > bp0.ovf_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bp0.err, kErrHlOverflow);
+    const uint32_t n = min(cnt, bp0.ovf_cap);
+    const uint32_t b0 = d.h->win_b0, b1 = d.h->win_b1;  // the plain form's window of run 0 (else everything)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint2 e = bp.ovf_buf[i];
-        if (e.y >= b0 && e.y < b1) atomicAnd(bp.map + size_t(e.x) * bp.wpc + (e.y >> 5), ~(1u << (e.y & 31)));
+        const uint2 e = bp0.ovf_buf[i];
+        // the run of virtual bit e.y: the last one whose first virtual tile is at or below it
+        const uint32_t vt = e.y / tb;
+        uint32_t lo = 0, hi = nrun - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (d.runs[mid].tb_vt0 <= vt) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchParams &bp = d.runs[lo];
+        const uint32_t t = e.y - bp.tb_vt0 * tb;
+        if (t < bp.nblk && t >= b0 && t < b1)
+            atomicAnd(bp.map + size_t(e.x) * bp.wpc + (t >> 5), ~(1u << (t & 31)));
     }
 }
 

@@ -442,3 +442,31 @@ def test_windows_without_sampling_equal_alone_and_the_sampled_run():
     for (a, b), (r, _), (f, _) in zip(wins, out, full):
         assert (r.primes, r.twins, r.evens) == (f.primes, f.twins, f.evens), (a, b)
         assert r.pmax == (f.pmax if f.pmax >= gbc.TAIL_T else 0), (a, b, r.pmax, f.pmax)
+
+
+def test_runs_hitlist_overflow_selfcheck():
+    """Three hit-listed runs in one batch, their marks binned through one
+    virtual tile-bin array, with the bins at 80% of their sizing: marks take
+    the overflow list, which finds each mark's run; the self-check (the
+    rebuild without hit lists, word for word) passes, and every statistic
+    equals that of the bins at full size."""
+    seg = 467_500_000
+    segs, limits = [], []
+    for h in (10**16, 10**17, 10**18):
+        segs += [(h, h + seg - 2), (h + seg, h + 2 * seg - 2)]
+        limits += [h + 2 * seg - 2] * 2
+    limit = max(limits)
+    flags = [0, gbc.SEG_VERIFY] * 3
+    out = {}
+    for pct in (100, 80):
+        with gbc.Context(limit=limit, segment_even=seg, max_batch=6, max_runs=3, p_mid=1 << 21, mtab_max_gb=96,
+                         hl_mode=1, hl_cap_pct=pct, selfcheck_every=1) as c:
+            c.enqueue_segments(0, segs, limits, flags)
+            res, t = c.collect(0, len(segs))
+            assert t.runs == 3
+            st = c.stats()
+            assert st.selfchecks >= 1
+            out[pct] = (res, st.hl_overflow)
+    assert out[100][1] == 0 and out[80][1] > 0  # the overflow list was used at 80%
+    for r1, r2 in zip(out[100][0], out[80][0]):
+        assert result_fields(r1) == result_fields(r2)
