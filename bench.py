@@ -85,16 +85,16 @@ def peaks():
 
 
 def ncu_counters():
-    """kernel -> (DRAM bytes, warp instructions) per launch from
-    profiles/ncu_counters.txt (one-pass ncu captures of the headline
-    workload; lines "kernel dram_bytes warp_inst note")."""
+    """kernel -> (DRAM bytes, warp instructions or None) per launch from
+    profiles/ncu_counters.txt (lines "kernel dram_bytes warp_inst note";
+    "-" for instructions not measured at this size)."""
     out = {}
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_counters.txt")) as f:
             for ln in f:
                 t = ln.split()
                 if len(t) >= 3 and not ln.startswith("#"):
-                    out[t[0]] = (float(t[1]), float(t[2]))
+                    out[t[0]] = (float(t[1]), None if t[2] == "-" else float(t[2]))
     except OSError:
         pass
     return out
@@ -673,8 +673,9 @@ def run_gb300(args, rep):
         have = [counters[k] for k in kerns if k in counters]
         if have:
             row["ncu_dram_bytes_per_launch"] = sum(c[0] for c in have)
-            row["ncu_warp_inst_per_launch"] = sum(c[1] for c in have)
-            row["issue_frac"] = row["ncu_warp_inst_per_launch"] / (ms / 1e3) / issue_peak if ms > 0 else None
+            if all(c[1] is not None for c in have):
+                row["ncu_warp_inst_per_launch"] = sum(c[1] for c in have)
+                row["issue_frac"] = row["ncu_warp_inst_per_launch"] / (ms / 1e3) / issue_peak if ms > 0 else None
         stage_bw[s_] = row
     dom = max(stage, key=stage.get)                     # the stage with the most device time per step
     kernel = stage_bw[dom]["kernel"]
