@@ -340,7 +340,8 @@ def sieve_knobs(knobs):
 
 def windows_leg(gbc, n=256, seed=7, knobs=None, sample_every=0):
     """Batched uneven windows against the same windows one at a time; knobs:
-    the sieve knobs of the tuning record (the batch shape stays 16 segments);
+    the sieve knobs of the tuning record, batches of up to 64 segments in up
+    to 64 runs (16 per batch: 238 against 255 G evens/s, device time);
     sample_every 0: p(n) of every even (the campaign statistics' sampling
     of a window's first segment), gbc.SAMPLE_NONE: the funnel verify + exact
     tail everywhere (largest p(n), prime / twin counts, gaps)."""
@@ -352,7 +353,7 @@ def windows_leg(gbc, n=256, seed=7, knobs=None, sample_every=0):
         wins.append((a, a + w))
     limit = max(b for _, b in wins)
     evens = sum((b - a) // 2 + 1 for a, b in wins)
-    with gbc.Context(limit=limit, segment_even=SEG, max_batch=16, max_runs=16, nslots=3, sample_every=sample_every,
+    with gbc.Context(limit=limit, segment_even=SEG, max_batch=64, max_runs=64, nslots=3, sample_every=sample_every,
                      **sieve_knobs(knobs)) as ctx:
         ctx.prepare(min(a for a, _ in wins), limit)
         ctx.verify_windows(wins[:4])                               # warm-up: graphs
@@ -371,7 +372,7 @@ def windows_leg(gbc, n=256, seed=7, knobs=None, sample_every=0):
             "mtab_gb": st.mtab_bytes / 1e9,
             "config": f"{n} windows, widths log-uniform [1e6, 1e10], starts uniform [1e15, 5e18], seed {seed}, "
                       + ("funnel verify + exact tail (largest p(n), counts, gaps)" if sample_every == gbc.SAMPLE_NONE
-                         else "p(n) of every even") + ", 16 segments / 16 runs per batch, 3 slots"}
+                         else "p(n) of every even") + ", 64 segments / 64 runs per batch, 3 slots"}
 
 
 def serving_leg(gbc, seconds=60.0, rate=50.0, seed=11, check=64, knobs=None):

@@ -262,9 +262,9 @@ static uint32_t tiles_of(uint64_t bits, uint32_t tile_bits) { return uint32_t((b
 // the largest tile the persistent tile kernel takes: 224 KB of shared memory
 constexpr uint32_t kMaxTileBits = 1835008;
 
-// runs a batch's binned hit lists are sized for (the windows' and the
-// serving loop's batches hold 16)
-constexpr uint32_t kHlBinnedRuns = 16;
+// runs a batch's binned hit lists are sized for (the serving loop's
+// batches hold 16, the windows leg's 64)
+constexpr uint32_t kHlBinnedRuns = 64;
 
 // overflow marks a binned batch may leave: 2% of a full batch's, at least 2^22
 static uint32_t overflow_cap(double marks)
