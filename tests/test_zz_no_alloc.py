@@ -11,8 +11,9 @@ with the map the per-segment path (gbc_enqueue_batch) built for the same q
 range, checks it against the oracle's hash of the primes in the range, and
 checks that every bit past the range is zero. The file is named so pytest
 collects it last: a failure here stops a -x run only after every other test
-has run. The argument checks run on the host before any CUDA call, so they
-are tested without a GPU.
+has run. A third test records the call inside a CUDA graph capture and replays
+it. The argument checks run on the host before any CUDA call, so they are
+tested without a GPU.
 """
 import ctypes as C
 
@@ -108,6 +109,41 @@ def test_noalloc_map_matches_existing_path_twice():
         assert np.array_equal(mine, class_bits(words, wpc, nblk))
         assert map_hash(mine, base) == oracle.map_hash(base, q_hi)
         assert not class_bits(got, nw, 32 * nw)[:, nblk:].any(), "bits past the range must be zero"
+
+
+@pytest.mark.gpu
+def test_noalloc_map_inside_a_captured_graph():
+    """The use the entry point exists for: the call recorded while the
+    caller's stream is being captured (torch.cuda.graph), after one warm
+    call outside the capture; replaying the graph writes the same map as
+    the per-segment path, with every bit past the range zero."""
+    torch = pytest.importorskip("torch")
+    lib = gbc.load()
+    primes = odd_primes_upto(1_650_000)
+    pd = torch.from_numpy(primes.view(np.int32)).to("cuda")
+    a, b, seg = 3 * 10**12, 3 * 10**12 + 3_999_998, 1_000_000
+    base, nblk, wpc, words = existing_map(a, b, seg)
+    q_hi = base + 30 * (nblk - 1) + 29
+    warm = noalloc_map(lib, torch, base, q_hi, C.c_void_p(pd.data_ptr()), len(primes), int(primes[-1]),
+                       C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    nw = warm[2]
+    out = torch.full((8 * nw,), -1, dtype=torch.int32, device="cuda")
+    b_out, n_out, w_out = C.c_uint64(), C.c_uint32(), C.c_uint32()
+    err = C.create_string_buffer(256)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = lib.gbc_class_map_noalloc(base, q_hi, C.c_void_p(pd.data_ptr()), len(primes), int(primes[-1]),
+                                       C.c_void_p(out.data_ptr()), 8 * nw, C.byref(b_out), C.byref(n_out),
+                                       C.byref(w_out), C.c_void_p(torch.cuda.current_stream().cuda_stream), err,
+                                       len(err))
+    assert rc == 0, err.value.decode()
+    out.fill_(-1)  # the replay, not the capture, must write the map
+    g.replay()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint32)
+    assert (b_out.value, n_out.value) == (base, nblk)
+    assert np.array_equal(class_bits(got, nw, nblk), class_bits(words, wpc, nblk))
+    assert not class_bits(got, nw, 32 * nw)[:, nblk:].any(), "bits past the range must be zero"
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits():
