@@ -121,7 +121,7 @@ def test_noalloc_map_inside_a_captured_graph():
     lib = gbc.load()
     primes = odd_primes_upto(1_650_000)
     pd = torch.from_numpy(primes.view(np.int32)).to("cuda")
-    a, b, seg = 3 * 10**12, 3 * 10**12 + 3_999_998, 1_000_000
+    a, b, seg = 2 * 10**12, 2 * 10**12 + 3_999_998, 1_000_000  # primes to 1.65e6 reach sqrt(b)
     base, nblk, wpc, words = existing_map(a, b, seg)
     q_hi = base + 30 * (nblk - 1) + 29
     warm = noalloc_map(lib, torch, base, q_hi, C.c_void_p(pd.data_ptr()), len(primes), int(primes[-1]),
