@@ -176,7 +176,7 @@ void attach_env_outputs(gbc_ctx *ctx);
 StatsCampaign *campaign_of(gbc_ctx *ctx);
 bool stats_gaps_of(gbc_ctx *ctx);
 
-// the version= field of this build's statistics lines and journal rows
+// the version= field of this library's statistics lines and journal rows
 constexpr const char *kVersion = "gb300-1.0";
 
 // runs that start below this keep no campaign statistics (STATS_MIN_START,

@@ -147,7 +147,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, const std::string &spv_p
         if (sieve_split_arg) {
             if (sieve_split_arg >= small.size() || small[sieve_split_arg] < 1024)
                 throw std::runtime_error("sieve split index " + std::to_string(sieve_split_arg) +
-                                         " outside this build's tile range (primes 1024 .. 2^23)");
+                                         " outside this implementation's tile range (primes 1024 .. 2^23)");
             p_mid = small[sieve_split_arg - 1];
         }
         split_used = uint32_t(std::upper_bound(small.begin(), small.end(), p_mid) - small.begin());

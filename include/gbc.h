@@ -450,7 +450,7 @@ uint64_t gbc_pn_exact(uint64_t n);
 /* Attaches campaign statistics to ctx: every run of gbc_verify_range and of
  * gbc_run_slices that passes and starts at >= 1e6 is merged into state and
  * logged in log, and the run's line is its GBSTATS v2 line as logged.
- * version: the lines' version= field (NULL: this build's); gaps = 0 keeps no
+ * version: the lines' version= field (NULL: this library's); gaps = 0 keeps no
  * gap statistics (the reference's GB_GAPS=0). The files are read now: a
  * damaged or incompatible state is GBC_E_STATE, nothing attached. state =
  * NULL detaches. */

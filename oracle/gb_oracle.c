@@ -2,8 +2,8 @@
  * gb_oracle.c -- CPU oracle of the dense Goldbach verify path.
  *
  * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py load or run this file, and only as the checker
- * or the timed CPU baseline. The GPU product path (goldbach-l0_gb300/) never
+ * CPU-baseline leg of bench.py load or run this file, and only to verify
+ * results or as the timed CPU baseline. The GPU product path (goldbach-l0_gb300/) never
  * links it and has no CPU fallback.
  *
  * What it restates (reference paths are relative to the goldbach-l0 project):

@@ -1,7 +1,7 @@
 """ctypes access to the CPU oracle (oracle/gb_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py as the checker or the timed CPU baseline, never
+CPU-baseline leg of bench.py to verify results or as the timed CPU baseline, never
 by the GPU product path.
 """
 import ctypes as C

@@ -1,7 +1,7 @@
 """CPU oracle of the sparse class map (the reference's --sparse path:
 include/sparse.hpp:1-33 geometry, src/sparse.cpp, kernels/sparse.cl).
 
-TEST INFRASTRUCTURE ONLY: used by tests/ as the checker, never by the GPU
+TEST INFRASTRUCTURE ONLY: used by tests/ to verify results, never by the GPU
 product path.
 
 The reference validates its sparse path against an independent CPU sieve of

@@ -1,7 +1,7 @@
 """Ridge store, records file and the CPU re-proof (the reference's
 RidgeTracker store, include/ridge.hpp, and records file + hook,
-include/gstats.hpp:836-868). Host logic only: the oracle's p(n) is the
-checker."""
+include/gstats.hpp:836-868). Host logic only, against the oracle's
+p(n)."""
 import os
 import time
 

@@ -2,7 +2,7 @@
 the checker plan holds exactly the candidates the geometry allows, each once,
 and the device calls fail loudly without a device. Mirrors the reference's
 host tests of its sparse path (tests/host_tests.cpp:473-530 residues and
-first hits, 734-800 plan validation); the oracle is the checker."""
+first hits, 734-800 plan validation), against the oracle."""
 import ctypes as C
 import math
 import os
