@@ -29,7 +29,7 @@ def build_main(tmp_path):
     """tests/cpp/run_gpu_main.cpp against include/gb_verifier.hpp, linked with libgbc.so."""
     gbc.load()
     exe = tmp_path / "run_gpu_main"
-    subprocess.run(["g++", "-std=c++17", "-O2", "-I", INC, MAIN, "-o", str(exe), "-L", PKG, "-lgbc",
+    subprocess.run(["g++", "-std=c++23", "-O2", "-I", INC, MAIN, "-o", str(exe), "-L", PKG, "-lgbc",
                     f"-Wl,-rpath,{PKG}"], check=True)
     return str(exe)
 
@@ -37,7 +37,7 @@ def build_main(tmp_path):
 def test_struct_layouts_equal_the_references(tmp_path):
     want, _ = fixture()
     exe = tmp_path / "probe"
-    subprocess.run(["g++", "-std=c++17", "-Wno-invalid-offsetof", "-I", INC, PROBE, "-o", str(exe)], check=True)
+    subprocess.run(["g++", "-std=c++23", "-Wno-invalid-offsetof", "-I", INC, PROBE, "-o", str(exe)], check=True)
     got = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines()
     assert got == want
 
@@ -45,7 +45,7 @@ def test_struct_layouts_equal_the_references(tmp_path):
 def test_library_exports_the_references_entry_points(tmp_path):
     _, want = fixture()
     obj = tmp_path / "probe.o"
-    subprocess.run(["g++", "-std=c++17", "-Wno-invalid-offsetof", "-DNAME_CALLS", "-I", INC, "-c", PROBE, "-o",
+    subprocess.run(["g++", "-std=c++23", "-Wno-invalid-offsetof", "-DNAME_CALLS", "-I", INC, "-c", PROBE, "-o",
                     str(obj)], check=True)
     nm = subprocess.run(["nm", "-u", str(obj)], check=True, capture_output=True, text=True).stdout
     assert sorted({ln.split()[-1] for ln in nm.splitlines() if "_ZN2gb" in ln}) == want
