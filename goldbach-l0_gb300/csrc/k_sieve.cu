@@ -735,8 +735,12 @@ __global__ void __launch_bounds__(256) k_hitlist(BatchDesc d, uint32_t direct)
             const uint32_t nw = uint32_t(w1 - w0);
             const uint64_t step = 120ull * p;
             uint64_t xw = uint64_t(p) * m0 - base + step * w0;
+            // the next table word loaded before this word's marks (its
+            // latency hidden behind them)
+            uint32_t vnext = __ldg(tw);
             for (uint32_t iw = 0; iw <= nw; ++iw, xw += step) {
-                uint32_t v = __ldg(tw + iw);
+                uint32_t v = vnext;
+                if (iw < nw) vnext = __ldg(tw + iw + 1);
                 if (iw == 0) v &= lo_mask;
                 if (iw == nw) v &= hi_mask;
                 while (v) {
