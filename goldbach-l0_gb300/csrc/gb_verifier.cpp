@@ -22,9 +22,9 @@
 //     store, records file, live snapshot and hook (GB_RIDGE, GB_RIDGE_FILE,
 //     GB_RECORDS_FILE, GB_STATS_LIVE, GB_RECORD_HOOK) and GB_RIDGE_MIN;
 //   - the batched form's tuned knobs (segments per batch up to 128, tiles
-//     of 1,835,008 bits, hit lists from 2^21 through a 96 GB multiplier
-//     table, 16 funnels of which 3 on every word) are this implementation's
-//     defaults;
+//     of 1,835,008 bits, the tile sieve to the same 1,835,008 and hit lists
+//     above it through a 96 GB multiplier table, 16 funnels of which 3 on
+//     every word) are this implementation's defaults;
 //   - it throws std::runtime_error on any failure, as the reference, and the
 //     statistics files are written only after the run passed.
 #include "../../include/gb_verifier.hpp"
@@ -117,9 +117,9 @@ double since(std::chrono::steady_clock::time_point t)
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
 }
 
-constexpr uint32_t kTunedPmid = 1u << 21;   // primes <= 2^21 in the shared-memory tiles
+constexpr uint32_t kTileBits = 1835008;     // bits per shared-memory tile (224 KB)
+constexpr uint32_t kTunedPmid = kTileBits;  // primes up to a tile's span in the shared-memory tiles
 constexpr uint32_t kMaskPrimes = 16;        // 7..67 by whole-word patterns
-constexpr uint32_t kTileBits = 1u << 20;
 
 }  // namespace
 
@@ -160,7 +160,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, const std::string &spv_p
     cfg.p_mid = p_mid;
     cfg.mtab_max_gb = 96;
     cfg.tile_log2 = 20;
-    cfg.tile_bits = 1835008;
+    cfg.tile_bits = kTileBits;
     cfg.plan_funnels = 16;
     cfg.verify_funnels = 3;
     cfg.sample_every = sample;
