@@ -38,7 +38,8 @@ SEG = 467_500_000
 KNOBS = {
     # the tile / hit-list split and the table budget that sets where the hit
     # lists start: one joint knob (a small budget pushes p_hl above p_mid)
-    ("p_mid", "mtab_max_gb"): [(p, g) for p in (1 << 20, 1835008, 1 << 21, 1 << 22, 1 << 23) for g in (16, 24, 48, 96, 160)],
+    ("p_mid", "mtab_max_gb"): [(p, g) for p in (1 << 20, 1638400, 1703936, 1769472, 1835008, 1 << 21, 1 << 22, 1 << 23)
+                               for g in (16, 24, 48, 96, 160)],
     "tile_log2": [19, 20],
     "tile_bits": [0, 1572864, 1835008],  # 0: 2^tile_log2 bits
     "max_batch": [32, 48, 64, 96, 128],

@@ -22,8 +22,8 @@
 //     store, records file, live snapshot and hook (GB_RIDGE, GB_RIDGE_FILE,
 //     GB_RECORDS_FILE, GB_STATS_LIVE, GB_RECORD_HOOK) and GB_RIDGE_MIN;
 //   - the batched form's tuned knobs (segments per batch up to 128, tiles
-//     of 1,835,008 bits, the tile sieve to the same 1,835,008 and hit lists
-//     above it through a 96 GB multiplier table, 16 funnels of which 3 on
+//     of 1,835,008 bits, the tile sieve to 1,703,936 and hit lists above it
+//     through a multiplier table of up to 160 GB, 16 funnels of which 3 on
 //     every word) are this implementation's defaults;
 //   - it throws std::runtime_error on any failure, as the reference, and the
 //     statistics files are written only after the run passed.
@@ -118,7 +118,7 @@ double since(std::chrono::steady_clock::time_point t)
 }
 
 constexpr uint32_t kTileBits = 1835008;     // bits per shared-memory tile (224 KB)
-constexpr uint32_t kTunedPmid = kTileBits;  // primes up to a tile's span in the shared-memory tiles
+constexpr uint32_t kTunedPmid = 1703936;    // primes to 1.625 * 2^20 in the shared-memory tiles (the tuned split)
 constexpr uint32_t kMaskPrimes = 16;        // 7..67 by whole-word patterns
 
 }  // namespace
@@ -158,7 +158,7 @@ RunStats run_gpu(uint64_t limit, uint64_t segment_even, const std::string &spv_p
     cfg.segment_even = seg;
     cfg.max_batch = uint32_t(std::min<size_t>(128, segs.size()));
     cfg.p_mid = p_mid;
-    cfg.mtab_max_gb = 96;
+    cfg.mtab_max_gb = 160;
     cfg.tile_log2 = 20;
     cfg.tile_bits = kTileBits;
     cfg.plan_funnels = 16;
