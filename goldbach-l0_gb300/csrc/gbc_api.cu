@@ -228,9 +228,9 @@ static double hl_density(double qmax, double p_hl, double p_max)
     return std::log(u1 * (L - u0) / (u0 * (L - u1))) / L * 30.0 / 8.0;
 }
 
-// Region bins of a one-run batch: regions of 2^rlog class bits (at least
-// 2^28, so that all of k_hl_apply's CTAs share one region of <= 32 MB of one
-// class at a time), at most kHlMaxBins / 8 per class.
+// Region bins of a binned batch: regions of 2^rlog bits of the virtual class
+// array (at least 2^28: few bins per harvest CTA, so its shared-memory
+// counters cover them), at most kHlMaxBins / 8 per class.
 static void hl_regions(uint64_t nblk, uint32_t &rlog, uint32_t &nreg)
 {
     rlog = 28;
