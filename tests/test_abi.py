@@ -136,3 +136,18 @@ def test_cli_crosscheck_status(tmp_path):
     lines = r.stdout.splitlines()
     assert lines[0].endswith("verified [1000, 2998]") and lines[1].endswith("verified [1000, 1998]")
     assert lines[2].startswith("both:   [1000, 1998] = 500 evens")
+
+
+def test_binding_constants_equal_the_headers():
+    """Every constant the ctypes binding mirrors has the value the header
+    defines (GBC_X in include/gbc.h <-> gbc.X)."""
+    src = open(HEADER).read()
+    defs = {}
+    for name, val in re.findall(r"^#define GBC_(\w+)\s+\(?(-?(?:0x[0-9A-Fa-f]+|\d+))[uUlL]*\)?", src, flags=re.M):
+        defs[name] = int(val, 0)
+    mirrored = ["NCAND", "NCLASS", "GBINS", "TAIL_CAP", "LEFT_CAP", "RIDGE_CAP", "TAIL_T", "DEFAULT_SEGMENT",
+                "MAX_LIMIT", "SEG_NOHASH", "SEG_VERIFY", "SAMPLE_NONE", "TEST_STAGING_WAIT", "TEST_RETRY_LIMIT",
+                "MAX_SLOTS"]
+    for name in mirrored:
+        assert name in defs, name
+        assert getattr(gbc, name) == defs[name], name
