@@ -470,3 +470,23 @@ def test_runs_hitlist_overflow_selfcheck():
     assert out[100][1] == 0 and out[80][1] > 0  # the overflow list was used at 80%
     for r1, r2 in zip(out[100][0], out[80][0]):
         assert result_fields(r1) == result_fields(r2)
+
+
+def test_uneven_windows_in_64_run_batches_against_oracle():
+    """The windows leg's batch shape and knobs (up to 64 segments in up to 64
+    runs, their hit lists binned through one virtual tile-bin array, the
+    tuned tile and split): 48 uneven
+    windows in shared batches; 4 of them (under 2e7 wide) against the
+    oracle's exact sieve, 8 against their runs alone."""
+    wins = uneven_windows()[:48]
+    small = [i for i, (a, b) in enumerate(wins) if b - a < 2 * 10**7]
+    pick = random.Random(12).sample(small, 4)
+    limit = max(b for _, b in wins)
+    with gbc.Context(limit=limit, segment_even=gbc.DEFAULT_SEGMENT, max_batch=64, max_runs=64, nslots=3,
+                     tile_bits=1835008, p_mid=1703936, mtab_max_gb=96) as c:
+        out, summ = c.verify_windows(wins)
+        assert summ.batches < summ.runs  # several runs per batch
+        for i in pick:
+            assert out[i][1] == oracle.stats_line(wins[i][0], wins[i][1], oracle.SIEVE), wins[i]
+        for i in random.Random(13).sample(range(len(wins)), 8):
+            assert out[i][1] == c.verify_range(*wins[i])[1], wins[i]
